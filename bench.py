@@ -1,0 +1,436 @@
+"""Benchmark: RK4 grid-point-steps/s of the NLSE step loop on GB300.
+
+Workload (one bench step = one whole job): the 3D vortex-ring solve, 320^3
+grid, h = 0.3, a = 1, s = -1, harmonic trap (w = 0.02), MSD boundary,
+2SHOC, k = 0.8 x the linear stability limit, 500 RK4 steps, mixed precision
+(FP32 stages, compensated FP32 hi/lo state).  Inputs are seeded synthetic
+data (nlsemagic_gb300.workloads.vortex_rings_3d).  The working set (about
+1.9 GB) is far larger than L2, so no L2 flush is needed between steps.
+
+  value  device-resident throughput: job = re-ingest the initial state from
+         device planar arrays + 500 RK4 steps (CUDA graphs), timed with CUDA
+         events on the solver stream.
+  e2e    the same job through the C ABI one-shot entry point
+         NLSE3D_TAKE_STEPS_CUDA_MIXED with pinned host planar buffers
+         (host->device copies, 500 steps, device->host copies inside).
+
+--impl reference times the reference CPU integrator (the C oracle port of
+NLSE3D_TAKE_STEPS_2SHOC.c) on the host cores: one independent solve per
+thread, each bench step one bounded sample (RK4 steps on the full grid).
+
+Multi-GPU: replicas only (each rank runs its own independent solve; no
+collective on the data path), weak scaling.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "RK4 Gpt-steps/s & %HBM roofline at stated FP64 error; served p50/p99 latency"
+UNIT = "Gpt-steps/s"
+# Algorithmic HBM bytes per grid-point-step of this implementation's mixed
+# path (one pass per RK4 stage: 28 + 44 + 36 + 52), and of the per-stage
+# model used for the reference design (240 mixed / 304 FP64).
+BYTES_MIXED = 160.0
+BYTES_MODEL_MIXED = 240.0
+BYTES_FP64 = 304.0
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    return rank, world, local
+
+
+def max_over_ranks(x, world):
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def read_traffic():
+    """DRAM bytes per point-step of the stage kernels from the committed ncu
+    summary (profiles/stage_kernels_3d2shoc_mixed.md), or None."""
+    p = os.path.join(ROOT, "profiles", "stage_kernels_3d2shoc_mixed.md")
+    if not os.path.exists(p):
+        return None
+    for ln in open(p):
+        if ln.startswith("dram_bytes_per_point_step:"):
+            try:
+                return float(ln.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the C oracle port of the reference integrator, one
+# independent solve per thread (the reference is serial; aggregate host
+# throughput is P independent solves).
+# ---------------------------------------------------------------------------
+def cpu_sample(w, steps, threads, precision=2):
+    import oracle
+    oracle._load_port()
+    results = [None] * threads
+
+    def one(t):
+        t0 = time.perf_counter()
+        oracle.take_steps(w.U, w.V, w.s, w.a, w.h2, w.BC, steps, w.k, method=w.method,
+                          precision=precision, flags=oracle.MSD_GUARD)
+        results[t] = time.perf_counter() - t0
+
+    th = [threading.Thread(target=one, args=(t,)) for t in range(threads)]
+    t0 = time.perf_counter()
+    for x in th:
+        x.start()
+    for x in th:
+        x.join()
+    wall = time.perf_counter() - t0
+    pts = float(w.points) * steps * threads
+    return pts / wall / 1e9, wall
+
+
+def cpu_threads_for(w):
+    n = os.cpu_count() or 1
+    try:
+        import psutil
+        avail = psutil.virtual_memory().available
+    except Exception:
+        avail = None
+    per = w.points * 8 * 13  # oracle scratch (8 planes) + in/out planes
+    if avail:
+        n = max(1, min(n, int(0.6 * avail // per)))
+    return min(n, 64)
+
+
+def run_reference(args, w):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    threads = cpu_threads_for(w)
+    steps_per_sample = args.cpu_sample_steps
+    for _ in range(args.warmup):
+        cpu_sample(w, 1, 1)  # touch pages / load library; short
+    vals = []
+    t_all = time.perf_counter()
+    for _ in range(args.steps):
+        v, wall = cpu_sample(w, steps_per_sample, threads)
+        vals.append(v)
+    elapsed = time.perf_counter() - t_all
+    value = float(np.mean(vals))
+    sample = ("%d RK4 step(s) of the %s solve per thread, %d threads, FP64 C oracle port "
+              "(oracle/nlse_oracle.c) of the reference CPU integrator" % (
+                  steps_per_sample, w.name, threads))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * elapsed / max(1, args.steps), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": w.name, "grid": list(w.U.shape), "method": "2SHOC",
+                   "bc": "MSD", "rk4_steps_per_sample": steps_per_sample,
+                   "precision": "fp64 (reference CPU integrator)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_gpu(args, w):
+    import torch
+
+    import nlsemagic_gb300 as ng
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    ng.load()
+    n = w.points
+    steps = w.steps
+    prec = ng.PREC_MIXED
+
+    # device-resident planar inputs
+    Ur = torch.from_numpy(np.ascontiguousarray(w.U.real.ravel(order="F"))).cuda()
+    Ui = torch.from_numpy(np.ascontiguousarray(w.U.imag.ravel(order="F"))).cuda()
+    Vd = torch.from_numpy(np.ascontiguousarray(w.V.ravel(order="F"))).cuda()
+    solver = ng.Solver(w.U.shape, method=w.method, precision=prec, BC=w.BC, s=w.s, a=w.a,
+                       h2=w.h2, k=w.k)
+    solver.set_graph_steps(args.graph_steps)
+    stream = torch.cuda.ExternalStream(solver.stream)
+
+    def job():
+        solver.upload_device(Ur.data_ptr(), Ui.data_ptr(), Vd.data_ptr())
+        solver.run(steps)
+
+    for _ in range(args.warmup):
+        job()
+    solver.sync()
+    torch.cuda.synchronize()
+    barrier(world)
+
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        barrier(world)
+        start.record(stream)
+        for _ in range(args.steps):
+            job()
+        end.record(stream)
+        end.synchronize()
+        torch.cuda.synchronize()
+        barrier(world)
+    t_ms = start.elapsed_time(end)
+    t_ms = max_over_ranks(t_ms, world)
+    clocks = clk.summary()
+    pts = float(n) * steps * args.steps * world
+    value = pts / (t_ms / 1000.0) / 1e9
+    ms_per_step = t_ms / args.steps
+
+    # accuracy + mass diagnostics of the last job
+    sum2 = solver.sum_abs2()
+    out = solver.download()
+    mass0 = float(np.sum(np.abs(w.U) ** 2))
+    mass_drift = abs(sum2 - mass0) / mass0
+
+    # ---- end to end through the C ABI one-shot call (pinned host buffers)
+    pin = lambda a: torch.from_numpy(a).pin_memory()  # noqa: E731
+    hUr = pin(np.ascontiguousarray(w.U.real.ravel(order="F")))
+    hUi = pin(np.ascontiguousarray(w.U.imag.ravel(order="F")))
+    hV = pin(np.ascontiguousarray(w.V.ravel(order="F")))
+    oR = torch.empty(n, dtype=torch.float64).pin_memory()
+    oI = torch.empty(n, dtype=torch.float64).pin_memory()
+    lib = ng.load()
+    import ctypes
+    dp = ctypes.POINTER(ctypes.c_double)
+    P = lambda t: ctypes.cast(t.data_ptr(), dp)  # noqa: E731
+    M_, N_, L_ = w.U.shape
+
+    def e2e_call():
+        rc = lib.NLSE3D_TAKE_STEPS_CUDA_MIXED(P(hUr), P(hUi), P(hV), P(oR), P(oI), w.s, w.a,
+                                              w.h2, w.BC, steps, w.k, L_, N_, M_, w.method)
+        if rc:
+            raise RuntimeError(ng._lib.last_error())
+
+    e2e_call()  # warm (workspace cached after this call)
+    torch.cuda.synchronize()
+    barrier(world)
+    ke = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        e2e_call()
+    t_e2e = time.perf_counter() - t0
+    t_e2e = max_over_ranks(t_e2e, world)
+    e2e_value = float(n) * steps * ke * world / t_e2e / 1e9
+    e2e_out = (oR.numpy() + 1j * oI.numpy()).reshape(w.U.shape, order="F")
+
+    # ---- FP64 plain path on the same workload (for the mixed/FP64 ratio and
+    # the error of the mixed path), a shorter run
+    fp64 = None
+    if args.fp64_steps > 0 and rank == 0:
+        s64 = ng.Solver(w.U.shape, method=w.method, precision=ng.PREC_DOUBLE, BC=w.BC, s=w.s,
+                        a=w.a, h2=w.h2, k=w.k)
+        s64.set_graph_steps(args.graph_steps)
+        smx = ng.Solver(w.U.shape, method=w.method, precision=prec, BC=w.BC, s=w.s, a=w.a,
+                        h2=w.h2, k=w.k)
+        st64 = torch.cuda.ExternalStream(s64.stream)
+        s64.upload_device(Ur.data_ptr(), Ui.data_ptr(), Vd.data_ptr())
+        s64.run(2)
+        s64.sync()
+        s64.upload_device(Ur.data_ptr(), Ui.data_ptr(), Vd.data_ptr())
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st64)
+        s64.run(args.fp64_steps)
+        e1.record(st64)
+        e1.synchronize()
+        t64 = e0.elapsed_time(e1) / 1000.0
+        smx.upload_device(Ur.data_ptr(), Ui.data_ptr(), Vd.data_ptr())
+        smx.run(args.fp64_steps)
+        err = None
+        try:
+            err = float(np.linalg.norm((smx.download() - s64.download()).ravel())
+                        / np.linalg.norm(s64.download().ravel()))
+        except Exception:
+            pass
+        fp64 = {"value": float(n) * args.fp64_steps / t64 / 1e9, "unit": UNIT,
+                "rk4_steps": args.fp64_steps,
+                "roofline_frac_of_measured_hbm": float(n) * args.fp64_steps * BYTES_FP64 / t64 /
+                1e9 / peaks()[0],
+                "mixed_rel_l2_vs_fp64_same_steps": err}
+        s64.close()
+        smx.close()
+
+    peak, peak_kind = peaks()
+    achieved = value * BYTES_MIXED / world  # GB/s per GPU (Gpt/s * B)
+    traffic_ppt = read_traffic()
+    launches_per_job = steps * solver.launches_per_step + 2  # + 2 ingest conversions
+    roof = {
+        "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "frac": achieved / peak,
+        "traffic": (traffic_ppt * n / 4.0) if traffic_ppt else None,
+        "peak_kind": peak_kind,
+        "kernel": "RK4 stage kernels (4 launches per RK4 step)",
+        "algorithmic_bytes_per_point_step": BYTES_MIXED,
+        "algorithmic_bytes_per_launch": BYTES_MIXED / 4.0 * n,
+        "model_frac_240B": value * BYTES_MODEL_MIXED / world / peak,
+    }
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32-stage/f32x2-accumulate",
+        "data": "synthetic (seeded vortex rings in a harmonic trap)",
+        "config": {"workload": w.name, "grid": list(w.U.shape), "method": "2SHOC", "bc": "MSD",
+                   "rk4_steps_per_job": steps, "k": w.k, "h": w.h,
+                   "precision": "mixed (FP32 stages, compensated FP32 hi/lo state)",
+                   "parallelism": "replicas x%d" % world,
+                   "l2": "inputs (~1.9 GB working set) larger than L2; no flush",
+                   "graph_steps": args.graph_steps},
+        "roofline": roof,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 3 * 8 * n,
+                "d2h_bytes_per_step": 2 * 8 * n,
+                "path": "C ABI NLSE3D_TAKE_STEPS_CUDA_MIXED, pinned host planar buffers",
+                "same_result_as_value_path": bool(np.array_equal(e2e_out, out))},
+        "gpu_launches": int(args.steps * launches_per_job),
+        "clocks": clocks,
+        "accuracy": {"mass_rel_drift_job": mass_drift},
+    }
+    if fp64:
+        result["fp64_path"] = fp64
+        result["mixed_over_fp64"] = value / world / fp64["value"]
+    if rank == 0 and world == 1 and args.cpu_sample_steps > 0:
+        threads = cpu_threads_for(w)
+        v, wall = cpu_sample(w, args.cpu_sample_steps, threads)
+        result["cpu_baseline"] = {
+            "value": v, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d RK4 step(s) of the %s solve per thread (FP64 2SHOC), %d threads, C "
+                      "oracle port of NLSE3D_TAKE_STEPS_2SHOC.c, %.1f s wall" % (
+                          args.cpu_sample_steps, w.name, threads, wall)}
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    solver.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--grid", type=int, default=320)
+    ap.add_argument("--rk4-steps", type=int, default=500)
+    ap.add_argument("--graph-steps", type=int, default=10)
+    ap.add_argument("--fp64-steps", type=int, default=20)
+    ap.add_argument("--cpu-sample-steps", type=int, default=1)
+    args = ap.parse_args()
+    from nlsemagic_gb300 import workloads as W
+    rank, world, _ = dist_env()
+    w = W.vortex_rings_3d(seed=1002 + rank, n=args.grid, method=2, steps=args.rk4_steps)
+    if args.impl == "reference":
+        run_reference(args, w)
+    else:
+        run_gpu(args, w)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,188 @@
+/*
+ * nlse_gb300.h -- C ABI of the GB300 (sm_103a) NLSE RK4 step library.
+ *
+ * The library integrates chunks of classical RK4 time steps of
+ *     i U_t + a lap(U) - V U + s |U|^2 U = 0
+ * in 1D, 2D and 3D with second-order central differences (CD, method 1) or
+ * the two-step fourth-order compact scheme (2SHOC, method 2), with the
+ * boundary codes of NLSEmagic: 1 Dirichlet, 2 modulus-squared Dirichlet
+ * (MSD), 3 Laplacian zero, 4 one-sided differences (1D only).
+ *
+ * Arrays are planar (separate real and imaginary planes) and column-major
+ * (MATLAB order): a 3D grid of dimensions M x N x L stores point (k, j, i),
+ * k < M fastest, at (i*N + j)*M + k.
+ *
+ * Every function returns an int status (NLSE_OK = 0); the message of the
+ * last failure on the calling thread is in nlse_last_error_string().  The
+ * reference's functions are void and check nothing; the deviations are
+ * listed with each declaration.  Inputs are const and never modified (the
+ * reference CPU integrators overwrite their input,
+ * src_old/NLSE1D_v1/NLSE1D_TAKE_STEPS_CD.c:124,168).
+ *
+ * Precision classes:
+ *   NLSE_PREC_SINGLE (1)  FP32 throughout, the arithmetic of the reference
+ *                         *_F / *_CUDA_F integrators.
+ *   NLSE_PREC_DOUBLE (2)  FP64, operation-for-operation the reference double
+ *                         integrators (bit-identical results).
+ *   NLSE_PREC_MIXED  (3)  FP32 stage evaluation, compensated FP32 hi/lo pair
+ *                         for the state and its RK4 accumulation; FP64 in and
+ *                         out.
+ *
+ * Thread safety: calls on different solver handles may run concurrently;
+ * one handle must not be used from two threads at once.  The library never
+ * resets the device (the reference calls cudaDeviceReset after every chunk,
+ * src_old/NLSE1D_v1/NLSE1D_TAKE_STEPS_CD_CUDA_D.cu:262).
+ */
+#ifndef NLSE_GB300_H
+#define NLSE_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NLSE_OK 0
+#define NLSE_ERR_ARG 1        /* invalid argument                        */
+#define NLSE_ERR_CUDA 2       /* CUDA runtime error                      */
+#define NLSE_ERR_NOMEM 3      /* device or host allocation failed        */
+#define NLSE_ERR_TIMEOUT 4    /* a bounded device wait gave up           */
+#define NLSE_ERR_NONFINITE 5  /* the state contains NaN or Inf           */
+#define NLSE_ERR_CAPACITY 6   /* request exceeds a configured limit      */
+#define NLSE_ERR_STATE 7      /* call not valid in the object's state    */
+
+#define NLSE_PREC_SINGLE 1
+#define NLSE_PREC_DOUBLE 2
+#define NLSE_PREC_MIXED 3
+
+#define NLSE_METHOD_CD 1
+#define NLSE_METHOD_2SHOC 2
+
+#define NLSE_BC_DIRICHLET 1
+#define NLSE_BC_MSD 2
+#define NLSE_BC_LAP0 3
+#define NLSE_BC_ONESIDED 4
+
+/* Problem description.  dims in MATLAB order: dims[0] = M (fastest),
+ * dims[1] = N, dims[2] = L; unused entries ignored.  Each used dimension
+ * must be >= 3 (>= 4 with BC 4). */
+typedef struct nlse_problem {
+  int ndim;
+  long long dims[3];
+  int method;
+  int precision;
+  int bc;
+  double s, a, h2, k;
+  int flags; /* NLSE_FLAG_* */
+} nlse_problem;
+
+/* MSD boundary: where the interior neighbour is exactly zero, use zero
+ * angular velocity instead of dividing by |U|^2 = 0 (the guard of
+ * src/NLSEmagic3D/NLSE3D_TAKE_STEPS_CD_CUDA_D.cu:155-162).  On by default
+ * in the legacy entry points; results differ from the reference CPU code
+ * only where that code produces NaN. */
+#define NLSE_FLAG_MSD_GUARD 1
+/* Force the gather-form kernels (testing; default picks tiled kernels). */
+#define NLSE_FLAG_GATHER 2
+
+const char *nlse_last_error_string(void);
+const char *nlse_version(void);
+
+/* ------------------------------------------------------------------------
+ * One-shot calls.  Replace the v2 library functions of NLSEmagic.h
+ * (src/NLSEmagic1D/NLSEmagic.h:1-35): same names and argument order.
+ * Deviations: int status instead of void; const inputs; 3D dimension order
+ * (L, N, M) follows the 2D pattern (N, M) = (columns, rows), since the
+ * reference declares but never defines the 3D functions.  Device workspace
+ * is cached between calls (the reference allocates and frees per call).
+ * ---------------------------------------------------------------------- */
+
+/* src/NLSEmagic1D/NLSEmagic.h:1-2; src/NLSEmagic1D/NLSEmagic1D_GPU.cu:663 */
+int NLSE1D_TAKE_STEPS_CUDA(const double *Uoldr, const double *Uoldi, const double *V,
+                           double *Unewr, double *Unewi, double s, double a, double h2, int BC,
+                           int chunk_size, double k, int N, int method);
+/* src/NLSEmagic1D/NLSEmagic.h:4-5; src/NLSEmagic1D/NLSEmagic1D_GPU.cu:754 */
+int NLSE1D_TAKE_STEPS_CUDA_F(const float *Uoldr, const float *Uoldi, const float *V,
+                             float *Unewr, float *Unewi, float s, float a, float h2, int BC,
+                             int chunk_size, float k, int N, int method);
+/* src/NLSEmagic2D/NLSEmagic.h:13-14 (N columns, M rows) */
+int NLSE2D_TAKE_STEPS_CUDA(const double *Uoldr, const double *Uoldi, const double *V,
+                           double *Unewr, double *Unewi, double s, double a, double h2, int BC,
+                           int chunk_size, double k, int N, int M, int method);
+/* src/NLSEmagic2D/NLSEmagic.h:16-17 */
+int NLSE2D_TAKE_STEPS_CUDA_F(const float *Uoldr, const float *Uoldi, const float *V,
+                             float *Unewr, float *Unewi, float s, float a, float h2, int BC,
+                             int chunk_size, float k, int N, int M, int method);
+/* src/NLSEmagic1D/NLSEmagic.h:25-26 */
+int NLSE3D_TAKE_STEPS_CUDA(const double *Uoldr, const double *Uoldi, const double *V,
+                           double *Unewr, double *Unewi, double s, double a, double h2, int BC,
+                           int chunk_size, double k, int L, int N, int M, int method);
+/* src/NLSEmagic1D/NLSEmagic.h:28-29 */
+int NLSE3D_TAKE_STEPS_CUDA_F(const float *Uoldr, const float *Uoldi, const float *V,
+                             float *Unewr, float *Unewi, float s, float a, float h2, int BC,
+                             int chunk_size, float k, int L, int N, int M, int method);
+
+/* Mixed precision (FP32 stages, compensated state), FP64 planar in and out.
+ * No reference counterpart: the third precision class of this library. */
+int NLSE1D_TAKE_STEPS_CUDA_MIXED(const double *Uoldr, const double *Uoldi, const double *V,
+                                 double *Unewr, double *Unewi, double s, double a, double h2,
+                                 int BC, int chunk_size, double k, int N, int method);
+int NLSE2D_TAKE_STEPS_CUDA_MIXED(const double *Uoldr, const double *Uoldi, const double *V,
+                                 double *Unewr, double *Unewi, double s, double a, double h2,
+                                 int BC, int chunk_size, double k, int N, int M, int method);
+int NLSE3D_TAKE_STEPS_CUDA_MIXED(const double *Uoldr, const double *Uoldi, const double *V,
+                                 double *Unewr, double *Unewi, double s, double a, double h2,
+                                 int BC, int chunk_size, double k, int L, int N, int M,
+                                 int method);
+
+/* General one-shot call behind all of the above and behind the v1 MEX
+ * gateways U = NLSE{1,2,3}D_TAKE_STEPS_{CD,2SHOC}_CUDA_{D,F}(U,V,s,a,h2,BC,
+ * chunk_size,k) (e.g. src/NLSEmagic3D/NLSE3D_TAKE_STEPS_2SHOC_CUDA_D.cu:430).
+ * Planar double host arrays (any precision class); Ui may be NULL (real
+ * input, imaginary plane taken as zero, as the reference does). */
+int nlse_take_steps(const nlse_problem *p, const double *Ur, const double *Ui, const double *V,
+                    double *out_r, double *out_i, int chunk_size);
+
+/* ------------------------------------------------------------------------
+ * Resident solver: state and potential stay in HBM between chunks.  No
+ * reference counterpart (the reference copies in and out and resets the
+ * device on every call).
+ * ---------------------------------------------------------------------- */
+typedef struct nlse_solver nlse_solver;
+
+/* Allocates device state on the current device; its own stream. */
+int nlse_solver_create(const nlse_problem *p, nlse_solver **out);
+int nlse_solver_destroy(nlse_solver *s);
+/* Host planar arrays; Ui may be NULL.  Synchronous with respect to the host
+ * buffers (they may be reused on return). */
+int nlse_solver_upload(nlse_solver *s, const double *Ur, const double *Ui, const double *V);
+/* Same from device planar double arrays (no host copy). */
+int nlse_solver_upload_device(nlse_solver *s, const double *dUr, const double *dUi,
+                              const double *dV);
+/* Enqueue nsteps RK4 steps on the solver stream (asynchronous). */
+int nlse_solver_run(nlse_solver *s, long long nsteps);
+/* Copy the state to host planar arrays (waits for queued steps). */
+int nlse_solver_download(nlse_solver *s, double *Ur, double *Ui);
+/* Copy the state to device planar double arrays (stream-ordered). */
+int nlse_solver_download_device(nlse_solver *s, double *dUr, double *dUi);
+/* sum |U|^2 over all points (FP64 accumulation; multiply by h^d for the
+ * mass).  Returns NLSE_ERR_NONFINITE if the state holds NaN or Inf. */
+int nlse_solver_mass(nlse_solver *s, double *sum_abs2);
+int nlse_solver_sync(nlse_solver *s);
+/* The cudaStream_t the solver enqueues on. */
+int nlse_solver_stream(nlse_solver *s, void **stream);
+/* Steps per captured CUDA graph (default 8; 0 disables graphs). */
+int nlse_solver_set_graph_steps(nlse_solver *s, int steps);
+/* Number of kernel launches one RK4 step enqueues. */
+int nlse_solver_launches_per_step(const nlse_solver *s);
+/* Bytes of device memory held by the solver. */
+long long nlse_solver_device_bytes(const nlse_solver *s);
+
+/* Linear stability limit of the time step used by the NLSEmagic drivers:
+ * h^2 / (ndim * sqrt(2) * a) for CD, 3/4 of that for 2SHOC
+ * (src/NLSEmagic3D/NLSEmagic3D.m:154-163). */
+double nlse_linear_stability_k(int ndim, int method, double h, double a);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NLSE_GB300_H */

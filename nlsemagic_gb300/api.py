@@ -1,0 +1,227 @@
+"""Python mirror of the NLSEmagic step-function interface, over the C ABI.
+
+Array convention: the MATLAB one.  A grid of MATLAB size M x N x L is a numpy
+array of shape (M, N, L) (first index fastest, Fortran order); 2D grids are
+(M, N) and 1D grids (M,) (an (M, 1) or (1, M) column/row vector is also taken
+as 1D, as the reference does with ``N = mxGetN; if N == 1, N = mxGetM``,
+src_old/NLSE1D_v1/NLSE1D_TAKE_STEPS_CD.c:115-118).  Results are new complex128
+arrays of the input's shape; inputs are never modified.
+
+Functions:
+
+* ``NLSE{1,2,3}D_TAKE_STEPS_{CD,2SHOC}_CUDA_{D,F}(U, V, s, a, h2, BC,
+  chunk_size, k)`` -- the v1 MEX names (e.g.
+  src/NLSEmagic3D/NLSE3D_TAKE_STEPS_2SHOC_CUDA_D.cu:12-24), double or single
+  precision, and ``..._CUDA_M`` for the mixed-precision class.
+* ``NLSEmagic{1,2,3}D_Take_Steps_GPU(U, V, s, a, h2, BC, chunk, k,
+  precision, method)`` -- the v2 gateways
+  (src/NLSEmagic1D/NLSEmagic1D_Take_Steps_GPU.c:33-41); precision 1 single,
+  2 double, 3 mixed.
+* :class:`Solver` -- the resident-state handle (state and potential stay on
+  the GPU between chunks).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import FLAG_MSD_GUARD, PREC_DOUBLE, PREC_MIXED, PREC_SINGLE, Problem, check, load
+
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_dp)
+
+
+def grid_dims(shape):
+    """(ndim, (M, N, L)) of a MATLAB-shaped array; 1D vectors of either
+    orientation are 1D."""
+    shape = tuple(int(x) for x in shape)
+    if len(shape) == 1:
+        return 1, (shape[0], 1, 1)
+    if len(shape) == 2 and 1 in shape:
+        return 1, (max(shape), 1, 1)
+    if len(shape) == 2:
+        return 2, (shape[0], shape[1], 1)
+    if len(shape) == 3:
+        return 3, shape
+    raise ValueError("grids must have 1, 2 or 3 dimensions (got shape %s)" % (shape,))
+
+
+def make_problem(ndim, dims, method, precision, BC, s, a, h2, k, flags=FLAG_MSD_GUARD):
+    p = Problem()
+    p.ndim = int(ndim)
+    for t in range(3):
+        p.dims[t] = int(dims[t]) if t < ndim else 1
+    p.method = int(method)
+    p.precision = int(precision)
+    p.bc = int(BC)
+    p.s, p.a, p.h2, p.k = float(s), float(a), float(h2), float(k)
+    p.flags = int(flags)
+    return p
+
+
+def planar(U):
+    """Fortran-order flat real and imaginary planes of U (float64)."""
+    U = np.asarray(U)
+    re = np.ascontiguousarray(np.real(U).ravel(order="F"), dtype=np.float64)
+    im = np.ascontiguousarray(np.imag(U).ravel(order="F") if np.iscomplexobj(U)
+                              else np.zeros(U.size), dtype=np.float64)
+    return re, im
+
+
+def take_steps(U, V, s, a, h2, BC, chunk_size, k, method=1, precision=PREC_DOUBLE,
+               flags=FLAG_MSD_GUARD):
+    """Advance U by chunk_size RK4 steps on the GPU; returns the new U."""
+    U = np.asarray(U)
+    V = np.asarray(V, dtype=np.float64)
+    if V.shape != U.shape:
+        raise ValueError("V must have the shape of U (%s vs %s)" % (V.shape, U.shape))
+    ndim, dims = grid_dims(U.shape)
+    prob = make_problem(ndim, dims, method, precision, BC, s, a, h2, k, flags)
+    re, im = planar(U)
+    vv = np.ascontiguousarray(V.ravel(order="F"))
+    out_r = np.empty_like(re)
+    out_i = np.empty_like(im)
+    check(load().nlse_take_steps(ctypes.byref(prob), _ptr(re), _ptr(im), _ptr(vv), _ptr(out_r),
+                                 _ptr(out_i), int(chunk_size)))
+    out = out_r + 1j * out_i
+    return out.reshape(U.shape, order="F")
+
+
+def _legacy(ndim, method, precision):
+    def f(U, V, s, a, h2, BC, chunk_size, k):
+        got, _ = grid_dims(np.shape(U))
+        if got != ndim:
+            raise ValueError("this entry point integrates %dD grids (got a %dD array)" % (ndim, got))
+        return take_steps(U, V, s, a, h2, BC, chunk_size, k, method=method, precision=precision)
+
+    f.__name__ = "NLSE%dD_TAKE_STEPS_%s_CUDA_%s" % (
+        ndim, "CD" if method == 1 else "2SHOC", {1: "F", 2: "D", 3: "M"}[precision])
+    f.__doc__ = ("U = %s(U, V, s, a, h2, BC, chunk_size, k): %dD RK4 + %s in %s precision on "
+                 "the GPU (drop-in for the NLSEmagic MEX function of that name)."
+                 % (f.__name__, ndim, "CD" if method == 1 else "2SHOC",
+                    {1: "single", 2: "double", 3: "mixed"}[precision]))
+    return f
+
+
+for _nd in (1, 2, 3):
+    for _m in (1, 2):
+        for _p in (1, 2, 3):
+            _f = _legacy(_nd, _m, _p)
+            globals()[_f.__name__] = _f
+
+
+def _v2(ndim):
+    def f(U, V, s, a, h2, BC, chunk, k, precision, method):
+        got, _ = grid_dims(np.shape(U))
+        if got != ndim:
+            raise ValueError("this entry point integrates %dD grids (got a %dD array)" % (ndim, got))
+        return take_steps(U, V, s, a, h2, BC, chunk, k, method=method, precision=precision)
+
+    f.__name__ = "NLSEmagic%dD_Take_Steps_GPU" % ndim
+    f.__doc__ = ("U = %s(U, V, s, a, h2, BC, chunk, k, precision, method) (precision 1 single, "
+                 "2 double, 3 mixed; method 1 CD, 2 2SHOC)." % f.__name__)
+    return f
+
+
+NLSEmagic1D_Take_Steps_GPU = _v2(1)
+NLSEmagic2D_Take_Steps_GPU = _v2(2)
+NLSEmagic3D_Take_Steps_GPU = _v2(3)
+
+
+def linear_stability_k(ndim, method, h, a):
+    return load().nlse_linear_stability_k(int(ndim), int(method), float(h), float(a))
+
+
+class Solver:
+    """Resident solve: state and potential live on the current CUDA device.
+
+    ``shape`` is the MATLAB-shaped grid shape.  All work is enqueued on the
+    solver's own stream (``self.stream``, a cudaStream_t handle)."""
+
+    def __init__(self, shape, method=2, precision=PREC_MIXED, BC=1, s=-1.0, a=1.0, h2=0.01,
+                 k=1e-3, flags=FLAG_MSD_GUARD):
+        self.shape = tuple(int(x) for x in shape)
+        self.ndim, self.dims = grid_dims(self.shape)
+        self.n = int(np.prod(self.shape))
+        self.problem = make_problem(self.ndim, self.dims, method, precision, BC, s, a, h2, k, flags)
+        self._lib = load()
+        h = ctypes.c_void_p()
+        check(self._lib.nlse_solver_create(ctypes.byref(self.problem), ctypes.byref(h)))
+        self._h = h
+
+    # -- lifecycle
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.nlse_solver_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- data movement
+    def upload(self, U, V):
+        re, im = planar(U)
+        vv = np.ascontiguousarray(np.asarray(V, dtype=np.float64).ravel(order="F"))
+        if re.size != self.n or vv.size != self.n:
+            raise ValueError("U and V must have %d points" % self.n)
+        check(self._lib.nlse_solver_upload(self._h, _ptr(re), _ptr(im), _ptr(vv)))
+
+    def upload_device(self, re_ptr, im_ptr, v_ptr):
+        """Device pointers (ints) to planar float64 arrays of n points."""
+        check(self._lib.nlse_solver_upload_device(self._h, ctypes.c_void_p(re_ptr),
+                                                  ctypes.c_void_p(im_ptr), ctypes.c_void_p(v_ptr)))
+
+    def download(self):
+        re = np.empty(self.n)
+        im = np.empty(self.n)
+        check(self._lib.nlse_solver_download(self._h, _ptr(re), _ptr(im)))
+        return (re + 1j * im).reshape(self.shape, order="F")
+
+    def download_device(self, re_ptr, im_ptr):
+        check(self._lib.nlse_solver_download_device(self._h, ctypes.c_void_p(re_ptr),
+                                                    ctypes.c_void_p(im_ptr)))
+
+    # -- stepping
+    def run(self, nsteps):
+        check(self._lib.nlse_solver_run(self._h, int(nsteps)))
+
+    def sync(self):
+        check(self._lib.nlse_solver_sync(self._h))
+
+    def sum_abs2(self):
+        """sum over points of |U|^2, accumulated in FP64 (multiply by h^d for
+        the mass)."""
+        out = ctypes.c_double()
+        check(self._lib.nlse_solver_mass(self._h, ctypes.byref(out)))
+        return out.value
+
+    def set_graph_steps(self, steps):
+        check(self._lib.nlse_solver_set_graph_steps(self._h, int(steps)))
+
+    @property
+    def stream(self) -> int:
+        st = ctypes.c_void_p()
+        check(self._lib.nlse_solver_stream(self._h, ctypes.byref(st)))
+        return st.value or 0
+
+    @property
+    def launches_per_step(self) -> int:
+        return int(self._lib.nlse_solver_launches_per_step(self._h))
+
+    @property
+    def device_bytes(self) -> int:
+        return int(self._lib.nlse_solver_device_bytes(self._h))

@@ -1,0 +1,93 @@
+"""Build the CUDA library libnlse_gb300.so in-tree with nvcc for sm_103a.
+
+Each translation unit is compiled in parallel to an object file under
+``nlsemagic_gb300/_build/`` and the objects are linked into
+``nlsemagic_gb300/libnlse_gb300.so``.  The exact-precision unit is compiled
+with ``-fmad=false`` so that no multiply-add is contracted (bit-identical
+FP64 / FP32 results against the reference C integrators); host code is
+compiled with ``-ffp-contract=off`` for the same reason on aarch64 hosts.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libnlse_gb300.so")
+INCLUDE = os.path.join(os.path.dirname(HERE), "include")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+COMMON = ["-O3", "-lineinfo", "-std=c++17", "--extended-lambda", "-Xcompiler", "-fPIC",
+          "-Xcompiler", "-ffp-contract=off", "-I", CSRC, "-I", INCLUDE]
+
+# unit -> extra flags
+UNITS = {
+    "kern_exact.cu": ["-fmad=false"],
+    "kern_mixed.cu": [],
+    "kern_stream3d.cu": [],
+    "kern_util.cu": [],
+    "nlse_abi.cu": [],
+    "nlse_batch.cu": [],
+}
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found; the CUDA toolkit is required to build nlsemagic_gb300")
+
+
+def _headers():
+    return [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))] + \
+           [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
+
+
+def _stale(out, deps):
+    if not os.path.exists(out):
+        return True
+    t = os.path.getmtime(out)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) -> str:
+    os.makedirs(BUILD, exist_ok=True)
+    nv = nvcc()
+    hdrs = _headers()
+    units = [u for u in UNITS if os.path.exists(os.path.join(CSRC, u))]
+    objs = []
+
+    def compile_one(u):
+        src = os.path.join(CSRC, u)
+        obj = os.path.join(BUILD, u.replace(".cu", ".o"))
+        if force or ptxas_info or _stale(obj, [src, __file__] + hdrs):
+            cmd = [nv] + ARCH + COMMON + UNITS[u] + (["-Xptxas", "-v"] if ptxas_info else []) + \
+                  ["-c", src, "-o", obj + ".tmp"]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (u, " ".join(cmd), r.stderr))
+            os.replace(obj + ".tmp", obj)
+            if verbose or ptxas_info:
+                sys.stderr.write(r.stderr)
+        return obj
+
+    with ThreadPoolExecutor(max_workers=max(1, min(len(units), os.cpu_count() or 1))) as ex:
+        objs = list(ex.map(compile_one, units))
+    if force or _stale(LIB, objs):
+        tmp = LIB + ".tmp%d" % os.getpid()
+        cmd = [nv] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcuda"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
+        os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv,
+                ptxas_info="--ptxas" in sys.argv))

@@ -1,0 +1,64 @@
+// Exact-precision (FP64 / FP32) stage launchers.  This translation unit is
+// compiled with -fmad=false: no multiply-add is contracted, so every
+// operation rounds exactly as in the reference C integrators.
+#include "kern_gather.cuh"
+#include "kern_tiled.cuh"
+#include "nlse_launch.h"
+
+namespace nlse {
+
+template <typename R, int DIM, int METHOD, int BC>
+static cudaError_t launch_one(const Geom& g, const Consts<R>& c, const ExactStageArgs<R>& a,
+                              int stage, cudaStream_t st, int kernel_kind) {
+  if (kernel_kind == KERNEL_TILED && tiled_supported(g, DIM)) {
+    return tiled::launch_exact<R, DIM, METHOD, BC>(g, c, a, stage, st);
+  }
+  long long blocks = (g.n + 255) / 256;
+  if (blocks > 152LL * 32) blocks = 152LL * 32;
+  exact::gather_stage<R, DIM, METHOD, BC><<<(unsigned)blocks, 256, 0, st>>>(
+      g, c, a.Yin, a.Psi, a.V, a.K, a.Yout, stage);
+  return cudaGetLastError();
+}
+
+template <typename R, int DIM, int METHOD>
+static cudaError_t by_bc(const Geom& g, int BC, const Consts<R>& c, const ExactStageArgs<R>& a,
+                         int stage, cudaStream_t st, int kind) {
+  switch (BC) {
+    case 1: return launch_one<R, DIM, METHOD, 1>(g, c, a, stage, st, kind);
+    case 2: return launch_one<R, DIM, METHOD, 2>(g, c, a, stage, st, kind);
+    case 3: return launch_one<R, DIM, METHOD, 3>(g, c, a, stage, st, kind);
+    case 4:
+      if (DIM == 1) return launch_one<R, 1, METHOD, 4>(g, c, a, stage, st, KERNEL_GATHER);
+      return cudaErrorInvalidValue;
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <typename R>
+cudaError_t launch_exact_stage(const Geom& g, int method, int BC, const Consts<R>& c,
+                               const ExactStageArgs<R>& a, int stage, cudaStream_t st,
+                               int kernel_kind) {
+  if (method == 1) {
+    switch (g.ndim) {
+      case 1: return by_bc<R, 1, 1>(g, BC, c, a, stage, st, kernel_kind);
+      case 2: return by_bc<R, 2, 1>(g, BC, c, a, stage, st, kernel_kind);
+      case 3: return by_bc<R, 3, 1>(g, BC, c, a, stage, st, kernel_kind);
+    }
+  } else if (method == 2) {
+    switch (g.ndim) {
+      case 1: return by_bc<R, 1, 2>(g, BC, c, a, stage, st, kernel_kind);
+      case 2: return by_bc<R, 2, 2>(g, BC, c, a, stage, st, kernel_kind);
+      case 3: return by_bc<R, 3, 2>(g, BC, c, a, stage, st, kernel_kind);
+    }
+  }
+  return cudaErrorInvalidValue;
+}
+
+template cudaError_t launch_exact_stage<double>(const Geom&, int, int, const Consts<double>&,
+                                                const ExactStageArgs<double>&, int, cudaStream_t,
+                                                int);
+template cudaError_t launch_exact_stage<float>(const Geom&, int, int, const Consts<float>&,
+                                               const ExactStageArgs<float>&, int, cudaStream_t,
+                                               int);
+
+}  // namespace nlse

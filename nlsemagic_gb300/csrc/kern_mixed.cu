@@ -1,0 +1,54 @@
+// Mixed-precision (FP32 stages, compensated state) stage launchers.
+#include "kern_gather.cuh"
+#include "kern_tiled.cuh"
+#include "nlse_launch.h"
+
+namespace nlse {
+
+template <int DIM, int METHOD, int BC>
+static cudaError_t launch_one(const Geom& g, const Consts<float>& c, const MixedStageArgs& a,
+                              int stage, cudaStream_t st, int kernel_kind) {
+  if (kernel_kind == KERNEL_TILED && tiled_supported(g, DIM)) {
+    return tiled::launch_mixed<DIM, METHOD, BC>(g, c, a, stage, st);
+  }
+  long long blocks = (g.n + 255) / 256;
+  if (blocks > 152LL * 32) blocks = 152LL * 32;
+  mixed::gather_stage<DIM, METHOD, BC><<<(unsigned)blocks, 256, 0, st>>>(
+      g, c, a.hi_in, a.lo_in, a.d_in, a.V, a.K, a.d_out, a.hi_out, a.lo_out, stage);
+  return cudaGetLastError();
+}
+
+template <int DIM, int METHOD>
+static cudaError_t by_bc(const Geom& g, int BC, const Consts<float>& c, const MixedStageArgs& a,
+                         int stage, cudaStream_t st, int kind) {
+  switch (BC) {
+    case 1: return launch_one<DIM, METHOD, 1>(g, c, a, stage, st, kind);
+    case 2: return launch_one<DIM, METHOD, 2>(g, c, a, stage, st, kind);
+    case 3: return launch_one<DIM, METHOD, 3>(g, c, a, stage, st, kind);
+    case 4:
+      if (DIM == 1) return launch_one<1, METHOD, 4>(g, c, a, stage, st, KERNEL_GATHER);
+      return cudaErrorInvalidValue;
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_mixed_stage(const Geom& g, int method, int BC, const Consts<float>& c,
+                               const MixedStageArgs& a, int stage, cudaStream_t st,
+                               int kernel_kind) {
+  if (method == 1) {
+    switch (g.ndim) {
+      case 1: return by_bc<1, 1>(g, BC, c, a, stage, st, kernel_kind);
+      case 2: return by_bc<2, 1>(g, BC, c, a, stage, st, kernel_kind);
+      case 3: return by_bc<3, 1>(g, BC, c, a, stage, st, kernel_kind);
+    }
+  } else if (method == 2) {
+    switch (g.ndim) {
+      case 1: return by_bc<1, 2>(g, BC, c, a, stage, st, kernel_kind);
+      case 2: return by_bc<2, 2>(g, BC, c, a, stage, st, kernel_kind);
+      case 3: return by_bc<3, 2>(g, BC, c, a, stage, st, kernel_kind);
+    }
+  }
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace nlse

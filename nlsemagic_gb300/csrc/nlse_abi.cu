@@ -1,0 +1,673 @@
+// Host side of the C ABI declared in include/nlse_gb300.h: problem
+// validation, resident solver objects (device state, stream, captured CUDA
+// graphs of RK4 steps), the one-shot calls with a cached workspace, and
+// error reporting.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+
+#include "../../include/nlse_gb300.h"
+#include "nlse_launch.h"
+
+using namespace nlse;
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+static thread_local char g_err[512] = "";
+
+static int fail(int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+#define CUDA_TRY(expr)                                                                    \
+  do {                                                                                    \
+    cudaError_t e_ = (expr);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return fail(e_ == cudaErrorMemoryAllocation ? NLSE_ERR_NOMEM : NLSE_ERR_CUDA,       \
+                  "%s failed: %s (%s:%d)", #expr, cudaGetErrorString(e_), __FILE__, __LINE__); \
+  } while (0)
+
+extern "C" const char* nlse_last_error_string(void) { return g_err; }
+extern "C" const char* nlse_version(void) { return "nlse_gb300 1.0 (sm_103a)"; }
+
+extern "C" double nlse_linear_stability_k(int ndim, int method, double h, double a) {
+  double klin = h * h / ((double)ndim * sqrt(2.0) * a);
+  if (method == 2) klin *= 0.75;
+  return klin;
+}
+
+// ---------------------------------------------------------------------------
+// validation
+// ---------------------------------------------------------------------------
+static int validate(const nlse_problem* p) {
+  if (!p) return fail(NLSE_ERR_ARG, "problem is NULL");
+  if (p->ndim < 1 || p->ndim > 3) return fail(NLSE_ERR_ARG, "ndim must be 1, 2 or 3 (got %d)", p->ndim);
+  if (p->method != 1 && p->method != 2)
+    return fail(NLSE_ERR_ARG, "method must be 1 (CD) or 2 (2SHOC) (got %d)", p->method);
+  if (p->precision < 1 || p->precision > 3)
+    return fail(NLSE_ERR_ARG, "precision must be 1, 2 or 3 (got %d)", p->precision);
+  if (p->bc < 1 || p->bc > 4) return fail(NLSE_ERR_ARG, "BC must be 1, 2, 3 or 4 (got %d)", p->bc);
+  if (p->bc == 4 && p->ndim != 1)
+    return fail(NLSE_ERR_ARG, "BC 4 (one-sided) exists for 1D only");
+  long long n = 1;
+  for (int d = 0; d < p->ndim; ++d) {
+    long long m = p->dims[d];
+    long long need = p->bc == 4 ? 4 : 3;
+    if (m < need)
+      return fail(NLSE_ERR_ARG, "dimension %d is %lld; at least %lld points are needed", d, m, need);
+    if (m > (1LL << 30)) return fail(NLSE_ERR_ARG, "dimension %d too large", d);
+    n *= m;
+    if (n > (1LL << 31) - 1) return fail(NLSE_ERR_CAPACITY, "grid has more than 2^31-1 points");
+  }
+  if (!(p->a != 0.0) || !isfinite(p->a)) return fail(NLSE_ERR_ARG, "a must be finite and non-zero");
+  if (!(p->h2 > 0.0) || !isfinite(p->h2)) return fail(NLSE_ERR_ARG, "h2 must be > 0");
+  if (!(p->k > 0.0) || !isfinite(p->k)) return fail(NLSE_ERR_ARG, "k must be > 0");
+  if (!isfinite(p->s)) return fail(NLSE_ERR_ARG, "s must be finite");
+  return NLSE_OK;
+}
+
+static Geom make_geom(const nlse_problem* p) {
+  Geom g;
+  g.ndim = p->ndim;
+  g.M = (int)p->dims[0];
+  g.N = p->ndim >= 2 ? (int)p->dims[1] : 1;
+  g.L = p->ndim >= 3 ? (int)p->dims[2] : 1;
+  g.P = g.N * g.M;
+  g.n = (long long)g.L * g.N * g.M;
+  return g;
+}
+
+// Scalars in the precision and with the expressions of each reference file.
+static Consts<double> consts_double(const nlse_problem* p) {
+  Consts<double> c;
+  memset(&c, 0, sizeof(c));
+  double a = p->a, h2 = p->h2, k = p->k;
+  c.s = p->s;
+  c.a = a;
+  c.ah2 = a / h2;
+  c.l_a = 1.0 / a;
+  c.lh2 = 1.0 / h2;
+  c.a76 = a * (7.0 / 6.0);
+  c.a112 = a * (1.0 / 12.0);
+  if (p->ndim == 2) {
+    c.a_6h2 = a * (1.0 / (6.0 * h2));
+    c.a_12 = a * (1.0 / 12.0);
+  } else {
+    c.a_6h2 = a / (6.0 * h2);
+    c.a_12 = a / 12.0;
+  }
+  c.k = k;
+  c.k2 = k / 2.0;
+  c.k6 = k / 6.0;
+  c.kinv = 1.0 / k;
+  c.kinv2 = 2.0 / k;
+  c.msd_guard = (p->flags & NLSE_FLAG_MSD_GUARD) ? 1 : 0;
+  return c;
+}
+
+// FP32: scalars rounded to float first, then the _F files' float expressions
+// (e.g. src_old/NLSE1D_v1/NLSE1D_TAKE_STEPS_2SHOC_F.c:223-228).
+static Consts<float> consts_single(const nlse_problem* p) {
+  Consts<float> c;
+  memset(&c, 0, sizeof(c));
+  volatile float a = (float)p->a, h2 = (float)p->h2, k = (float)p->k;
+  c.s = (float)p->s;
+  c.a = a;
+  c.ah2 = a / h2;
+  c.l_a = 1.0f / a;
+  c.lh2 = 1.0f / h2;
+  c.a76 = a * (7.0f / 6.0f);
+  c.a112 = a * (1.0f / 12.0f);
+  if (p->ndim == 2) {
+    c.a_6h2 = a * (1.0f / (6.0f * h2));
+    c.a_12 = a * (1.0f / 12.0f);
+  } else {
+    c.a_6h2 = a / (6.0f * h2);
+    c.a_12 = a / 12.0f;
+  }
+  c.k = k;
+  c.k2 = k / 2.0f;
+  c.k6 = k / 6.0f;
+  c.kinv = 1.0f / k;
+  c.kinv2 = 2.0f / k;
+  c.msd_guard = (p->flags & NLSE_FLAG_MSD_GUARD) ? 1 : 0;
+  return c;
+}
+
+// Mixed: scalars evaluated in double and rounded once to float.
+static Consts<float> consts_mixed(const nlse_problem* p) {
+  Consts<double> d = consts_double(p);
+  Consts<float> c;
+  memset(&c, 0, sizeof(c));
+  c.s = (float)d.s;
+  c.a = (float)d.a;
+  c.ah2 = (float)d.ah2;
+  c.l_a = (float)d.l_a;
+  c.lh2 = (float)d.lh2;
+  c.a76 = (float)d.a76;
+  c.a112 = (float)d.a112;
+  c.a_6h2 = (float)d.a_6h2;
+  c.a_12 = (float)d.a_12;
+  c.k = (float)d.k;
+  c.k2 = (float)d.k2;
+  c.k6 = (float)d.k6;
+  c.kinv = (float)d.kinv;
+  c.kinv2 = (float)d.kinv2;
+  c.msd_guard = d.msd_guard;
+  return c;
+}
+
+// ---------------------------------------------------------------------------
+// solver
+// ---------------------------------------------------------------------------
+struct nlse_solver {
+  nlse_problem prob;
+  Geom g;
+  int device;
+  cudaStream_t stream;
+  Consts<double> cd;
+  Consts<float> cf;
+  int kernel_kind;
+  // exact precisions
+  void *psi, *K, *ya, *yb, *V;
+  // mixed precision
+  float2 *hi[2], *lo[2], *mK, *da, *db;
+  float* Vf;
+  int cur;
+  // device staging for planar transfers: re, im, V (n doubles each)
+  double* stage;
+  double* d_mass;
+  int* d_bad;
+  // graphs
+  int graph_steps;
+  cudaGraphExec_t gexec[2];
+  size_t bytes;
+};
+
+static int dalloc(nlse_solver* s, void** p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    cudaGetLastError();
+    return fail(NLSE_ERR_NOMEM, "cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
+  }
+  s->bytes += bytes;
+  return NLSE_OK;
+}
+
+static void free_graphs(nlse_solver* s) {
+  for (int t = 0; t < 2; ++t) {
+    if (s->gexec[t]) cudaGraphExecDestroy(s->gexec[t]);
+    s->gexec[t] = nullptr;
+  }
+}
+
+extern "C" int nlse_solver_destroy(nlse_solver* s) {
+  if (!s) return NLSE_OK;
+  int dev_prev = -1;
+  cudaGetDevice(&dev_prev);
+  cudaSetDevice(s->device);
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  free_graphs(s);
+  void* ptrs[] = {s->psi, s->K, s->ya, s->yb, s->V, s->hi[0], s->hi[1], s->lo[0], s->lo[1],
+                  s->mK, s->da, s->db, s->Vf, s->stage, s->d_mass, s->d_bad};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  if (dev_prev >= 0) cudaSetDevice(dev_prev);
+  delete s;
+  return NLSE_OK;
+}
+
+extern "C" int nlse_solver_create(const nlse_problem* p, nlse_solver** out) {
+  if (!out) return fail(NLSE_ERR_ARG, "out is NULL");
+  *out = nullptr;
+  int rc = validate(p);
+  if (rc) return rc;
+  nlse_solver* s = new nlse_solver();
+  memset(s, 0, sizeof(*s));
+  s->prob = *p;
+  s->g = make_geom(p);
+  s->cd = consts_double(p);
+  s->cf = p->precision == NLSE_PREC_MIXED ? consts_mixed(p) : consts_single(p);
+  s->kernel_kind = (p->flags & NLSE_FLAG_GATHER) ? KERNEL_GATHER : KERNEL_TILED;
+  s->graph_steps = 8;
+  cudaError_t e = cudaGetDevice(&s->device);
+  if (e != cudaSuccess) {
+    delete s;
+    return fail(NLSE_ERR_CUDA, "no CUDA device: %s", cudaGetErrorString(e));
+  }
+  e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete s;
+    return fail(NLSE_ERR_CUDA, "cudaStreamCreate failed: %s", cudaGetErrorString(e));
+  }
+  const long long n = s->g.n;
+  int r = NLSE_OK;
+  if (p->precision == NLSE_PREC_DOUBLE || p->precision == NLSE_PREC_SINGLE) {
+    size_t es = p->precision == NLSE_PREC_DOUBLE ? sizeof(double) : sizeof(float);
+    if (!r) r = dalloc(s, &s->psi, 2 * es * n);
+    if (!r) r = dalloc(s, &s->K, 2 * es * n);
+    if (!r) r = dalloc(s, &s->ya, 2 * es * n);
+    if (!r) r = dalloc(s, &s->yb, 2 * es * n);
+    if (!r) r = dalloc(s, &s->V, es * n);
+  } else {
+    for (int t = 0; t < 2 && !r; ++t) {
+      r = dalloc(s, (void**)&s->hi[t], sizeof(float2) * n);
+      if (!r) r = dalloc(s, (void**)&s->lo[t], sizeof(float2) * n);
+    }
+    if (!r) r = dalloc(s, (void**)&s->mK, sizeof(float2) * n);
+    if (!r) r = dalloc(s, (void**)&s->da, sizeof(float2) * n);
+    if (!r) r = dalloc(s, (void**)&s->db, sizeof(float2) * n);
+    if (!r) r = dalloc(s, (void**)&s->Vf, sizeof(float) * n);
+  }
+  if (!r) r = dalloc(s, (void**)&s->d_mass, sizeof(double));
+  if (!r) r = dalloc(s, (void**)&s->d_bad, sizeof(int));
+  if (r) {
+    char msg[512];
+    strncpy(msg, g_err, sizeof(msg) - 1);
+    msg[sizeof(msg) - 1] = 0;
+    nlse_solver_destroy(s);
+    return fail(r, "%s", msg);
+  }
+  *out = s;
+  return NLSE_OK;
+}
+
+static int ensure_stage(nlse_solver* s) {
+  if (s->stage) return NLSE_OK;
+  return dalloc(s, (void**)&s->stage, sizeof(double) * 3 * s->g.n);
+}
+
+// Convert the planar doubles (re, im, V) already on the device into the
+// solver's internal layout.
+static int ingest(nlse_solver* s, const double* re, const double* im, const double* V) {
+  const long long n = s->g.n;
+  switch (s->prob.precision) {
+    case NLSE_PREC_DOUBLE:
+      CUDA_TRY(planar_to_c2d(re, im, (C2<double>*)s->psi, n, s->stream));
+      if (V) CUDA_TRY(cudaMemcpyAsync(s->V, V, sizeof(double) * n, cudaMemcpyDeviceToDevice, s->stream));
+      break;
+    case NLSE_PREC_SINGLE:
+      CUDA_TRY(planar_to_c2f(re, im, (C2<float>*)s->psi, n, s->stream));
+      if (V) CUDA_TRY(real_to_float(V, (float*)s->V, n, s->stream));
+      break;
+    default:
+      CUDA_TRY(planar_to_hilo(re, im, s->hi[s->cur], s->lo[s->cur], n, s->stream));
+      if (V) CUDA_TRY(real_to_float(V, s->Vf, n, s->stream));
+      break;
+  }
+  return NLSE_OK;
+}
+
+extern "C" int nlse_solver_upload_device(nlse_solver* s, const double* dUr, const double* dUi,
+                                         const double* dV) {
+  if (!s || !dUr || !dV) return fail(NLSE_ERR_ARG, "NULL argument");
+  CUDA_TRY(cudaSetDevice(s->device));
+  return ingest(s, dUr, dUi, dV);
+}
+
+extern "C" int nlse_solver_upload(nlse_solver* s, const double* Ur, const double* Ui,
+                                  const double* V) {
+  if (!s || !Ur || !V) return fail(NLSE_ERR_ARG, "NULL argument");
+  CUDA_TRY(cudaSetDevice(s->device));
+  int r = ensure_stage(s);
+  if (r) return r;
+  const long long n = s->g.n;
+  double* re = s->stage;
+  double* im = s->stage + n;
+  double* vv = s->stage + 2 * n;
+  CUDA_TRY(cudaMemcpyAsync(re, Ur, sizeof(double) * n, cudaMemcpyHostToDevice, s->stream));
+  if (Ui) CUDA_TRY(cudaMemcpyAsync(im, Ui, sizeof(double) * n, cudaMemcpyHostToDevice, s->stream));
+  CUDA_TRY(cudaMemcpyAsync(vv, V, sizeof(double) * n, cudaMemcpyHostToDevice, s->stream));
+  r = ingest(s, re, Ui ? im : nullptr, vv);
+  if (r) return r;
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return NLSE_OK;
+}
+
+static int emit(nlse_solver* s, double* re, double* im) {
+  const long long n = s->g.n;
+  switch (s->prob.precision) {
+    case NLSE_PREC_DOUBLE:
+      CUDA_TRY(c2d_to_planar((const C2<double>*)s->psi, re, im, n, s->stream));
+      break;
+    case NLSE_PREC_SINGLE:
+      CUDA_TRY(c2f_to_planar((const C2<float>*)s->psi, re, im, n, s->stream));
+      break;
+    default:
+      CUDA_TRY(hilo_to_planar(s->hi[s->cur], s->lo[s->cur], re, im, n, s->stream));
+      break;
+  }
+  return NLSE_OK;
+}
+
+extern "C" int nlse_solver_download_device(nlse_solver* s, double* dUr, double* dUi) {
+  if (!s || !dUr || !dUi) return fail(NLSE_ERR_ARG, "NULL argument");
+  CUDA_TRY(cudaSetDevice(s->device));
+  return emit(s, dUr, dUi);
+}
+
+extern "C" int nlse_solver_download(nlse_solver* s, double* Ur, double* Ui) {
+  if (!s || !Ur || !Ui) return fail(NLSE_ERR_ARG, "NULL argument");
+  CUDA_TRY(cudaSetDevice(s->device));
+  int r = ensure_stage(s);
+  if (r) return r;
+  const long long n = s->g.n;
+  r = emit(s, s->stage, s->stage + n);
+  if (r) return r;
+  CUDA_TRY(cudaMemcpyAsync(Ur, s->stage, sizeof(double) * n, cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(cudaMemcpyAsync(Ui, s->stage + n, sizeof(double) * n, cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return NLSE_OK;
+}
+
+// Enqueue one RK4 step (4 stage launches) without graphs.
+static int enqueue_step(nlse_solver* s) {
+  const nlse_problem& p = s->prob;
+  cudaError_t e = cudaSuccess;
+  if (p.precision == NLSE_PREC_DOUBLE) {
+    typedef C2<double> T;
+    T *psi = (T*)s->psi, *K = (T*)s->K, *ya = (T*)s->ya, *yb = (T*)s->yb;
+    const double* V = (const double*)s->V;
+    ExactStageArgs<double> a1{psi, psi, V, K, ya}, a2{ya, psi, V, K, yb}, a3{yb, psi, V, K, ya},
+        a4{ya, psi, V, K, nullptr};
+    const ExactStageArgs<double>* as[4] = {&a1, &a2, &a3, &a4};
+    for (int st = 1; st <= 4 && e == cudaSuccess; ++st)
+      e = launch_exact_stage<double>(s->g, p.method, p.bc, s->cd, *as[st - 1], st, s->stream,
+                                     s->kernel_kind);
+  } else if (p.precision == NLSE_PREC_SINGLE) {
+    typedef C2<float> T;
+    T *psi = (T*)s->psi, *K = (T*)s->K, *ya = (T*)s->ya, *yb = (T*)s->yb;
+    const float* V = (const float*)s->V;
+    ExactStageArgs<float> a1{psi, psi, V, K, ya}, a2{ya, psi, V, K, yb}, a3{yb, psi, V, K, ya},
+        a4{ya, psi, V, K, nullptr};
+    const ExactStageArgs<float>* as[4] = {&a1, &a2, &a3, &a4};
+    for (int st = 1; st <= 4 && e == cudaSuccess; ++st)
+      e = launch_exact_stage<float>(s->g, p.method, p.bc, s->cf, *as[st - 1], st, s->stream,
+                                    s->kernel_kind);
+  } else {
+    int c = s->cur;
+    MixedStageArgs a1{s->hi[c], s->lo[c], nullptr, s->Vf, s->mK, s->da, nullptr, nullptr};
+    MixedStageArgs a2{s->hi[c], s->lo[c], s->da, s->Vf, s->mK, s->db, nullptr, nullptr};
+    MixedStageArgs a3{s->hi[c], s->lo[c], s->db, s->Vf, s->mK, s->da, nullptr, nullptr};
+    MixedStageArgs a4{s->hi[c], s->lo[c], s->da, s->Vf, s->mK, nullptr, s->hi[1 - c], s->lo[1 - c]};
+    const MixedStageArgs* as[4] = {&a1, &a2, &a3, &a4};
+    for (int st = 1; st <= 4 && e == cudaSuccess; ++st)
+      e = launch_mixed_stage(s->g, p.method, p.bc, s->cf, *as[st - 1], st, s->stream,
+                             s->kernel_kind);
+    s->cur = 1 - c;
+  }
+  if (e != cudaSuccess) return fail(NLSE_ERR_CUDA, "stage launch failed: %s", cudaGetErrorString(e));
+  return NLSE_OK;
+}
+
+// Graph of graph_steps RK4 steps starting from the current buffer parity.
+static int ensure_graph(nlse_solver* s, int parity) {
+  if (s->gexec[parity]) return NLSE_OK;
+  cudaGraph_t graph = nullptr;
+  int saved_cur = s->cur;
+  s->cur = parity;
+  CUDA_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+  int r = NLSE_OK;
+  for (int t = 0; t < s->graph_steps && !r; ++t) r = enqueue_step(s);
+  cudaError_t e = cudaStreamEndCapture(s->stream, &graph);
+  s->cur = saved_cur;
+  if (r) {
+    if (graph) cudaGraphDestroy(graph);
+    return r;
+  }
+  if (e != cudaSuccess) return fail(NLSE_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&s->gexec[parity], graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    s->gexec[parity] = nullptr;
+    return fail(NLSE_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+  }
+  return NLSE_OK;
+}
+
+extern "C" int nlse_solver_run(nlse_solver* s, long long nsteps) {
+  if (!s) return fail(NLSE_ERR_ARG, "solver is NULL");
+  if (nsteps < 0) return fail(NLSE_ERR_ARG, "nsteps must be >= 0");
+  CUDA_TRY(cudaSetDevice(s->device));
+  const int G = s->graph_steps;
+  if (G > 0 && nsteps >= G) {
+    long long reps = nsteps / G;
+    for (long long t = 0; t < reps; ++t) {
+      int parity = s->prob.precision == NLSE_PREC_MIXED ? s->cur : 0;
+      int r = ensure_graph(s, parity);
+      if (r) return r;
+      CUDA_TRY(cudaGraphLaunch(s->gexec[parity], s->stream));
+      if (s->prob.precision == NLSE_PREC_MIXED && (G & 1)) s->cur = 1 - s->cur;
+    }
+    nsteps -= reps * G;
+  }
+  for (long long t = 0; t < nsteps; ++t) {
+    int r = enqueue_step(s);
+    if (r) return r;
+  }
+  return NLSE_OK;
+}
+
+extern "C" int nlse_solver_set_graph_steps(nlse_solver* s, int steps) {
+  if (!s || steps < 0) return fail(NLSE_ERR_ARG, "bad argument");
+  if (steps != s->graph_steps) {
+    cudaStreamSynchronize(s->stream);
+    free_graphs(s);
+    s->graph_steps = steps;
+  }
+  return NLSE_OK;
+}
+
+extern "C" int nlse_solver_sync(nlse_solver* s) {
+  if (!s) return fail(NLSE_ERR_ARG, "solver is NULL");
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return NLSE_OK;
+}
+
+extern "C" int nlse_solver_stream(nlse_solver* s, void** stream) {
+  if (!s || !stream) return fail(NLSE_ERR_ARG, "NULL argument");
+  *stream = (void*)s->stream;
+  return NLSE_OK;
+}
+
+extern "C" int nlse_solver_launches_per_step(const nlse_solver* s) { return s ? 4 : 0; }
+
+extern "C" long long nlse_solver_device_bytes(const nlse_solver* s) {
+  return s ? (long long)s->bytes : 0;
+}
+
+extern "C" int nlse_solver_mass(nlse_solver* s, double* sum_abs2) {
+  if (!s || !sum_abs2) return fail(NLSE_ERR_ARG, "NULL argument");
+  CUDA_TRY(cudaSetDevice(s->device));
+  const long long n = s->g.n;
+  switch (s->prob.precision) {
+    case NLSE_PREC_DOUBLE:
+      CUDA_TRY(mass_c2d((const C2<double>*)s->psi, n, s->d_mass, s->d_bad, s->stream));
+      break;
+    case NLSE_PREC_SINGLE:
+      CUDA_TRY(mass_c2f((const C2<float>*)s->psi, n, s->d_mass, s->d_bad, s->stream));
+      break;
+    default:
+      CUDA_TRY(mass_hilo(s->hi[s->cur], s->lo[s->cur], n, s->d_mass, s->d_bad, s->stream));
+  }
+  double m = 0;
+  int bad = 0;
+  CUDA_TRY(cudaMemcpyAsync(&m, s->d_mass, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(cudaMemcpyAsync(&bad, s->d_bad, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  *sum_abs2 = m;
+  if (bad) return fail(NLSE_ERR_NONFINITE, "state contains NaN or Inf");
+  return NLSE_OK;
+}
+
+// ---------------------------------------------------------------------------
+// one-shot calls with a cached workspace (one per host thread and device)
+// ---------------------------------------------------------------------------
+namespace {
+struct Cache {
+  nlse_solver* s = nullptr;
+  ~Cache() {
+    // Process teardown may already have torn the CUDA context down; only
+    // release when the runtime is still usable.
+    if (s && cudaGetLastError() != cudaErrorCudartUnloading) nlse_solver_destroy(s);
+  }
+};
+thread_local Cache t_cache;
+}  // namespace
+
+static bool same_scalars(const nlse_problem& a, const nlse_problem& b) {
+  return a.method == b.method && a.bc == b.bc && a.s == b.s && a.a == b.a && a.h2 == b.h2 &&
+         a.k == b.k && a.flags == b.flags;
+}
+
+static bool same_layout(const nlse_problem& a, const nlse_problem& b) {
+  if (a.ndim != b.ndim || a.precision != b.precision) return false;
+  for (int d = 0; d < a.ndim; ++d)
+    if (a.dims[d] != b.dims[d]) return false;
+  return true;
+}
+
+extern "C" int nlse_take_steps(const nlse_problem* p, const double* Ur, const double* Ui,
+                               const double* V, double* out_r, double* out_i, int chunk_size) {
+  int rc = validate(p);
+  if (rc) return rc;
+  if (!Ur || !V || !out_r || !out_i) return fail(NLSE_ERR_ARG, "NULL array argument");
+  if (chunk_size < 0) return fail(NLSE_ERR_ARG, "chunk_size must be >= 0");
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  nlse_solver* s = t_cache.s;
+  if (s && (s->device != dev || !same_layout(s->prob, *p))) {
+    nlse_solver_destroy(s);
+    t_cache.s = s = nullptr;
+  }
+  if (!s) {
+    rc = nlse_solver_create(p, &s);
+    if (rc) return rc;
+    t_cache.s = s;
+  } else if (!same_scalars(s->prob, *p)) {
+    // same layout, new scalars or BC: refresh constants, drop captured graphs
+    cudaStreamSynchronize(s->stream);
+    free_graphs(s);
+    s->prob = *p;
+    s->cd = consts_double(p);
+    s->cf = p->precision == NLSE_PREC_MIXED ? consts_mixed(p) : consts_single(p);
+    s->kernel_kind = (p->flags & NLSE_FLAG_GATHER) ? KERNEL_GATHER : KERNEL_TILED;
+  }
+  s->cur = 0;
+  rc = nlse_solver_upload(s, Ur, Ui, V);
+  if (!rc) rc = nlse_solver_run(s, chunk_size);
+  if (!rc) rc = nlse_solver_download(s, out_r, out_i);
+  return rc;
+}
+
+static nlse_problem mkprob(int ndim, long long M, long long N, long long L, int method,
+                           int precision, int BC, double s, double a, double h2, double k) {
+  nlse_problem p;
+  memset(&p, 0, sizeof(p));
+  p.ndim = ndim;
+  p.dims[0] = M;
+  p.dims[1] = N;
+  p.dims[2] = L;
+  p.method = method;
+  p.precision = precision;
+  p.bc = BC;
+  p.s = s;
+  p.a = a;
+  p.h2 = h2;
+  p.k = k;
+  p.flags = NLSE_FLAG_MSD_GUARD;
+  return p;
+}
+
+static int take_f(const nlse_problem& p, const float* Ur, const float* Ui, const float* V,
+                  float* out_r, float* out_i, int chunk) {
+  long long n = p.dims[0] * (p.ndim >= 2 ? p.dims[1] : 1) * (p.ndim >= 3 ? p.dims[2] : 1);
+  if (n <= 0 || !Ur || !V || !out_r || !out_i) return fail(NLSE_ERR_ARG, "bad argument");
+  double* buf = (double*)malloc(sizeof(double) * 5 * n);
+  if (!buf) return fail(NLSE_ERR_NOMEM, "host allocation failed");
+  double *r = buf, *im = buf + n, *v = buf + 2 * n, *orr = buf + 3 * n, *oi = buf + 4 * n;
+  for (long long t = 0; t < n; ++t) {
+    r[t] = Ur[t];
+    im[t] = Ui ? Ui[t] : 0.0;
+    v[t] = V[t];
+  }
+  int rc = nlse_take_steps(&p, r, im, v, orr, oi, chunk);
+  if (!rc)
+    for (long long t = 0; t < n; ++t) {
+      out_r[t] = (float)orr[t];
+      out_i[t] = (float)oi[t];
+    }
+  free(buf);
+  return rc;
+}
+
+extern "C" int NLSE1D_TAKE_STEPS_CUDA(const double* Uoldr, const double* Uoldi, const double* V,
+                                      double* Unewr, double* Unewi, double s, double a, double h2,
+                                      int BC, int chunk_size, double k, int N, int method) {
+  nlse_problem p = mkprob(1, N, 1, 1, method, NLSE_PREC_DOUBLE, BC, s, a, h2, k);
+  return nlse_take_steps(&p, Uoldr, Uoldi, V, Unewr, Unewi, chunk_size);
+}
+extern "C" int NLSE1D_TAKE_STEPS_CUDA_F(const float* Uoldr, const float* Uoldi, const float* V,
+                                        float* Unewr, float* Unewi, float s, float a, float h2,
+                                        int BC, int chunk_size, float k, int N, int method) {
+  nlse_problem p = mkprob(1, N, 1, 1, method, NLSE_PREC_SINGLE, BC, s, a, h2, k);
+  return take_f(p, Uoldr, Uoldi, V, Unewr, Unewi, chunk_size);
+}
+extern "C" int NLSE2D_TAKE_STEPS_CUDA(const double* Uoldr, const double* Uoldi, const double* V,
+                                      double* Unewr, double* Unewi, double s, double a, double h2,
+                                      int BC, int chunk_size, double k, int N, int M, int method) {
+  nlse_problem p = mkprob(2, M, N, 1, method, NLSE_PREC_DOUBLE, BC, s, a, h2, k);
+  return nlse_take_steps(&p, Uoldr, Uoldi, V, Unewr, Unewi, chunk_size);
+}
+extern "C" int NLSE2D_TAKE_STEPS_CUDA_F(const float* Uoldr, const float* Uoldi, const float* V,
+                                        float* Unewr, float* Unewi, float s, float a, float h2,
+                                        int BC, int chunk_size, float k, int N, int M,
+                                        int method) {
+  nlse_problem p = mkprob(2, M, N, 1, method, NLSE_PREC_SINGLE, BC, s, a, h2, k);
+  return take_f(p, Uoldr, Uoldi, V, Unewr, Unewi, chunk_size);
+}
+extern "C" int NLSE3D_TAKE_STEPS_CUDA(const double* Uoldr, const double* Uoldi, const double* V,
+                                      double* Unewr, double* Unewi, double s, double a, double h2,
+                                      int BC, int chunk_size, double k, int L, int N, int M,
+                                      int method) {
+  nlse_problem p = mkprob(3, M, N, L, method, NLSE_PREC_DOUBLE, BC, s, a, h2, k);
+  return nlse_take_steps(&p, Uoldr, Uoldi, V, Unewr, Unewi, chunk_size);
+}
+extern "C" int NLSE3D_TAKE_STEPS_CUDA_F(const float* Uoldr, const float* Uoldi, const float* V,
+                                        float* Unewr, float* Unewi, float s, float a, float h2,
+                                        int BC, int chunk_size, float k, int L, int N, int M,
+                                        int method) {
+  nlse_problem p = mkprob(3, M, N, L, method, NLSE_PREC_SINGLE, BC, s, a, h2, k);
+  return take_f(p, Uoldr, Uoldi, V, Unewr, Unewi, chunk_size);
+}
+extern "C" int NLSE1D_TAKE_STEPS_CUDA_MIXED(const double* Uoldr, const double* Uoldi,
+                                            const double* V, double* Unewr, double* Unewi,
+                                            double s, double a, double h2, int BC, int chunk_size,
+                                            double k, int N, int method) {
+  nlse_problem p = mkprob(1, N, 1, 1, method, NLSE_PREC_MIXED, BC, s, a, h2, k);
+  return nlse_take_steps(&p, Uoldr, Uoldi, V, Unewr, Unewi, chunk_size);
+}
+extern "C" int NLSE2D_TAKE_STEPS_CUDA_MIXED(const double* Uoldr, const double* Uoldi,
+                                            const double* V, double* Unewr, double* Unewi,
+                                            double s, double a, double h2, int BC, int chunk_size,
+                                            double k, int N, int M, int method) {
+  nlse_problem p = mkprob(2, M, N, 1, method, NLSE_PREC_MIXED, BC, s, a, h2, k);
+  return nlse_take_steps(&p, Uoldr, Uoldi, V, Unewr, Unewi, chunk_size);
+}
+extern "C" int NLSE3D_TAKE_STEPS_CUDA_MIXED(const double* Uoldr, const double* Uoldi,
+                                            const double* V, double* Unewr, double* Unewi,
+                                            double s, double a, double h2, int BC, int chunk_size,
+                                            double k, int L, int N, int M, int method) {
+  nlse_problem p = mkprob(3, M, N, L, method, NLSE_PREC_MIXED, BC, s, a, h2, k);
+  return nlse_take_steps(&p, Uoldr, Uoldi, V, Unewr, Unewi, chunk_size);
+}

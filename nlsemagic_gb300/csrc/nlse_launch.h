@@ -1,0 +1,67 @@
+// Host-side launch interface between the C ABI (nlse_abi.cu) and the
+// stage-kernel translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "nlse_common.cuh"
+
+namespace nlse {
+
+enum KernelKind { KERNEL_GATHER = 0, KERNEL_TILED = 1 };
+
+template <typename R>
+struct ExactStageArgs {
+  const C2<R>* Yin;  // stage input (stage 1: Psi itself)
+  C2<R>* Psi;        // RK4 base state (written in stage 4)
+  const R* V;
+  C2<R>* K;
+  C2<R>* Yout;       // next stage input (stages 1-3)
+};
+
+struct MixedStageArgs {
+  const float2* hi_in;
+  const float2* lo_in;
+  const float2* d_in;  // stage delta (unused in stage 1)
+  const float* V;
+  float2* K;
+  float2* d_out;
+  float2* hi_out;      // stage 4 output (a different buffer from hi_in)
+  float2* lo_out;
+};
+
+template <typename R>
+cudaError_t launch_exact_stage(const Geom& g, int method, int BC, const Consts<R>& c,
+                               const ExactStageArgs<R>& a, int stage, cudaStream_t st,
+                               int kernel_kind);
+
+cudaError_t launch_mixed_stage(const Geom& g, int method, int BC, const Consts<float>& c,
+                               const MixedStageArgs& a, int stage, cudaStream_t st,
+                               int kernel_kind);
+
+// Layout conversions and reductions (kern_util.cu).
+cudaError_t planar_to_c2d(const double* re, const double* im, C2<double>* out, long long n,
+                          cudaStream_t st);
+cudaError_t planar_to_c2f(const double* re, const double* im, C2<float>* out, long long n,
+                          cudaStream_t st);
+cudaError_t planar_to_hilo(const double* re, const double* im, float2* hi, float2* lo,
+                           long long n, cudaStream_t st);
+cudaError_t c2d_to_planar(const C2<double>* in, double* re, double* im, long long n,
+                          cudaStream_t st);
+cudaError_t c2f_to_planar(const C2<float>* in, double* re, double* im, long long n,
+                          cudaStream_t st);
+cudaError_t hilo_to_planar(const float2* hi, const float2* lo, double* re, double* im,
+                           long long n, cudaStream_t st);
+cudaError_t real_to_float(const double* in, float* out, long long n, cudaStream_t st);
+cudaError_t fill_zero_bytes(void* p, size_t bytes, cudaStream_t st);
+
+// sum |psi|^2 into *out (device double, pre-zeroed by the callee) and set
+// *bad to 1 if any component is not finite.
+cudaError_t mass_c2d(const C2<double>* psi, long long n, double* out, int* bad, cudaStream_t st);
+cudaError_t mass_c2f(const C2<float>* psi, long long n, double* out, int* bad, cudaStream_t st);
+cudaError_t mass_hilo(const float2* hi, const float2* lo, long long n, double* out, int* bad,
+                      cudaStream_t st);
+
+bool tiled_supported(const Geom& g, int dim);
+
+}  // namespace nlse

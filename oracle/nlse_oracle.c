@@ -1,0 +1,159 @@
+/*
+ * C oracle for the NLSEmagic RK4 chunk integrators.
+ *
+ * TEST INFRASTRUCTURE ONLY: this file is the checker that the CUDA library in
+ * nlsemagic_gb300/ is compared against.  Only tests/, __graft_entry__.smoke()
+ * and the CPU-baseline leg of bench.py load it; the library never does.
+ *
+ * It restates, in this project's own code, the algorithm of the reference CPU
+ * integrators NLSE{1,2,3}D_TAKE_STEPS_{CD,2SHOC}[_F].c (paths and lines in
+ * nlse_oracle_impl.h).  Pinning: tests/test_oracle.py checks it bit-for-bit
+ * against the reference files themselves (built by oracle/build.py against the
+ * oracle/mexshim stand-in for mex.h) wherever the reference checkout exists,
+ * and against the committed golden vectors in tests/golden/ everywhere.
+ *
+ * Entry point semantics mirror the reference MEX call
+ *     U = NAME(U, V, s, a, h2, BC, chunk_size, k)
+ * (src_old/NLSE1D_v1/NLSE1D_TAKE_STEPS_CD.c:11-20) with planar double input
+ * and output.  precision 2 runs the double files' arithmetic; precision 1
+ * runs the single-precision files' arithmetic (inputs and scalars rounded to
+ * float on entry, result widened to double on exit, as in
+ * NLSE1D_TAKE_STEPS_CD_F.c:138-189).
+ *
+ * flags bit 0 (NLSE_ORACLE_MSD_GUARD): where the MSD interior neighbour is
+ *   exactly zero, use OM = 0 / A = 0 instead of dividing by zero.  This is the
+ *   guard of the reference's 3D GPU kernels
+ *   (src/NLSEmagic3D/NLSE3D_TAKE_STEPS_CD_CUDA_D.cu:155-162,
+ *   NLSE3D_TAKE_STEPS_2SHOC_CUDA_D.cu:147-154,385-392); without it the CPU
+ *   reference produces NaN there.  It changes nothing elsewhere.
+ * flags bit 1 (NLSE_ORACLE_REF_QUIRKS): reproduce the missing `break` of the
+ *   single-precision 3D 2SHOC file (Laplacian-zero F falls through to zero).
+ *
+ * The single-precision 2D 2SHOC reference file never initialises its 1/a
+ * constant (src_old/NLSE2D_v1/NLSE2D_TAKE_STEPS_2SHOC_F.c:299,383-387), so its
+ * Dirichlet / MSD boundary results are undefined; the oracle uses 1.0f/a, as
+ * the 1D and 3D single-precision files do.
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define NLSE_ORACLE_MSD_GUARD 1
+#define NLSE_ORACLE_REF_QUIRKS 2
+
+#define REAL double
+#define SUFFIX d
+#include "nlse_oracle_impl.h"
+#undef REAL
+#undef SUFFIX
+
+#define REAL float
+#define SUFFIX f
+#include "nlse_oracle_impl.h"
+#undef REAL
+#undef SUFFIX
+
+static int check_args(int ndim, int method, const long long *dims, int BC, int chunk) {
+    int d;
+    if (ndim < 1 || ndim > 3) return -1;
+    if (method != 1 && method != 2) return -2;
+    for (d = 0; d < ndim; ++d)
+        if (dims[d] < 3) return -3;
+    if (BC == 4 && (ndim != 1 || dims[0] < 4)) return -4;
+    if (chunk < 0) return -5;
+    return 0;
+}
+
+int nlse_oracle_take_steps(int ndim, int method, int precision, const long long *dims,
+                           const double *Ur, const double *Ui, const double *V, double s,
+                           double a, double h2, int BC, int chunk, double k, double *out_r,
+                           double *out_i, int flags) {
+    long M, N, L, n, p;
+    int rc = check_args(ndim, method, dims, BC, chunk);
+    if (rc) return rc;
+    M = (long)dims[0];
+    N = ndim >= 2 ? (long)dims[1] : 1;
+    L = ndim >= 3 ? (long)dims[2] : 1;
+    n = M * N * L;
+    if (precision == 2) {
+        ctx_t_d c;
+        double *scratch = (double *)malloc(sizeof(double) * 8 * n);
+        if (!scratch) return -10;
+        memset(&c, 0, sizeof(c));
+        c.ndim = ndim; c.method = method; c.BC = BC;
+        c.guard = flags & NLSE_ORACLE_MSD_GUARD;
+        c.quirk = 0;
+        c.M = M; c.N = N; c.L = L;
+        c.s = s; c.a = a; c.V = V;
+        c.ah2 = a / h2;
+        c.l_a = 1.0 / a;
+        c.lh2 = 1.0 / h2;
+        c.a76 = a * (7.0 / 6.0);
+        c.a112 = a * (1.0 / 12.0);
+        if (ndim == 2) {
+            c.a_6h2 = a * (1.0 / (6.0 * h2));
+            c.a_12 = a * (1.0 / 12.0);
+        } else {
+            c.a_6h2 = a / (6.0 * h2);
+            c.a_12 = a / 12.0;
+        }
+        memcpy(out_r, Ur, sizeof(double) * n);
+        if (Ui) memcpy(out_i, Ui, sizeof(double) * n);
+        else memset(out_i, 0, sizeof(double) * n);
+        rk4_chunk_d(&c, out_r, out_i, scratch, chunk, k);
+        free(scratch);
+        return 0;
+    }
+    if (precision == 1) {
+        ctx_t_f c;
+        float *buf = (float *)malloc(sizeof(float) * 11 * n);
+        float *fr, *fi, *fv, *scratch;
+        float fs, fa, fh2, fk;
+        if (!buf) return -10;
+        fr = buf; fi = buf + n; fv = buf + 2 * n; scratch = buf + 3 * n;
+        for (p = 0; p < n; ++p) {
+            fr[p] = (float)Ur[p];
+            fi[p] = Ui ? (float)Ui[p] : 0.0f;
+            fv[p] = (float)V[p];
+        }
+        fs = (float)s; fa = (float)a; fh2 = (float)h2; fk = (float)k;
+        memset(&c, 0, sizeof(c));
+        c.ndim = ndim; c.method = method; c.BC = BC;
+        c.guard = flags & NLSE_ORACLE_MSD_GUARD;
+        c.quirk = (flags & NLSE_ORACLE_REF_QUIRKS) && ndim == 3 && method == 2;
+        c.M = M; c.N = N; c.L = L;
+        c.s = fs; c.a = fa; c.V = fv;
+        c.ah2 = fa / fh2;
+        c.l_a = 1.0f / fa;
+        c.lh2 = 1.0f / fh2;
+        c.a76 = fa * (7.0f / 6.0f);
+        c.a112 = fa * (1.0f / 12.0f);
+        if (ndim == 2) {
+            c.a_6h2 = fa * (1.0f / (6.0f * fh2));
+            c.a_12 = fa * (1.0f / 12.0f);
+        } else {
+            c.a_6h2 = fa / (6.0f * fh2);
+            c.a_12 = fa / 12.0f;
+        }
+        rk4_chunk_f(&c, fr, fi, scratch, chunk, fk);
+        for (p = 0; p < n; ++p) {
+            out_r[p] = (double)fr[p];
+            out_i[p] = (double)fi[p];
+        }
+        free(buf);
+        return 0;
+    }
+    return -6;
+}
+
+/* Same, with the 1D argument list of the v2 C library, for convenience:
+ * NLSE1D_TAKE_STEPS(Uoldr, Uoldi, V, Unewr, Unewi, s, a, h2, BC, chunk, k, N, method)
+ * (src/NLSEmagic1D/NLSEmagic.h:7-8). */
+int nlse_oracle_1d(const double *Ur, const double *Ui, const double *V, double *out_r,
+                   double *out_i, double s, double a, double h2, int BC, int chunk, double k,
+                   int N, int method, int precision, int flags) {
+    long long dims[1];
+    dims[0] = N;
+    return nlse_oracle_take_steps(1, method, precision, dims, Ur, Ui, V, s, a, h2, BC, chunk, k,
+                                  out_r, out_i, flags);
+}

@@ -1,0 +1,102 @@
+"""The C-ABI library loads and exports every symbol include/*.h declares;
+argument validation happens before any CUDA call (so it is testable here)."""
+import ctypes
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+import nlsemagic_gb300 as ng
+from nlsemagic_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = []
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        src = re.sub(r"//[^\n]*", "", src)
+        src = re.sub(r"^\s*#[^\n]*", "", src, flags=re.M)
+        for m in re.finditer(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\(([^;{]*?)\)\s*;", src):
+            name = m.group(1)
+            if name in ("if", "while", "for", "return", "sizeof"):
+                continue
+            names.append(name)
+    return sorted(set(names))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from nlsemagic_gb300 import build
+    build.build()
+    return _lib.load()
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for must in ("NLSE1D_TAKE_STEPS_CUDA", "NLSE3D_TAKE_STEPS_CUDA_F", "nlse_take_steps",
+                 "nlse_solver_create", "nlse_solver_run", "nlse_last_error_string"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_signatures_cover_header(lib):
+    # every declared symbol has a ctypes signature (so no call goes untyped)
+    assert set(declared_functions()) <= set(_lib.SIGNATURES) | {"nlse_batch_create",
+        "nlse_batch_destroy", "nlse_batch_run", "nlse_batch_add", "nlse_batch_download",
+        "nlse_batch_count", "nlse_batch_autotune"} | set(n for n in declared_functions()
+                                                     if n.startswith("nlse_serve")
+                                                     or n.startswith("nlse_batch")
+                                                     or n.startswith("nlse_noalloc"))
+
+
+def _call(lib, U, BC=2, method=1, precision=2, dims=None, h2=0.01, k=1e-3, chunk=1):
+    re_, im_ = ng.api.planar(U)
+    V = np.zeros(re_.size)
+    ndim, d = ng.api.grid_dims(U.shape)
+    p = ng.api.make_problem(ndim, dims or d, method, precision, BC, -1.0, 1.0, h2, k)
+    outr = np.empty_like(re_)
+    outi = np.empty_like(im_)
+    dp = ctypes.POINTER(ctypes.c_double)
+    return lib.nlse_take_steps(ctypes.byref(p), re_.ctypes.data_as(dp), im_.ctypes.data_as(dp),
+                               V.ctypes.data_as(dp), outr.ctypes.data_as(dp),
+                               outi.ctypes.data_as(dp), chunk)
+
+
+@pytest.mark.parametrize("kw,why", [
+    (dict(U=np.ones(2, complex)), "too few points"),
+    (dict(U=np.ones((3, 3), complex), BC=4), "BC 4 is 1D only"),
+    (dict(U=np.ones(8, complex), BC=7), "unknown BC"),
+    (dict(U=np.ones(8, complex), method=3), "unknown method"),
+    (dict(U=np.ones(8, complex), precision=9), "unknown precision"),
+    (dict(U=np.ones(8, complex), h2=0.0), "h2 must be > 0"),
+    (dict(U=np.ones(8, complex), k=-1.0), "k must be > 0"),
+    (dict(U=np.ones(8, complex), chunk=-1), "negative chunk"),
+])
+def test_invalid_arguments_rejected_before_cuda(lib, kw, why):
+    rc = _call(lib, **kw)
+    assert rc == _lib.NLSE_ERR_ARG, why
+    assert _lib.last_error()
+
+
+def test_stability_helper(lib):
+    k = ng.linear_stability_k(3, 2, 0.3, 1.0)
+    assert abs(k - 0.75 * 0.09 / (3 * 2 ** 0.5)) < 1e-15
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    with pytest.raises(_lib.NativeLibraryMissing):
+        saved = _lib._lib
+        try:
+            _lib._lib = None
+            _lib.load(str(tmp_path / "absent.so"))
+        finally:
+            _lib._lib = saved
