@@ -259,10 +259,12 @@ def run_gpu(args, w):
         solver.upload_device(Ur.data_ptr(), Ui.data_ptr(), Vd.data_ptr())
         solver.run(steps)
 
+    t0 = time.perf_counter()
     for _ in range(args.warmup):
         job()
     solver.sync()
     torch.cuda.synchronize()
+    log("warmup: %d jobs in %.2f s" % (args.warmup, time.perf_counter() - t0))
     barrier(world)
 
     start = torch.cuda.Event(enable_timing=True)
@@ -278,6 +280,7 @@ def run_gpu(args, w):
         torch.cuda.synchronize()
         barrier(world)
     t_ms = start.elapsed_time(end)
+    log("timed: %d jobs in %.1f ms" % (args.steps, t_ms))
     t_ms = max_over_ranks(t_ms, world)
     clocks = clk.summary()
     pts = float(n) * steps * args.steps * world
@@ -317,6 +320,7 @@ def run_gpu(args, w):
     for _ in range(ke):
         e2e_call()
     t_e2e = time.perf_counter() - t0
+    log("e2e: %d calls in %.2f s" % (ke, t_e2e))
     t_e2e = max_over_ranks(t_e2e, world)
     e2e_value = float(n) * steps * ke * world / t_e2e / 1e9
     e2e_out = (oR.numpy() + 1j * oI.numpy()).reshape(w.U.shape, order="F")
@@ -332,7 +336,7 @@ def run_gpu(args, w):
                         h2=w.h2, k=w.k)
         st64 = torch.cuda.ExternalStream(s64.stream)
         s64.upload_device(Ur.data_ptr(), Ui.data_ptr(), Vd.data_ptr())
-        s64.run(2)
+        s64.run(max(1, args.graph_steps))  # captures the graph outside the timed run
         s64.sync()
         s64.upload_device(Ur.data_ptr(), Ui.data_ptr(), Vd.data_ptr())
         e0 = torch.cuda.Event(enable_timing=True)

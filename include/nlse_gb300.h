@@ -176,6 +176,46 @@ int nlse_solver_launches_per_step(const nlse_solver *s);
 /* Bytes of device memory held by the solver. */
 long long nlse_solver_device_bytes(const nlse_solver *s);
 
+/* ------------------------------------------------------------------------
+ * Batched solves: many independent solves of uneven dimension, size,
+ * method, boundary code and precision class (FP64 or mixed) advance together
+ * in one persistent cooperative launch per call of nlse_batch_run, driven by
+ * a tile work queue (one pass over all tiles per RK4 stage, separated by a
+ * bounded grid barrier).  State lives in a device pool of a fixed byte
+ * budget; solves are admitted while the pool has room and keep their state
+ * resident until removed.  No reference counterpart (the reference runs one
+ * solve per MEX call).
+ * ---------------------------------------------------------------------- */
+typedef struct nlse_batch nlse_batch;
+
+/* pool_bytes: device memory budget for solve state; max_solves: slots. */
+int nlse_batch_create(long long pool_bytes, int max_solves, nlse_batch **out);
+int nlse_batch_destroy(nlse_batch *b);
+/* Device bytes a solve of this problem occupies in the pool. */
+long long nlse_batch_bytes_for(const nlse_problem *p);
+/* Admit a solve that is to advance nsteps RK4 steps.  Host planar arrays
+ * (Ui may be NULL).  Returns NLSE_ERR_CAPACITY (no slot or no pool room),
+ * leaving the batch unchanged.  precision must be NLSE_PREC_DOUBLE or
+ * NLSE_PREC_MIXED. */
+int nlse_batch_add(nlse_batch *b, const nlse_problem *p, const double *Ur, const double *Ui,
+                   const double *V, long long nsteps, int *slot);
+/* Advance every unfinished solve by up to max_steps RK4 steps (one
+ * persistent launch; asynchronous on the batch stream). */
+int nlse_batch_run(nlse_batch *b, int max_steps);
+/* Steps still to run for a slot (host view, exact after nlse_batch_sync). */
+int nlse_batch_remaining(nlse_batch *b, int slot, long long *steps_left);
+/* Copy a slot's state to host planar arrays (waits for queued work). */
+int nlse_batch_download(nlse_batch *b, int slot, double *Ur, double *Ui);
+/* Release a slot and its pool memory. */
+int nlse_batch_remove(nlse_batch *b, int slot);
+int nlse_batch_sync(nlse_batch *b);
+/* Active solves, total grid points, and free pool bytes. */
+int nlse_batch_stats(nlse_batch *b, int *active, long long *points, long long *free_bytes);
+/* cudaStream_t of the batch. */
+int nlse_batch_stream(nlse_batch *b, void **stream);
+/* Kernel launches issued by the last nlse_batch_run (1 when any solve ran). */
+int nlse_batch_last_launches(nlse_batch *b);
+
 /* Linear stability limit of the time step used by the NLSEmagic drivers:
  * h^2 / (ndim * sqrt(2) * a) for CD, 3/4 of that for 2SHOC
  * (src/NLSEmagic3D/NLSEmagic3D.m:154-163). */

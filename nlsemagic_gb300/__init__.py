@@ -10,6 +10,6 @@ CPU fallback: without the built library every call raises
 from ._lib import (FLAG_GATHER, FLAG_MSD_GUARD, PREC_DOUBLE, PREC_MIXED, PREC_SINGLE,  # noqa: F401
                    NativeLibraryMissing, NLSEError, load)
 from .api import *  # noqa: F401,F403
-from .api import Solver, linear_stability_k, take_steps  # noqa: F401
+from .api import Batch, Solver, linear_stability_k, take_steps  # noqa: F401
 
 __version__ = "1.0.0"

@@ -73,6 +73,19 @@ SIGNATURES = {
     "nlse_solver_set_graph_steps": (_i, [_vp, _i]),
     "nlse_solver_launches_per_step": (_i, [_vp]),
     "nlse_solver_device_bytes": (_ll, [_vp]),
+    "nlse_batch_create": (_i, [_ll, _i, ctypes.POINTER(_vp)]),
+    "nlse_batch_destroy": (_i, [_vp]),
+    "nlse_batch_bytes_for": (_ll, [ctypes.POINTER(Problem)]),
+    "nlse_batch_add": (_i, [_vp, ctypes.POINTER(Problem), _dp, _dp, _dp, _ll,
+                            ctypes.POINTER(_i)]),
+    "nlse_batch_run": (_i, [_vp, _i]),
+    "nlse_batch_remaining": (_i, [_vp, _i, ctypes.POINTER(_ll)]),
+    "nlse_batch_download": (_i, [_vp, _i, _dp, _dp]),
+    "nlse_batch_remove": (_i, [_vp, _i]),
+    "nlse_batch_sync": (_i, [_vp]),
+    "nlse_batch_stats": (_i, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_ll), ctypes.POINTER(_ll)]),
+    "nlse_batch_stream": (_i, [_vp, ctypes.POINTER(_vp)]),
+    "nlse_batch_last_launches": (_i, [_vp]),
 }
 for _dim, _dims in ((1, [_i]), (2, [_i, _i]), (3, [_i, _i, _i])):
     SIGNATURES["NLSE%dD_TAKE_STEPS_CUDA" % _dim] = (

@@ -225,3 +225,90 @@ class Solver:
     @property
     def device_bytes(self) -> int:
         return int(self._lib.nlse_solver_device_bytes(self._h))
+
+
+class Batch:
+    """Many independent solves advancing together in one persistent launch
+    per :meth:`run` call (FP64 and mixed precision classes may be mixed).
+
+    ``pool_bytes`` is the device memory budget for solve state; :meth:`add`
+    raises :class:`~nlsemagic_gb300._lib.NLSEError` with code
+    NLSE_ERR_CAPACITY when a solve does not fit."""
+
+    def __init__(self, pool_bytes, max_solves=4096):
+        self._lib = load()
+        h = ctypes.c_void_p()
+        check(self._lib.nlse_batch_create(int(pool_bytes), int(max_solves), ctypes.byref(h)))
+        self._h = h
+        self.shapes = {}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.nlse_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def bytes_for(shape, precision):
+        ndim, dims = grid_dims(shape)
+        p = make_problem(ndim, dims, 1, precision, 1, 0.0, 1.0, 1.0, 1.0)
+        return int(load().nlse_batch_bytes_for(ctypes.byref(p)))
+
+    def add(self, U, V, s, a, h2, BC, nsteps, k, method=2, precision=PREC_MIXED,
+            flags=FLAG_MSD_GUARD):
+        U = np.asarray(U)
+        ndim, dims = grid_dims(U.shape)
+        p = make_problem(ndim, dims, method, precision, BC, s, a, h2, k, flags)
+        re, im = planar(U)
+        vv = np.ascontiguousarray(np.asarray(V, dtype=np.float64).ravel(order="F"))
+        slot = ctypes.c_int()
+        check(self._lib.nlse_batch_add(self._h, ctypes.byref(p), _ptr(re), _ptr(im), _ptr(vv),
+                                       int(nsteps), ctypes.byref(slot)))
+        self.shapes[slot.value] = U.shape
+        return slot.value
+
+    def run(self, max_steps):
+        check(self._lib.nlse_batch_run(self._h, int(max_steps)))
+
+    def sync(self):
+        check(self._lib.nlse_batch_sync(self._h))
+
+    def remaining(self, slot):
+        out = ctypes.c_longlong()
+        check(self._lib.nlse_batch_remaining(self._h, int(slot), ctypes.byref(out)))
+        return out.value
+
+    def download(self, slot):
+        shape = self.shapes[slot]
+        n = int(np.prod(shape))
+        re = np.empty(n)
+        im = np.empty(n)
+        check(self._lib.nlse_batch_download(self._h, int(slot), _ptr(re), _ptr(im)))
+        return (re + 1j * im).reshape(shape, order="F")
+
+    def remove(self, slot):
+        check(self._lib.nlse_batch_remove(self._h, int(slot)))
+        self.shapes.pop(slot, None)
+
+    def stats(self):
+        a = ctypes.c_int()
+        pts = ctypes.c_longlong()
+        free = ctypes.c_longlong()
+        check(self._lib.nlse_batch_stats(self._h, ctypes.byref(a), ctypes.byref(pts),
+                                         ctypes.byref(free)))
+        return {"active": a.value, "points": pts.value, "free_bytes": free.value}
+
+    @property
+    def stream(self):
+        st = ctypes.c_void_p()
+        check(self._lib.nlse_batch_stream(self._h, ctypes.byref(st)))
+        return st.value or 0
+
+    @property
+    def last_launches(self):
+        return int(self._lib.nlse_batch_last_launches(self._h))

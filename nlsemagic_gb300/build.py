@@ -32,7 +32,7 @@ UNITS = {
     "kern_stream3d.cu": [],
     "kern_util.cu": [],
     "nlse_abi.cu": [],
-    "nlse_batch.cu": [],
+    "nlse_batch.cu": ["-fmad=false"],
 }
 
 

@@ -26,41 +26,61 @@ __device__ __forceinline__ long long lin(const Geom& g, int i, int j, int k) {
 // =========================== exact precisions ================================
 namespace exact {
 
+template <typename R, int DIM>
+__device__ __forceinline__ C2<R> d_int_at(const Geom& g, const Consts<R>& c, const C2<R>* U,
+                                          long long p) {
+  if (DIM == 1) return d_int_1d<R>(c, U[p + 1], U[p], U[p - 1]);
+  if (DIM == 2) {
+    const long long M = g.M;
+    return d_int_2d<R>(c, U[p + M], U[p - M], U[p], U[p + 1], U[p - 1]);
+  }
+  const long long M = g.M, P = g.P;
+  return d_int_3d<R>(c, U[p + P], U[p - P], U[p + M], U[p - M], U[p + 1], U[p - 1], U[p]);
+}
+
 template <typename R, int DIM, int BC>
 __device__ C2<R> d_at(const Geom& g, const Consts<R>& c, const C2<R>* U, const R* V, int i, int j,
                       int k) {
   long long p = lin(g, i, j, k);
-  if (is_interior(g, i, j, k)) return d_interior<R, DIM>(g, c, U, p);
+  if (is_interior(g, i, j, k)) return d_int_at<R, DIM>(g, c, U, p);
+  if (BC == 4) {
+    const long long N = g.M;
+    if (p == 0) return d_onesided<R>(c, U[3], U[2], U[1], U[0]);
+    return d_onesided<R>(c, U[N - 4], U[N - 3], U[N - 2], U[N - 1]);
+  }
   long long q = msd_neighbour(g, i, j, k);
   C2<R> dq = {0, 0};
-  if (BC == 2) dq = d_interior<R, DIM>(g, c, U, q);
-  return d_boundary<R, DIM, BC>(g, c, U, V, p, q, dq);
+  if (BC == 2) dq = d_int_at<R, DIM>(g, c, U, q);
+  return d_bnd<R, BC>(c, U[p], V[p], U[q], V[q], dq);
 }
 
 template <typename R, int DIM, int METHOD, int BC>
 __device__ C2<R> f_int(const Geom& g, const Consts<R>& c, const C2<R>* U, const R* V, int i, int j,
                        int k) {
   long long p = lin(g, i, j, k);
-  if (METHOD == 1) return f_interior_cd<R, DIM>(g, c, U, V, p);
-  C2<R> d0 = d_at<R, DIM, BC>(g, c, U, V, i, j, k);
-  C2<R> dn[6];
-  if (DIM == 1) {
-    dn[0] = d_at<R, DIM, BC>(g, c, U, V, i, j, k + 1);
-    dn[1] = d_at<R, DIM, BC>(g, c, U, V, i, j, k - 1);
-  } else if (DIM == 2) {
-    dn[0] = d_at<R, DIM, BC>(g, c, U, V, i, j + 1, k);
-    dn[1] = d_at<R, DIM, BC>(g, c, U, V, i, j - 1, k);
-    dn[2] = d_at<R, DIM, BC>(g, c, U, V, i, j, k + 1);
-    dn[3] = d_at<R, DIM, BC>(g, c, U, V, i, j, k - 1);
-  } else {
-    dn[0] = d_at<R, DIM, BC>(g, c, U, V, i + 1, j, k);
-    dn[1] = d_at<R, DIM, BC>(g, c, U, V, i - 1, j, k);
-    dn[2] = d_at<R, DIM, BC>(g, c, U, V, i, j + 1, k);
-    dn[3] = d_at<R, DIM, BC>(g, c, U, V, i, j - 1, k);
-    dn[4] = d_at<R, DIM, BC>(g, c, U, V, i, j, k + 1);
-    dn[5] = d_at<R, DIM, BC>(g, c, U, V, i, j, k - 1);
+  const long long M = g.M, P = g.P;
+  if (METHOD == 1) {
+    if (DIM == 1) return f_cd_1d<R>(c, U[p], V[p], U[p + 1], U[p - 1]);
+    if (DIM == 2) return f_cd_2d<R>(c, U[p], V[p], U[p + M], U[p - M], U[p + 1], U[p - 1]);
+    return f_cd_3d<R>(c, U[p], V[p], U[p + P], U[p - P], U[p + M], U[p - M], U[p + 1], U[p - 1]);
   }
-  return f_interior_2shoc<R, DIM>(g, c, U, V, p, d0, dn);
+  C2<R> d0 = d_at<R, DIM, BC>(g, c, U, V, i, j, k);
+  if (DIM == 1) {
+    return f_2shoc_1d<R>(c, U[p], V[p], d0, d_at<R, DIM, BC>(g, c, U, V, i, j, k + 1),
+                         d_at<R, DIM, BC>(g, c, U, V, i, j, k - 1));
+  }
+  if (DIM == 2) {
+    C2<R> dn[4] = {d_at<R, DIM, BC>(g, c, U, V, i, j + 1, k), d_at<R, DIM, BC>(g, c, U, V, i, j - 1, k),
+                   d_at<R, DIM, BC>(g, c, U, V, i, j, k + 1), d_at<R, DIM, BC>(g, c, U, V, i, j, k - 1)};
+    C2<R> dg[4] = {U[p + M + 1], U[p + M - 1], U[p - M + 1], U[p - M - 1]};
+    return f_2shoc_2d<R>(c, U[p], V[p], d0, dn, dg);
+  }
+  C2<R> dn[6] = {d_at<R, DIM, BC>(g, c, U, V, i + 1, j, k), d_at<R, DIM, BC>(g, c, U, V, i - 1, j, k),
+                 d_at<R, DIM, BC>(g, c, U, V, i, j + 1, k), d_at<R, DIM, BC>(g, c, U, V, i, j - 1, k),
+                 d_at<R, DIM, BC>(g, c, U, V, i, j, k + 1), d_at<R, DIM, BC>(g, c, U, V, i, j, k - 1)};
+  C2<R> e[12] = {U[p + P + M], U[p + M + 1], U[p + P + 1], U[p - P - M], U[p - M - 1], U[p - P - 1],
+                 U[p + P - M], U[p + M - 1], U[p + P - 1], U[p - P + M], U[p - M + 1], U[p - P + 1]};
+  return f_2shoc_3d<R>(c, U[p], V[p], d0, dn, e);
 }
 
 template <typename R, int DIM, int METHOD, int BC>
@@ -68,6 +88,11 @@ __device__ C2<R> f_at(const Geom& g, const Consts<R>& c, const C2<R>* U, const R
                       int k) {
   if (is_interior(g, i, j, k)) return f_int<R, DIM, METHOD, BC>(g, c, U, V, i, j, k);
   long long b = lin(g, i, j, k);
+  if (BC == 4) {
+    const long long N = g.M;
+    if (b == 0) return f_onesided<R, METHOD>(c, U[0], V[0], U[3], U[2], U[1], U[0]);
+    return f_onesided<R, METHOD>(c, U[N - 1], V[N - 1], U[N - 4], U[N - 3], U[N - 2], U[N - 1]);
+  }
   long long q = msd_neighbour(g, i, j, k);
   C2<R> fq = {0, 0};
   if (BC == 2) {
@@ -75,39 +100,7 @@ __device__ C2<R> f_at(const Geom& g, const Consts<R>& c, const C2<R>* U, const R
     decompose(g, q, qi, qj, qk);
     fq = f_int<R, DIM, METHOD, BC>(g, c, U, V, qi, qj, qk);
   }
-  return f_boundary<R, DIM, METHOD, BC>(g, c, U, V, b, q, fq);
-}
-
-// RK4 stage update in the reference's vec_add order
-// (src_old/NLSE1D_v1/NLSE1D_TAKE_STEPS_CD.c:158-168):
-//  1: K = T;        Y' = Psi + k/2 T
-//  2: K = K + 2 T;  Y' = Psi + k/2 T
-//  3: K = K + 2 T;  Y' = Psi + k T
-//  4: K = K + 1 T;  Psi = Psi + k/6 K
-template <typename R>
-__device__ __forceinline__ void update(const Consts<R>& c, int stage, long long p, C2<R> T,
-                                       C2<R>* Psi, C2<R>* K, C2<R>* Yout) {
-  C2<R> ps = Psi[p];
-  if (stage == 1) {
-    K[p] = T;
-    C2<R> y = {ps.r + c.k2 * T.r, ps.i + c.k2 * T.i};
-    Yout[p] = y;
-  } else if (stage == 2 || stage == 3) {
-    C2<R> kk = K[p];
-    kk.r = kk.r + (R)2.0 * T.r;
-    kk.i = kk.i + (R)2.0 * T.i;
-    K[p] = kk;
-    R cf = stage == 2 ? c.k2 : c.k;
-    C2<R> y = {ps.r + cf * T.r, ps.i + cf * T.i};
-    Yout[p] = y;
-  } else {
-    C2<R> kk = K[p];
-    kk.r = kk.r + (R)1.0 * T.r;
-    kk.i = kk.i + (R)1.0 * T.i;
-    ps.r = ps.r + c.k6 * kk.r;
-    ps.i = ps.i + c.k6 * kk.i;
-    Psi[p] = ps;
-  }
+  return f_bnd<R, BC>(c, U[b], V[b], U[q], fq);
 }
 
 template <typename R, int DIM, int METHOD, int BC>

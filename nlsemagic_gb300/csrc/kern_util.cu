@@ -208,8 +208,6 @@ cudaError_t mass_hilo(const float2* hi, const float2* lo, long long n, double* o
 namespace nlse {
 // Shapes handled by the tiled kernels (kern_tiled.cuh); others use gather.
 bool tiled_supported(const Geom& g, int dim) {
-  (void)g;
-  (void)dim;
-  return false;
+  return dim == 3 && g.ndim == 3 && g.M >= 3 && g.N >= 3 && g.L >= 3;
 }
 }  // namespace nlse

@@ -36,6 +36,16 @@ static int fail(int code, const char* fmt, ...) {
   } while (0)
 
 extern "C" const char* nlse_last_error_string(void) { return g_err; }
+
+namespace nlse {
+int set_error(int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return code;
+}
+}  // namespace nlse
 extern "C" const char* nlse_version(void) { return "nlse_gb300 1.0 (sm_103a)"; }
 
 extern "C" double nlse_linear_stability_k(int ndim, int method, double h, double a) {
@@ -73,6 +83,8 @@ static int validate(const nlse_problem* p) {
   if (!isfinite(p->s)) return fail(NLSE_ERR_ARG, "s must be finite");
   return NLSE_OK;
 }
+
+int nlse_validate_problem(const nlse_problem* p) { return validate(p); }
 
 static Geom make_geom(const nlse_problem* p) {
   Geom g;
@@ -163,6 +175,11 @@ static Consts<float> consts_mixed(const nlse_problem* p) {
   c.kinv2 = (float)d.kinv2;
   c.msd_guard = d.msd_guard;
   return c;
+}
+
+void nlse_fill_consts(const nlse_problem* p, void* cd, void* cf) {
+  *(Consts<double>*)cd = consts_double(p);
+  *(Consts<float>*)cf = p->precision == NLSE_PREC_MIXED ? consts_mixed(p) : consts_single(p);
 }
 
 // ---------------------------------------------------------------------------

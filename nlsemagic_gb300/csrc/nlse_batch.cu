@@ -1,0 +1,604 @@
+// Batched solves in one persistent launch (C ABI: nlse_batch_* in
+// include/nlse_gb300.h).
+//
+// Device side: a cooperative persistent kernel.  All active solves are cut
+// into tiles of TILE consecutive grid points; per RK4 stage every CTA pulls
+// tiles from an atomic work-queue counter of that stage until the queue is
+// empty, evaluates the stage with the gather-form stencil (kern_gather.cuh)
+// for the tile's solve, and then waits at a grid barrier.  The barrier spins
+// with a bounded clock budget; if it runs out, the kernel records
+// NLSE_ERR_TIMEOUT in an error word and every CTA returns.  Solves that have
+// finished their step count skip their tiles, so solves of different
+// lengths share a launch.
+//
+// Host side: a fixed-size device pool with a first-fit allocator holds the
+// solve state; a slot table and the tile list are rebuilt when the set of
+// running solves changes.
+//
+// This unit is compiled with -fmad=false so that the FP64 solves are
+// bit-identical to the single-solve path and to the reference integrators.
+#include <stdio.h>
+#include <string.h>
+
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "../../include/nlse_gb300.h"
+#include "kern_gather.cuh"
+#include "nlse_launch.h"
+
+using namespace nlse;
+
+namespace {
+
+constexpr int TILE = 1024;
+constexpr int BT = 256;  // threads per CTA
+
+struct BSolve {
+  Geom g;
+  int method, bc, prec, cur;
+  long long steps_left;  // steps this solve still runs when the launch starts
+  Consts<double> cd;
+  Consts<float> cf;
+  void* buf[8];
+  // exact: psi, K, ya, yb, V ; mixed: hi0, hi1, lo0, lo1, K, da, db, V
+};
+
+struct BTile {
+  int solve;
+  int pad;
+  long long start;
+};
+
+// ---------------------------------------------------------------- device --
+
+template <typename R, int DIM, int METHOD, int BC>
+__device__ __noinline__ void tile_exact(const BSolve& s, int stage, long long p0, long long p1) {
+  typedef C2<R> T2;
+  T2* psi = (T2*)s.buf[0];
+  T2* K = (T2*)s.buf[1];
+  T2* ya = (T2*)s.buf[2];
+  T2* yb = (T2*)s.buf[3];
+  const R* V = (const R*)s.buf[4];
+  const T2* Yin = stage == 1 ? psi : (stage == 3 ? yb : ya);
+  T2* Yout = stage == 2 ? yb : ya;
+  const Consts<R>& c = *reinterpret_cast<const Consts<R>*>(&s.cd);
+  for (long long p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
+    int i, j, k;
+    decompose(s.g, p, i, j, k);
+    T2 T = exact::f_at<R, DIM, METHOD, BC>(s.g, c, Yin, V, i, j, k);
+    exact::update<R>(c, stage, p, T, psi, K, Yout);
+  }
+}
+
+template <int DIM, int METHOD, int BC>
+__device__ __noinline__ void tile_mixed(const BSolve& s, int stage, int par, long long p0,
+                                        long long p1) {
+  const float2* hi_in = (const float2*)s.buf[par];
+  const float2* lo_in = (const float2*)s.buf[2 + par];
+  float2* hi_out = (float2*)s.buf[1 - par];
+  float2* lo_out = (float2*)s.buf[3 - par];
+  float2* K = (float2*)s.buf[4];
+  float2* da = (float2*)s.buf[5];
+  float2* db = (float2*)s.buf[6];
+  const float* V = (const float*)s.buf[7];
+  const float2* d_in = stage == 3 ? db : da;
+  float2* d_out = stage == 2 ? db : da;
+  mixed::YIn Y{hi_in, lo_in, stage == 1 ? nullptr : d_in};
+  for (long long p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
+    int i, j, k;
+    decompose(s.g, p, i, j, k);
+    float2 T = mixed::f_at<DIM, METHOD, BC>(s.g, s.cf, Y, V, i, j, k);
+    mixed::update(s.cf, stage, p, T, hi_in, lo_in, d_in, K, d_out, hi_out, lo_out);
+  }
+}
+
+template <int DIM, int METHOD>
+__device__ void by_bc(const BSolve& s, int stage, int par, long long p0, long long p1) {
+  if (s.prec == NLSE_PREC_DOUBLE) {
+    switch (s.bc) {
+      case 1: tile_exact<double, DIM, METHOD, 1>(s, stage, p0, p1); break;
+      case 2: tile_exact<double, DIM, METHOD, 2>(s, stage, p0, p1); break;
+      case 3: tile_exact<double, DIM, METHOD, 3>(s, stage, p0, p1); break;
+      default:
+        if (DIM == 1) tile_exact<double, 1, METHOD, 4>(s, stage, p0, p1);
+        break;
+    }
+  } else {
+    switch (s.bc) {
+      case 1: tile_mixed<DIM, METHOD, 1>(s, stage, par, p0, p1); break;
+      case 2: tile_mixed<DIM, METHOD, 2>(s, stage, par, p0, p1); break;
+      case 3: tile_mixed<DIM, METHOD, 3>(s, stage, par, p0, p1); break;
+      default:
+        if (DIM == 1) tile_mixed<1, METHOD, 4>(s, stage, par, p0, p1);
+        break;
+    }
+  }
+}
+
+__device__ void process_tile(const BSolve& s, int stage, int par, long long p0, long long p1) {
+  if (s.method == 1) {
+    if (s.g.ndim == 1) by_bc<1, 1>(s, stage, par, p0, p1);
+    else if (s.g.ndim == 2) by_bc<2, 1>(s, stage, par, p0, p1);
+    else by_bc<3, 1>(s, stage, par, p0, p1);
+  } else {
+    if (s.g.ndim == 1) by_bc<1, 2>(s, stage, par, p0, p1);
+    else if (s.g.ndim == 2) by_bc<2, 2>(s, stage, par, p0, p1);
+    else by_bc<3, 2>(s, stage, par, p0, p1);
+  }
+}
+
+struct BarrierState {
+  unsigned count;
+  unsigned gen;
+};
+
+// Grid barrier with a bounded wait.  All CTAs are co-resident (cooperative
+// launch).  Returns false if the wait budget ran out (error word set).
+__device__ bool grid_barrier(BarrierState* bar, int* err, long long budget) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    s_ok = 1;
+    volatile unsigned* vgen = &bar->gen;
+    unsigned g = *vgen;
+    __threadfence();
+    unsigned arrived = atomicAdd(&bar->count, 1u);
+    if (arrived == gridDim.x - 1) {
+      bar->count = 0;
+      __threadfence();
+      atomicAdd(&bar->gen, 1u);
+    } else {
+      long long t0 = clock64();
+      while (*vgen == g) {
+        if (*(volatile int*)err) {
+          s_ok = 0;
+          break;
+        }
+        if (clock64() - t0 > budget) {
+          atomicExch(err, NLSE_ERR_TIMEOUT);
+          s_ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+__global__ void __launch_bounds__(BT) batch_kernel(const BSolve* __restrict__ solves,
+                                                   const BTile* __restrict__ tiles, int ntiles,
+                                                   int steps, unsigned* qctr, BarrierState* bar,
+                                                   int* err, long long budget) {
+  __shared__ BSolve s;
+  __shared__ int s_t;
+  for (int step = 0; step < steps; ++step) {
+    for (int stage = 1; stage <= 4; ++stage) {
+      const int pass = step * 4 + stage - 1;
+      while (true) {
+        if (threadIdx.x == 0) s_t = (int)atomicAdd(&qctr[pass], 1u);
+        __syncthreads();
+        const int t = s_t;
+        if (t >= ntiles) break;
+        const BTile tl = tiles[t];
+        // cooperative copy of the solve descriptor into shared memory
+        {
+          const int* src = reinterpret_cast<const int*>(&solves[tl.solve]);
+          int* dst = reinterpret_cast<int*>(&s);
+          for (int w = threadIdx.x; w < (int)(sizeof(BSolve) / sizeof(int)); w += blockDim.x)
+            dst[w] = src[w];
+        }
+        __syncthreads();
+        if (step < s.steps_left) {
+          long long p1 = tl.start + TILE;
+          if (p1 > s.g.n) p1 = s.g.n;
+          process_tile(s, stage, s.cur ^ (step & 1), tl.start, p1);
+        }
+        __syncthreads();
+      }
+      if (!grid_barrier(bar, err, budget)) return;
+    }
+  }
+}
+
+}  // namespace
+
+// Shared with nlse_abi.cu: error reporting, validation, scalar constants.
+namespace nlse {
+int set_error(int code, const char* fmt, ...);
+}
+int nlse_validate_problem(const nlse_problem* p);
+void nlse_fill_consts(const nlse_problem* p, void* cd, void* cf);
+
+#define BTRY(expr)                                                                       \
+  do {                                                                                   \
+    cudaError_t e_ = (expr);                                                             \
+    if (e_ != cudaSuccess) {                                                             \
+      char m_[400];                                                                      \
+      snprintf(m_, sizeof(m_), "%s failed: %s", #expr, cudaGetErrorString(e_));          \
+      return nlse::set_error(e_ == cudaErrorMemoryAllocation ? NLSE_ERR_NOMEM : NLSE_ERR_CUDA, "%s", m_); \
+    }                                                                                    \
+  } while (0)
+
+static const size_t ALIGN = 256;
+static size_t al(size_t x) { return (x + ALIGN - 1) / ALIGN * ALIGN; }
+
+struct Slot {
+  bool used = false;
+  nlse_problem prob;
+  BSolve d;
+  size_t offset = 0, bytes = 0;
+};
+
+struct nlse_batch {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  char* pool = nullptr;
+  size_t pool_bytes = 0;
+  std::map<size_t, size_t> free_list;  // offset -> size
+  std::vector<Slot> slots;
+  // device tables
+  BSolve* d_solves = nullptr;
+  BTile* d_tiles = nullptr;
+  size_t tiles_cap = 0;
+  unsigned* d_qctr = nullptr;
+  size_t qctr_cap = 0;
+  BarrierState* d_bar = nullptr;
+  int* d_err = nullptr;
+  // pinned host mirrors
+  BSolve* h_solves = nullptr;
+  BTile* h_tiles = nullptr;
+  // staging for transfers (planar doubles)
+  double* stage = nullptr;
+  size_t stage_cap = 0;
+  int max_blocks = 0;
+  int last_launches = 0;
+};
+
+static bool layout(const nlse_problem* p, size_t* sizes, int* nbuf) {
+  long long n = p->dims[0] * (p->ndim >= 2 ? p->dims[1] : 1) * (p->ndim >= 3 ? p->dims[2] : 1);
+  if (p->precision == NLSE_PREC_DOUBLE) {
+    for (int t = 0; t < 4; ++t) sizes[t] = 16 * (size_t)n;
+    sizes[4] = 8 * (size_t)n;
+    *nbuf = 5;
+  } else if (p->precision == NLSE_PREC_MIXED) {
+    for (int t = 0; t < 7; ++t) sizes[t] = 8 * (size_t)n;
+    sizes[7] = 4 * (size_t)n;
+    *nbuf = 8;
+  } else {
+    return false;
+  }
+  return true;
+}
+
+extern "C" long long nlse_batch_bytes_for(const nlse_problem* p) {
+  size_t sz[8];
+  int nb = 0;
+  if (!p || !layout(p, sz, &nb)) return -1;
+  size_t tot = 0;
+  for (int t = 0; t < nb; ++t) tot += al(sz[t]);
+  return (long long)tot;
+}
+
+static bool pool_alloc(nlse_batch* b, size_t bytes, size_t* off) {
+  for (auto it = b->free_list.begin(); it != b->free_list.end(); ++it) {
+    if (it->second >= bytes) {
+      *off = it->first;
+      size_t rest = it->second - bytes;
+      size_t noff = it->first + bytes;
+      b->free_list.erase(it);
+      if (rest) b->free_list[noff] = rest;
+      return true;
+    }
+  }
+  return false;
+}
+
+static void pool_free(nlse_batch* b, size_t off, size_t bytes) {
+  auto it = b->free_list.emplace(off, bytes).first;
+  // merge with next
+  auto nx = std::next(it);
+  if (nx != b->free_list.end() && it->first + it->second == nx->first) {
+    it->second += nx->second;
+    b->free_list.erase(nx);
+  }
+  // merge with previous
+  if (it != b->free_list.begin()) {
+    auto pv = std::prev(it);
+    if (pv->first + pv->second == it->first) {
+      pv->second += it->second;
+      b->free_list.erase(it);
+    }
+  }
+}
+
+extern "C" int nlse_batch_destroy(nlse_batch* b) {
+  if (!b) return NLSE_OK;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  void* dp[] = {b->pool, b->d_solves, b->d_tiles, b->d_qctr, b->d_bar, b->d_err, b->stage};
+  for (void* p : dp)
+    if (p) cudaFree(p);
+  if (b->h_solves) cudaFreeHost(b->h_solves);
+  if (b->h_tiles) cudaFreeHost(b->h_tiles);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return NLSE_OK;
+}
+
+extern "C" int nlse_batch_create(long long pool_bytes, int max_solves, nlse_batch** out) {
+  if (!out || pool_bytes <= 0 || max_solves <= 0)
+    return nlse::set_error(NLSE_ERR_ARG, "pool_bytes and max_solves must be > 0");
+  *out = nullptr;
+  nlse_batch* b = new nlse_batch();
+  int rc = NLSE_OK;
+  auto cleanup = [&](int code) {
+    nlse_batch_destroy(b);
+    return code;
+  };
+  if (cudaGetDevice(&b->device) != cudaSuccess) return cleanup(nlse::set_error(NLSE_ERR_CUDA, "no CUDA device"));
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return cleanup(nlse::set_error(NLSE_ERR_CUDA, "cudaStreamCreate failed"));
+  b->pool_bytes = al((size_t)pool_bytes);
+  if (cudaMalloc(&b->pool, b->pool_bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return cleanup(nlse::set_error(NLSE_ERR_NOMEM, "pool allocation of %lld bytes failed", pool_bytes));
+  }
+  b->free_list[0] = b->pool_bytes;
+  b->slots.resize(max_solves);
+  if (cudaMalloc(&b->d_solves, sizeof(BSolve) * max_solves) != cudaSuccess ||
+      cudaMalloc(&b->d_bar, sizeof(BarrierState)) != cudaSuccess ||
+      cudaMalloc(&b->d_err, sizeof(int)) != cudaSuccess ||
+      cudaMallocHost(&b->h_solves, sizeof(BSolve) * max_solves) != cudaSuccess) {
+    cudaGetLastError();
+    return cleanup(nlse::set_error(NLSE_ERR_NOMEM, "batch table allocation failed"));
+  }
+  cudaMemsetAsync(b->d_bar, 0, sizeof(BarrierState), b->stream);
+  cudaMemsetAsync(b->d_err, 0, sizeof(int), b->stream);
+  int sms = 0, per_sm = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, BT, 0);
+  if (per_sm < 1) return cleanup(nlse::set_error(NLSE_ERR_CUDA, "batch kernel cannot be resident"));
+  b->max_blocks = sms * per_sm;
+  (void)rc;
+  *out = b;
+  return NLSE_OK;
+}
+
+static int ensure_stage(nlse_batch* b, size_t doubles) {
+  if (b->stage_cap >= doubles) return NLSE_OK;
+  if (b->stage) cudaFree(b->stage);
+  b->stage = nullptr;
+  b->stage_cap = 0;
+  BTRY(cudaMalloc(&b->stage, doubles * sizeof(double)));
+  b->stage_cap = doubles;
+  return NLSE_OK;
+}
+
+extern "C" int nlse_batch_add(nlse_batch* b, const nlse_problem* p, const double* Ur,
+                              const double* Ui, const double* V, long long nsteps, int* slot) {
+  if (!b || !p || !Ur || !V || !slot) return nlse::set_error(NLSE_ERR_ARG, "NULL argument");
+  if (nsteps < 0) return nlse::set_error(NLSE_ERR_ARG, "nsteps must be >= 0");
+  if (p->precision != NLSE_PREC_DOUBLE && p->precision != NLSE_PREC_MIXED)
+    return nlse::set_error(NLSE_ERR_ARG, "batched solves are FP64 or mixed precision");
+  {
+    int rc = nlse_validate_problem(p);  // same rules as single solves
+    if (rc) return rc;
+  }
+  int idx = -1;
+  for (size_t t = 0; t < b->slots.size(); ++t)
+    if (!b->slots[t].used) {
+      idx = (int)t;
+      break;
+    }
+  if (idx < 0) return nlse::set_error(NLSE_ERR_CAPACITY, "no free batch slot");
+  size_t sz[8];
+  int nb = 0;
+  layout(p, sz, &nb);
+  size_t tot = (size_t)nlse_batch_bytes_for(p);
+  size_t off = 0;
+  if (!pool_alloc(b, tot, &off)) return nlse::set_error(NLSE_ERR_CAPACITY, "batch pool full");
+  BTRY(cudaSetDevice(b->device));
+  Slot& S = b->slots[idx];
+  S.used = true;
+  S.prob = *p;
+  S.offset = off;
+  S.bytes = tot;
+  memset(&S.d, 0, sizeof(S.d));
+  S.d.g.ndim = p->ndim;
+  S.d.g.M = (int)p->dims[0];
+  S.d.g.N = p->ndim >= 2 ? (int)p->dims[1] : 1;
+  S.d.g.L = p->ndim >= 3 ? (int)p->dims[2] : 1;
+  S.d.g.P = S.d.g.N * S.d.g.M;
+  S.d.g.n = (long long)S.d.g.L * S.d.g.N * S.d.g.M;
+  S.d.method = p->method;
+  S.d.bc = p->bc;
+  S.d.prec = p->precision;
+  S.d.cur = 0;
+  S.d.steps_left = nsteps;
+  nlse_fill_consts(p, &S.d.cd, &S.d.cf);
+  size_t o = off;
+  for (int t = 0; t < nb; ++t) {
+    S.d.buf[t] = b->pool + o;
+    o += al(sz[t]);
+  }
+  // upload
+  const long long n = S.d.g.n;
+  int rc = ensure_stage(b, 3 * (size_t)n);
+  if (rc) {
+    pool_free(b, S.offset, S.bytes);
+    S.used = false;
+    return rc;
+  }
+  double *re = b->stage, *im = b->stage + n, *vv = b->stage + 2 * n;
+  BTRY(cudaMemcpyAsync(re, Ur, sizeof(double) * n, cudaMemcpyHostToDevice, b->stream));
+  if (Ui) BTRY(cudaMemcpyAsync(im, Ui, sizeof(double) * n, cudaMemcpyHostToDevice, b->stream));
+  BTRY(cudaMemcpyAsync(vv, V, sizeof(double) * n, cudaMemcpyHostToDevice, b->stream));
+  if (p->precision == NLSE_PREC_DOUBLE) {
+    BTRY(planar_to_c2d(re, Ui ? im : nullptr, (C2<double>*)S.d.buf[0], n, b->stream));
+    BTRY(cudaMemcpyAsync(S.d.buf[4], vv, sizeof(double) * n, cudaMemcpyDeviceToDevice, b->stream));
+  } else {
+    BTRY(planar_to_hilo(re, Ui ? im : nullptr, (float2*)S.d.buf[0], (float2*)S.d.buf[2], n,
+                        b->stream));
+    BTRY(real_to_float(vv, (float*)S.d.buf[7], n, b->stream));
+  }
+  BTRY(cudaStreamSynchronize(b->stream));  // host buffers reusable on return
+  *slot = idx;
+  return NLSE_OK;
+}
+
+extern "C" int nlse_batch_run(nlse_batch* b, int max_steps) {
+  if (!b || max_steps < 0) return nlse::set_error(NLSE_ERR_ARG, "bad argument");
+  BTRY(cudaSetDevice(b->device));
+  BTRY(cudaStreamSynchronize(b->stream));  // host mirrors may be rewritten below
+  b->last_launches = 0;
+  int err = 0;
+  BTRY(cudaMemcpy(&err, b->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (err) return nlse::set_error(err, "a previous batch launch gave up waiting at a grid barrier");
+  // solve table + tile list of the solves that still run
+  int nsolves = 0;
+  long long ntiles = 0;
+  int steps = 0;
+  std::vector<int> which;
+  for (size_t t = 0; t < b->slots.size(); ++t) {
+    Slot& S = b->slots[t];
+    if (!S.used || S.d.steps_left <= 0) continue;
+    which.push_back((int)t);
+    ntiles += (S.d.g.n + TILE - 1) / TILE;
+    long long adv = S.d.steps_left < max_steps ? S.d.steps_left : max_steps;
+    if (adv > steps) steps = (int)adv;
+  }
+  if (which.empty() || steps == 0) return NLSE_OK;
+  if (ntiles > (1LL << 31) - 1) return nlse::set_error(NLSE_ERR_CAPACITY, "too many tiles");
+  if ((size_t)ntiles > b->tiles_cap) {
+    if (b->d_tiles) cudaFree(b->d_tiles);
+    if (b->h_tiles) cudaFreeHost(b->h_tiles);
+    b->d_tiles = nullptr;
+    b->h_tiles = nullptr;
+    size_t cap = (size_t)ntiles * 2;
+    BTRY(cudaMalloc(&b->d_tiles, sizeof(BTile) * cap));
+    BTRY(cudaMallocHost(&b->h_tiles, sizeof(BTile) * cap));
+    b->tiles_cap = cap;
+  }
+  size_t passes = (size_t)steps * 4;
+  if (passes > b->qctr_cap) {
+    if (b->d_qctr) cudaFree(b->d_qctr);
+    b->d_qctr = nullptr;
+    BTRY(cudaMalloc(&b->d_qctr, sizeof(unsigned) * passes));
+    b->qctr_cap = passes;
+  }
+  long long tt = 0;
+  for (int id : which) {
+    Slot& S = b->slots[id];
+    b->h_solves[nsolves] = S.d;
+    long long nt = (S.d.g.n + TILE - 1) / TILE;
+    for (long long q = 0; q < nt; ++q) {
+      b->h_tiles[tt].solve = nsolves;
+      b->h_tiles[tt].pad = 0;
+      b->h_tiles[tt].start = q * TILE;
+      ++tt;
+    }
+    ++nsolves;
+  }
+  BTRY(cudaMemcpyAsync(b->d_solves, b->h_solves, sizeof(BSolve) * nsolves, cudaMemcpyHostToDevice,
+                       b->stream));
+  BTRY(cudaMemcpyAsync(b->d_tiles, b->h_tiles, sizeof(BTile) * ntiles, cudaMemcpyHostToDevice,
+                       b->stream));
+  BTRY(cudaMemsetAsync(b->d_qctr, 0, sizeof(unsigned) * passes, b->stream));
+  BTRY(cudaMemsetAsync(b->d_bar, 0, sizeof(BarrierState), b->stream));
+  int blocks = b->max_blocks;
+  if ((long long)blocks > ntiles) blocks = (int)ntiles;
+  int nt_i = (int)ntiles;
+  long long budget = 100000000000LL;  // clock cycles a CTA may wait at one barrier
+  void* args[] = {&b->d_solves, &b->d_tiles, &nt_i, &steps, &b->d_qctr, &b->d_bar, &b->d_err,
+                  &budget};
+  BTRY(cudaLaunchCooperativeKernel((const void*)batch_kernel, dim3(blocks), dim3(BT), args, 0,
+                                   b->stream));
+  b->last_launches = 1;
+  // host bookkeeping of the steps each solve advanced in this launch
+  for (int id : which) {
+    Slot& S = b->slots[id];
+    long long adv = S.d.steps_left < steps ? S.d.steps_left : steps;
+    S.d.steps_left -= adv;
+    if (S.d.prec == NLSE_PREC_MIXED && (adv & 1)) S.d.cur ^= 1;
+  }
+  return NLSE_OK;
+}
+
+extern "C" int nlse_batch_sync(nlse_batch* b) {
+  if (!b) return nlse::set_error(NLSE_ERR_ARG, "batch is NULL");
+  BTRY(cudaStreamSynchronize(b->stream));
+  int err = 0;
+  BTRY(cudaMemcpy(&err, b->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (err) return nlse::set_error(err, "batch launch gave up waiting at a grid barrier");
+  return NLSE_OK;
+}
+
+extern "C" int nlse_batch_remaining(nlse_batch* b, int slot, long long* steps_left) {
+  if (!b || !steps_left || slot < 0 || slot >= (int)b->slots.size() || !b->slots[slot].used)
+    return nlse::set_error(NLSE_ERR_ARG, "bad slot");
+  *steps_left = b->slots[slot].d.steps_left;
+  return NLSE_OK;
+}
+
+extern "C" int nlse_batch_download(nlse_batch* b, int slot, double* Ur, double* Ui) {
+  if (!b || !Ur || !Ui || slot < 0 || slot >= (int)b->slots.size() || !b->slots[slot].used)
+    return nlse::set_error(NLSE_ERR_ARG, "bad slot or NULL array");
+  int rc = nlse_batch_sync(b);
+  if (rc) return rc;
+  Slot& S = b->slots[slot];
+  const long long n = S.d.g.n;
+  rc = ensure_stage(b, 2 * (size_t)n);
+  if (rc) return rc;
+  if (S.d.prec == NLSE_PREC_DOUBLE) {
+    BTRY(c2d_to_planar((const C2<double>*)S.d.buf[0], b->stage, b->stage + n, n, b->stream));
+  } else {
+    int c = S.d.cur;
+    BTRY(hilo_to_planar((const float2*)S.d.buf[c], (const float2*)S.d.buf[2 + c], b->stage,
+                        b->stage + n, n, b->stream));
+  }
+  BTRY(cudaMemcpyAsync(Ur, b->stage, sizeof(double) * n, cudaMemcpyDeviceToHost, b->stream));
+  BTRY(cudaMemcpyAsync(Ui, b->stage + n, sizeof(double) * n, cudaMemcpyDeviceToHost, b->stream));
+  BTRY(cudaStreamSynchronize(b->stream));
+  return NLSE_OK;
+}
+
+extern "C" int nlse_batch_remove(nlse_batch* b, int slot) {
+  if (!b || slot < 0 || slot >= (int)b->slots.size() || !b->slots[slot].used)
+    return nlse::set_error(NLSE_ERR_ARG, "bad slot");
+  BTRY(cudaStreamSynchronize(b->stream));
+  Slot& S = b->slots[slot];
+  pool_free(b, S.offset, S.bytes);
+  S.used = false;
+  return NLSE_OK;
+}
+
+extern "C" int nlse_batch_stats(nlse_batch* b, int* active, long long* points,
+                                long long* free_bytes) {
+  if (!b) return nlse::set_error(NLSE_ERR_ARG, "batch is NULL");
+  int a = 0;
+  long long pts = 0;
+  for (auto& S : b->slots)
+    if (S.used) {
+      ++a;
+      pts += S.d.g.n;
+    }
+  long long fb = 0;
+  for (auto& kv : b->free_list) fb += (long long)kv.second;
+  if (active) *active = a;
+  if (points) *points = pts;
+  if (free_bytes) *free_bytes = fb;
+  return NLSE_OK;
+}
+
+extern "C" int nlse_batch_stream(nlse_batch* b, void** stream) {
+  if (!b || !stream) return nlse::set_error(NLSE_ERR_ARG, "NULL argument");
+  *stream = (void*)b->stream;
+  return NLSE_OK;
+}
+
+extern "C" int nlse_batch_last_launches(nlse_batch* b) { return b ? b->last_launches : 0; }

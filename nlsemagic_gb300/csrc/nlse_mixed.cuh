@@ -72,7 +72,9 @@ __device__ __forceinline__ float2 d_boundary(const Consts<float>& c, const HE& u
     if (c.msd_guard && yq.x == 0.f && yq.y == 0.f) {
       A = 0.f;
     } else {
-      A = (dq.x * yq.x + dq.y * yq.y) / (yq.x * yq.x + yq.y * yq.y);
+      // in FP64: |yq|^2 of a small FP32 value would underflow in FP32
+      double qx = yq.x, qy = yq.y;
+      A = (float)(((double)dq.x * qx + (double)dq.y * qy) / (qx * qx + qy * qy));
     }
     float Nb = c.s * (y.x * y.x + y.y * y.y) - vb;
     float Nb1 = c.s * (yq.x * yq.x + yq.y * yq.y) - vq;
@@ -141,7 +143,9 @@ __device__ __forceinline__ float2 f_boundary(const Consts<float>& c, const HE& u
     if (c.msd_guard && yq.x == 0.f && yq.y == 0.f) {
       OM = 0.f;
     } else {
-      OM = (fq.y * yq.x - fq.x * yq.y) / (yq.x * yq.x + yq.y * yq.y);
+      // in FP64, as above (boundary points only)
+      double qx = yq.x, qy = yq.y;
+      OM = (float)(((double)fq.y * qx - (double)fq.x * qy) / (qx * qx + qy * qy));
     }
     return f2(-OM * y.y, OM * y.x);
   } else if (BC == 3) {

@@ -52,10 +52,13 @@ def test_golden_vectors_on_gpu(gpu_lib):
             continue  # reference single-precision fall-through quirk; covered below
         got = gpu(U, V, s, a, h2, BC, chunk, k, method, prec)
         if np.isnan(ref).any():
-            # zero MSD neighbour: the library guards (reference GPU semantics)
+            # NaN in the reference output: either an exactly-zero MSD
+            # neighbour (the library guards it, as the reference GPU code
+            # does) or a genuine blow-up (the library reproduces it).
             want = orc(U, V, s, a, h2, BC, chunk, k, method, prec)
-            assert np.isfinite(got).all()
             assert bits_equal(got, want), "golden case %d" % n
+            if np.count_nonzero(U == 0) == 1:
+                assert np.isfinite(got).all()
         else:
             assert bits_equal(got, ref), "golden case %d differs" % n
         checked += 1

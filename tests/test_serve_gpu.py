@@ -1,0 +1,55 @@
+"""Serving loop: continuous batching of a Poisson request stream.
+
+Every request completes; each result is identical to the same solve run
+alone (the batch never mixes solves), latency statistics are reported, and
+admission honours the pool budget (requests wait, not fail, when it is full).
+"""
+import numpy as np
+import pytest
+
+from nlsemagic_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def bits_equal(a, b):
+    a = np.ascontiguousarray(a, dtype=np.complex128).view(np.float64)
+    b = np.ascontiguousarray(b, dtype=np.complex128).view(np.float64)
+    return np.array_equal(a, b, equal_nan=True)
+
+
+def small_stream(count=30, rate=400.0):
+    return W.serving_requests(count=count, rate=rate, n1=(256, 2048), n2=(32, 96), n3=(12, 24),
+                              steps=(20, 120))
+
+
+def test_serving_results_equal_alone(gpu_lib):
+    import nlsemagic_gb300 as ng
+    from nlsemagic_gb300.serve import Server
+    reqs = small_stream()
+    srv = Server(pool_bytes=1 << 28, chunk_steps=16, keep_snapshots=True)
+    summary, done = srv.serve(reqs)
+    srv.close()
+    assert summary["requests"] == len(reqs)
+    assert summary["p99_latency_s"] >= summary["p50_latency_s"] > 0
+    by_id = {c.rid: c for c in done}
+    for r in reqs[:12]:
+        i = r.inst
+        b = ng.Batch(1 << 26)
+        sl = b.add(i.U, i.V, i.s, i.a, i.h * i.h, i.BC, i.steps, i.k, i.method, i.precision)
+        b.run(i.steps)
+        assert bits_equal(by_id[r.rid].snapshot, b.download(sl))
+        b.close()
+
+
+def test_serving_waits_when_pool_is_full(gpu_lib):
+    import nlsemagic_gb300 as ng
+    from nlsemagic_gb300.serve import Server
+    reqs = small_stream(count=16, rate=1e6)  # all arrive at once
+    biggest = max(ng.Batch.bytes_for(r.inst.U.shape, r.inst.precision) for r in reqs)
+    srv = Server(pool_bytes=2 * biggest, chunk_steps=32)
+    summary, done = srv.serve(reqs)
+    srv.close()
+    assert summary["requests"] == len(reqs)
+    assert summary["rejected"] == 0
+    assert summary["p99_queue_s"] > 0
