@@ -80,7 +80,7 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
         objs = list(ex.map(compile_one, units))
     if force or _stale(LIB, objs):
         tmp = LIB + ".tmp%d" % os.getpid()
-        cmd = [nv] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcuda"]
+        cmd = [nv] + ARCH + ["-shared", "-o", tmp] + objs
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))

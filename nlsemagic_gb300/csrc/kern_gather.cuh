@@ -125,18 +125,11 @@ namespace mixed {
 
 struct YIn {
   const float2* hi;
-  const float2* lo;
-  const float2* d;  // null in stage 1
+  const float2* e;  // E of this stage (lo in stage 1)
   __device__ __forceinline__ HE at(long long q) const {
     HE r;
     r.h = hi[q];
-    float2 l = lo[q];
-    if (d) {
-      float2 dd = d[q];
-      r.e = make_float2(l.x + dd.x, l.y + dd.y);
-    } else {
-      r.e = l;
-    }
+    r.e = e[q];
     return r;
   }
 };
@@ -276,33 +269,22 @@ __device__ float2 f_at(const Geom& g, const Consts<float>& c, const YIn& Y, cons
   return f_boundary<METHOD, BC>(c, ub, V[b], uq, fq, os);
 }
 
-// Mixed RK4 stage update.  With d2 = k/2 K1, d3 = k/2 K2, d4 = k K3 kept as
-// the stage deltas, K1 and K3 are recovered from d2 and d4, so the only
-// accumulator written is K12 = K1 + 2 K2 (stage 2):
-//  1: d' = k/2 T
-//  2: K = d*(2/k) + 2 T;  d' = k/2 T
-//  3: d' = k T
-//  4: psi_out = psi + k/6 (K + 2 d*(1/k) + T)   (compensated)
+// Mixed RK4 stage update at point p (E format, see nlse_mixed.cuh).
 __device__ __forceinline__ void update(const Consts<float>& c, int stage, long long p, float2 T,
-                                       const float2* hi_in, const float2* lo_in, const float2* d_in,
-                                       float2* K, float2* d_out, float2* hi_out, float2* lo_out) {
-  if (stage == 1) {
-    d_out[p] = scl(c.k2, T);
-  } else if (stage == 2) {
-    float2 d = d_in[p];
-    K[p] = make_float2(d.x * c.kinv2 + 2.f * T.x, d.y * c.kinv2 + 2.f * T.y);
-    d_out[p] = scl(c.k2, T);
-  } else if (stage == 3) {
-    d_out[p] = scl(c.k, T);
+                                       const float2* hi_in, const float2* lo_in, const float2* e_in,
+                                       float2* K, float2* e_out, float2* hi_out, float2* lo_out) {
+  float2 lo = lo_in[p];
+  float2 e = stage == 2 || stage == 4 ? e_in[p] : lo;
+  float2 hi = stage == 4 ? hi_in[p] : lo;
+  float2 kv = stage == 4 ? K[p] : lo;
+  float2 eo, ko, ho, lo2;
+  stage_update(c, stage, T, hi, lo, e, kv, eo, ko, ho, lo2);
+  if (stage == 2) K[p] = ko;
+  if (stage < 4) {
+    e_out[p] = eo;
   } else {
-    float2 d = d_in[p];
-    float2 kk = K[p];
-    float2 kt = make_float2(kk.x + 2.f * (d.x * c.kinv) + T.x, kk.y + 2.f * (d.y * c.kinv) + T.y);
-    float2 h = hi_in[p], l = lo_in[p];
-    comp_add(h.x, l.x, c.k6 * kt.x);
-    comp_add(h.y, l.y, c.k6 * kt.y);
-    hi_out[p] = h;
-    lo_out[p] = l;
+    hi_out[p] = ho;
+    lo_out[p] = lo2;
   }
 }
 
@@ -316,7 +298,7 @@ __global__ void __launch_bounds__(256) gather_stage(Geom g, Consts<float> c,
                                                     float2* __restrict__ d_out,
                                                     float2* __restrict__ hi_out,
                                                     float2* __restrict__ lo_out, int stage) {
-  YIn Y{hi_in, lo_in, stage == 1 ? nullptr : d_in};
+  YIn Y{hi_in, stage == 1 ? lo_in : d_in};
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < g.n;
        p += (long long)gridDim.x * blockDim.x) {
     int i, j, k;

@@ -14,7 +14,7 @@ static cudaError_t launch_one(const Geom& g, const Consts<float>& c, const Mixed
   long long blocks = (g.n + 255) / 256;
   if (blocks > 152LL * 32) blocks = 152LL * 32;
   mixed::gather_stage<DIM, METHOD, BC><<<(unsigned)blocks, 256, 0, st>>>(
-      g, c, a.hi_in, a.lo_in, a.d_in, a.V, a.K, a.d_out, a.hi_out, a.lo_out, stage);
+      g, c, a.hi_in, a.lo_in, a.e_in, a.V, a.K, a.e_out, a.hi_out, a.lo_out, stage);
   return cudaGetLastError();
 }
 

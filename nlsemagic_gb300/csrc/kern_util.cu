@@ -205,7 +205,37 @@ cudaError_t mass_hilo(const float2* hi, const float2* lo, long long n, double* o
 
 }  // namespace nlse
 
+#include "../../include/nlse_gb300.h"
+
 namespace nlse {
+namespace tiled {
+// Device error word written by kernels whose bounded waits gave up
+// (NLSE_ERR_TIMEOUT) or whose self-checks failed; allocated on first use,
+// outside any stream capture (solver creation calls it).
+static int* g_err_word = nullptr;
+int* error_word() {
+  if (!g_err_word) {
+    if (cudaMalloc(&g_err_word, sizeof(int)) != cudaSuccess) {
+      cudaGetLastError();
+      g_err_word = nullptr;
+      return nullptr;
+    }
+    cudaMemset(g_err_word, 0, sizeof(int));
+  }
+  return g_err_word;
+}
+}  // namespace tiled
+
+// Reads and clears the device error word (0 when no kernel reported one).
+int take_device_error() {
+  int* w = tiled::error_word();
+  if (!w) return NLSE_ERR_NOMEM;
+  int v = 0;
+  if (cudaMemcpy(&v, w, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return NLSE_ERR_CUDA;
+  if (v) cudaMemset(w, 0, sizeof(int));
+  return v;
+}
+
 // Shapes handled by the tiled kernels (kern_tiled.cuh); others use gather.
 bool tiled_supported(const Geom& g, int dim) {
   return dim == 3 && g.ndim == 3 && g.M >= 3 && g.N >= 3 && g.L >= 3;

@@ -209,6 +209,13 @@ struct nlse_solver {
   size_t bytes;
 };
 
+static int device_error_check() {
+  int v = take_device_error();
+  if (v == NLSE_ERR_TIMEOUT) return fail(v, "a stage kernel gave up waiting for its tile loads");
+  if (v) return fail(v, "a stage kernel reported error %d", v);
+  return NLSE_OK;
+}
+
 static int dalloc(nlse_solver* s, void** p, size_t bytes) {
   cudaError_t e = cudaMalloc(p, bytes);
   if (e != cudaSuccess) {
@@ -261,6 +268,10 @@ extern "C" int nlse_solver_create(const nlse_problem* p, nlse_solver** out) {
   if (e != cudaSuccess) {
     delete s;
     return fail(NLSE_ERR_CUDA, "no CUDA device: %s", cudaGetErrorString(e));
+  }
+  if (!nlse::tiled::error_word()) {
+    delete s;
+    return fail(NLSE_ERR_NOMEM, "device error word allocation failed");
   }
   e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
@@ -384,7 +395,7 @@ extern "C" int nlse_solver_download(nlse_solver* s, double* Ur, double* Ui) {
   CUDA_TRY(cudaMemcpyAsync(Ur, s->stage, sizeof(double) * n, cudaMemcpyDeviceToHost, s->stream));
   CUDA_TRY(cudaMemcpyAsync(Ui, s->stage + n, sizeof(double) * n, cudaMemcpyDeviceToHost, s->stream));
   CUDA_TRY(cudaStreamSynchronize(s->stream));
-  return NLSE_OK;
+  return device_error_check();
 }
 
 // Enqueue one RK4 step (4 stage launches) without graphs.
@@ -488,7 +499,7 @@ extern "C" int nlse_solver_set_graph_steps(nlse_solver* s, int steps) {
 extern "C" int nlse_solver_sync(nlse_solver* s) {
   if (!s) return fail(NLSE_ERR_ARG, "solver is NULL");
   CUDA_TRY(cudaStreamSynchronize(s->stream));
-  return NLSE_OK;
+  return device_error_check();
 }
 
 extern "C" int nlse_solver_stream(nlse_solver* s, void** stream) {

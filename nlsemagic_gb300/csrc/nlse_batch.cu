@@ -85,7 +85,7 @@ __device__ __noinline__ void tile_mixed(const BSolve& s, int stage, int par, lon
   const float* V = (const float*)s.buf[7];
   const float2* d_in = stage == 3 ? db : da;
   float2* d_out = stage == 2 ? db : da;
-  mixed::YIn Y{hi_in, lo_in, stage == 1 ? nullptr : d_in};
+  mixed::YIn Y{hi_in, stage == 1 ? lo_in : d_in};
   for (long long p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
     int i, j, k;
     decompose(s.g, p, i, j, k);

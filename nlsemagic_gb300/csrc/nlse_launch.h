@@ -22,10 +22,10 @@ struct ExactStageArgs {
 struct MixedStageArgs {
   const float2* hi_in;
   const float2* lo_in;
-  const float2* d_in;  // stage delta (unused in stage 1)
+  const float2* e_in;  // stage input E = lo + d (unused in stage 1)
   const float* V;
   float2* K;
-  float2* d_out;
+  float2* e_out;      // next stage input E
   float2* hi_out;      // stage 4 output (a different buffer from hi_in)
   float2* lo_out;
 };
@@ -63,5 +63,12 @@ cudaError_t mass_hilo(const float2* hi, const float2* lo, long long n, double* o
                       cudaStream_t st);
 
 bool tiled_supported(const Geom& g, int dim);
+
+// Device error word of the tiled kernels (bounded-wait timeouts, self-check
+// failures): take_device_error() returns and clears it.
+namespace tiled {
+int* error_word();
+}
+int take_device_error();
 
 }  // namespace nlse

@@ -1,18 +1,25 @@
 // Mixed-precision stencil: FP32 stage evaluation on a compensated state.
 //
 // State: psi = hi + lo, two float2 planes (about 48 significant bits).  The
-// stage input of RK4 stage s is Y_s = psi + d_s, where d_s is the small FP32
-// stage delta (k/2 K1, k/2 K2, k K3).  Each grid point is presented to the
-// stencil as the pair (h, e) = (hi, lo + d_s).
+// stage input of RK4 stage s is Y_s = hi + E_s, with E_1 = lo and
+// E_s = lo + d_s (s > 1) for the stage delta d_s (k/2 K1, k/2 K2, k K3).
+// Each grid point is presented to the stencil as the pair (h, e) = (hi, E).
 //
-// Every Laplacian-type sum is taken in difference form,
-//     sum_n (Y_n - Y_c) = sum_n (h_n - h_c) + sum_n (e_n - e_c),
-// so FP32 rounding is relative to the (small) differences and not to |Y|.
-// Storing Y itself in FP32 would add a representation error of ~6e-8 |Y| per
-// point that the 1/h^2 of the Laplacian amplifies to ~1e-5 in F.
-// Pointwise terms (nonlinearity, potential, boundary formulas) use
-// y = h + e rounded to FP32.  The formulas are those of the exact path
-// (nlse_exact.cuh), algebraically rearranged only as stated above.
+// Laplacian-type sums are split by parts:
+//     sum_n (Y_n - Y_c) = sum_n (h_n - h_c) + (sum_n e_n - N e_c).
+// The hi part is taken in difference form, so its FP32 rounding is relative
+// to the (small) differences of neighbouring values and not to |Y|; storing
+// Y itself in FP32 would add a representation error of ~6e-8 |Y| per point
+// that the 1/h^2 of the Laplacian amplifies to ~1e-5 in F.  The E part is
+// small (|E| <~ |k F|), so it is summed directly.  Pointwise terms
+// (nonlinearity, potential, boundary formulas) use y = h + e in FP32.
+//
+// All arithmetic is written with explicit-rounding intrinsics, most of it on
+// packed complex pairs (__fadd2_rn / __ffma2_rn / __fmul2_rn, sm_100+), so
+// the results do not depend on the compiler's FMA contraction: every kernel
+// that uses these functions (gather, tiled, batched) produces the same bits.
+// The formulas are those of the exact path (nlse_exact.cuh), rearranged only
+// as stated here.
 #pragma once
 
 #include "nlse_common.cuh"
@@ -25,36 +32,62 @@ struct HE {
 };
 
 __device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
-__device__ __forceinline__ float2 add(float2 a, float2 b) { return f2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 sub(float2 a, float2 b) { return f2(a.x - b.x, a.y - b.y); }
-__device__ __forceinline__ float2 scl(float s, float2 a) { return f2(s * a.x, s * a.y); }
-__device__ __forceinline__ float2 val(const HE& p) { return add(p.h, p.e); }
+__device__ __forceinline__ float2 P2(float s) { return make_float2(s, s); }
+__device__ __forceinline__ float2 padd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 psub(float2 a, float2 b) { return __ffma2_rn(b, P2(-1.f), a); }
+__device__ __forceinline__ float2 pmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 pfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 val(const HE& p) { return padd(p.h, p.e); }
 
-// (Y_n - Y_c) in two pieces, accumulated into sh (hi differences) and se.
-__device__ __forceinline__ void acc_diff(float2& sh, float2& se, const HE& n, const HE& c) {
-  sh.x += n.h.x - c.h.x;
-  sh.y += n.h.y - c.h.y;
-  se.x += n.e.x - c.e.x;
-  se.y += n.e.y - c.e.y;
+// sum_n (Y_n - Y_c) over NN neighbours
+template <int NN>
+__device__ __forceinline__ float2 lapsum(const HE& c, const HE* nb) {
+  float2 sh = psub(nb[0].h, c.h);
+  float2 se = nb[0].e;
+#pragma unroll
+  for (int t = 1; t < NN; ++t) {
+    sh = padd(sh, psub(nb[t].h, c.h));
+    se = padd(se, nb[t].e);
+  }
+  se = pfma(c.e, P2(-(float)NN), se);
+  return padd(sh, se);
 }
 
+// s |y|^2 - V
 __device__ __forceinline__ float nl_term(const Consts<float>& c, float2 y, float v) {
-  return c.s * (y.x * y.x + y.y * y.y) - v;
+  float m = __fmaf_rn(y.x, y.x, __fmul_rn(y.y, y.y));
+  return __fmaf_rn(c.s, m, -v);
 }
 
-// i * (a_lap + nl*y) split into components: F = (-a_lap.i - nl*y.i, a_lap.r + nl*y.r)
-__device__ __forceinline__ float2 rhs(float2 alap, float nl, float2 y) {
-  return f2(-alap.y - nl * y.y, alap.x + nl * y.x);
+// F = i (lin + nl y):  (-(lin.i + nl y.i), lin.r + nl y.r)
+__device__ __forceinline__ float2 rhs(float2 lin, float nl, float2 y) {
+  float2 t = pfma(P2(nl), f2(y.y, y.x), f2(lin.y, lin.x));
+  return f2(-t.x, t.y);
 }
 
 // ---- 2SHOC D at an interior point ------------------------------------------
-// nb[]: face neighbours (2*DIM of them)
+// nb[]: the 2*DIM face neighbours
 template <int DIM>
 __device__ __forceinline__ float2 d_interior(const Consts<float>& c, const HE& u0, const HE* nb) {
-  float2 sh = f2(0.f, 0.f), se = f2(0.f, 0.f);
-#pragma unroll
-  for (int t = 0; t < 2 * DIM; ++t) acc_diff(sh, se, nb[t], u0);
-  return scl(c.lh2, add(sh, se));
+  return pmul(P2(c.lh2), lapsum<2 * DIM>(u0, nb));
+}
+
+// -(y3-y0) + 4(y2-y0) - 5(y1-y0) = -y3 + 4 y2 - 5 y1 + 2 y0  (1D one-sided)
+__device__ __forceinline__ float2 onesided_sum(const HE* os) {
+  float2 d3 = padd(psub(os[3].h, os[0].h), psub(os[3].e, os[0].e));
+  float2 d2 = padd(psub(os[2].h, os[0].h), psub(os[2].e, os[0].e));
+  float2 d1 = padd(psub(os[1].h, os[0].h), psub(os[1].e, os[0].e));
+  return pfma(P2(-5.f), d1, pfma(P2(4.f), d2, pmul(P2(-1.f), d3)));
+}
+
+// MSD ratio in FP64 (boundary points only; |w|^2 of a small FP32 value would
+// underflow in FP32): cross = 0 -> (u.w)/|w|^2, cross = 1 -> (u_i w_r - u_r w_i)/|w|^2.
+__device__ __forceinline__ float msd_ratio(float2 u, float2 w, int cross) {
+  double wx = w.x, wy = w.y, ux = u.x, uy = u.y;
+  double num = cross ? __dsub_rn(__dmul_rn(uy, wx), __dmul_rn(ux, wy))
+                     : __dadd_rn(__dmul_rn(ux, wx), __dmul_rn(uy, wy));
+  double den = __dadd_rn(__dmul_rn(wx, wx), __dmul_rn(wy, wy));
+  return (float)__ddiv_rn(num, den);
 }
 
 // ---- D at a boundary point -------------------------------------------------
@@ -64,28 +97,18 @@ __device__ __forceinline__ float2 d_boundary(const Consts<float>& c, const HE& u
                                              const HE* os /* 1D BC4: points 0..3 inward */) {
   float2 y = val(ub);
   if (BC == 1) {
-    float t = c.l_a * (vb - c.s * (y.x * y.x + y.y * y.y));
-    return scl(t, y);
+    // (1/a)(V - s|y|^2) y
+    float t = __fmul_rn(c.l_a, -nl_term(c, y, vb));
+    return pmul(P2(t), y);
   } else if (BC == 2) {
     float2 yq = val(uq);
-    float A;
-    if (c.msd_guard && yq.x == 0.f && yq.y == 0.f) {
-      A = 0.f;
-    } else {
-      // in FP64: |yq|^2 of a small FP32 value would underflow in FP32
-      double qx = yq.x, qy = yq.y;
-      A = (float)(((double)dq.x * qx + (double)dq.y * qy) / (qx * qx + qy * qy));
-    }
-    float Nb = c.s * (y.x * y.x + y.y * y.y) - vb;
-    float Nb1 = c.s * (yq.x * yq.x + yq.y * yq.y) - vq;
-    return scl(A + c.l_a * (Nb1 - Nb), y);
+    float A = (c.msd_guard && yq.x == 0.f && yq.y == 0.f) ? 0.f : msd_ratio(dq, yq, 0);
+    float Nb = nl_term(c, y, vb);
+    float Nb1 = nl_term(c, yq, vq);
+    float t = __fmaf_rn(c.l_a, __fsub_rn(Nb1, Nb), A);
+    return pmul(P2(t), y);
   } else if (BC == 4) {
-    // -y3 + 4 y2 - 5 y1 + 2 y0 = -(y3-y0) + 4(y2-y0) - 5(y1-y0)
-    float2 d3 = add(sub(os[3].h, os[0].h), sub(os[3].e, os[0].e));
-    float2 d2 = add(sub(os[2].h, os[0].h), sub(os[2].e, os[0].e));
-    float2 d1 = add(sub(os[1].h, os[0].h), sub(os[1].e, os[0].e));
-    float2 s = f2(-d3.x + 4.f * d2.x - 5.f * d1.x, -d3.y + 4.f * d2.y - 5.f * d1.y);
-    return scl(c.lh2, s);
+    return pmul(P2(c.lh2), onesided_sum(os));
   }
   return f2(0.f, 0.f);
 }
@@ -94,11 +117,8 @@ __device__ __forceinline__ float2 d_boundary(const Consts<float>& c, const HE& u
 template <int DIM>
 __device__ __forceinline__ float2 f_interior_cd(const Consts<float>& c, const HE& u0, float v,
                                                 const HE* nb) {
-  float2 sh = f2(0.f, 0.f), se = f2(0.f, 0.f);
-#pragma unroll
-  for (int t = 0; t < 2 * DIM; ++t) acc_diff(sh, se, nb[t], u0);
   float2 y = val(u0);
-  return rhs(scl(c.ah2, add(sh, se)), nl_term(c, y, v), y);
+  return rhs(pmul(P2(c.ah2), lapsum<2 * DIM>(u0, nb)), nl_term(c, y, v), y);
 }
 
 // ---- interior F, 2SHOC -----------------------------------------------------
@@ -111,23 +131,19 @@ __device__ __forceinline__ float2 f_interior_2shoc(const Consts<float>& c, const
   float nl = nl_term(c, y, v);
   float2 lin;  // a * (compact fourth-order Laplacian)
   if (DIM == 1) {
-    // a/12 (D+ + D-) ... written as a76*D0 - a112*(D+ + D-) for the real part of i*(...)
-    lin = f2(c.a76 * d0.x - c.a112 * (dn[0].x + dn[1].x), c.a76 * d0.y - c.a112 * (dn[0].y + dn[1].y));
+    // a76 D0 - a112 (D+ + D-)
+    lin = pfma(P2(c.a76), d0, pmul(P2(-c.a112), padd(dn[0], dn[1])));
   } else if (DIM == 2) {
-    float2 sh = f2(0.f, 0.f), se = f2(0.f, 0.f);
-#pragma unroll
-    for (int t = 0; t < 4; ++t) acc_diff(sh, se, ed[t], u0);
-    float2 sdg = add(sh, se);
-    float2 sd = add(add(dn[0], dn[1]), add(dn[2], dn[3]));
-    lin = f2(c.a * d0.x - c.a_12 * sd.x + c.a_6h2 * sdg.x, c.a * d0.y - c.a_12 * sd.y + c.a_6h2 * sdg.y);
+    // a D0 - a/12 sum D(4) + a/(6h^2) sum_diag (Y_d - Y_0)
+    float2 sdg = lapsum<4>(u0, ed);
+    float2 sd = padd(padd(dn[0], dn[1]), padd(dn[2], dn[3]));
+    lin = pfma(P2(c.a), d0, pfma(P2(-c.a_12), sd, pmul(P2(c.a_6h2), sdg)));
   } else {
-    float2 sh = f2(0.f, 0.f), se = f2(0.f, 0.f);
-#pragma unroll
-    for (int t = 0; t < 12; ++t) acc_diff(sh, se, ed[t], u0);
-    float2 sdg = add(sh, se);
-    float2 sd = add(add(add(dn[0], dn[1]), add(dn[2], dn[3])), add(dn[4], dn[5]));
-    lin = f2(-c.a_12 * (sd.x - 10.f * d0.x) + c.a_6h2 * sdg.x,
-             -c.a_12 * (sd.y - 10.f * d0.y) + c.a_6h2 * sdg.y);
+    // -a/12 (sum D(6) - 10 D0) + a/(6h^2) sum_edge (Y_e - Y_0)
+    float2 sdg = lapsum<12>(u0, ed);
+    float2 sd = padd(padd(padd(dn[0], dn[1]), padd(dn[2], dn[3])), padd(dn[4], dn[5]));
+    float2 t = pfma(d0, P2(-10.f), sd);
+    lin = pfma(P2(c.a_6h2), sdg, pmul(P2(-c.a_12), t));
   }
   return rhs(lin, nl, y);
 }
@@ -139,25 +155,14 @@ __device__ __forceinline__ float2 f_boundary(const Consts<float>& c, const HE& u
   float2 y = val(ub);
   if (BC == 2) {
     float2 yq = val(uq);
-    float OM;
-    if (c.msd_guard && yq.x == 0.f && yq.y == 0.f) {
-      OM = 0.f;
-    } else {
-      // in FP64, as above (boundary points only)
-      double qx = yq.x, qy = yq.y;
-      OM = (float)(((double)fq.y * qx - (double)fq.x * qy) / (qx * qx + qy * qy));
-    }
-    return f2(-OM * y.y, OM * y.x);
+    float OM = (c.msd_guard && yq.x == 0.f && yq.y == 0.f) ? 0.f : msd_ratio(fq, yq, 1);
+    return pmul(P2(OM), f2(-y.y, y.x));
   } else if (BC == 3) {
     float nl = nl_term(c, y, vb);
-    return f2(-nl * y.y, nl * y.x);
+    return pmul(P2(nl), f2(-y.y, y.x));
   } else if (BC == 4) {
-    float2 d3 = add(sub(os[3].h, os[0].h), sub(os[3].e, os[0].e));
-    float2 d2 = add(sub(os[2].h, os[0].h), sub(os[2].e, os[0].e));
-    float2 d1 = add(sub(os[1].h, os[0].h), sub(os[1].e, os[0].e));
-    float2 s = f2(-d3.x + 4.f * d2.x - 5.f * d1.x, -d3.y + 4.f * d2.y - 5.f * d1.y);
-    float coef = METHOD == 1 ? c.ah2 : c.a * c.lh2;
-    return rhs(scl(coef, s), nl_term(c, y, vb), y);
+    float coef = METHOD == 1 ? c.ah2 : __fmul_rn(c.a, c.lh2);
+    return rhs(pmul(P2(coef), onesided_sum(os)), nl_term(c, y, vb), y);
   }
   return f2(0.f, 0.f);
 }
@@ -175,6 +180,38 @@ __device__ __forceinline__ void comp_add(float& hi, float& lo, float inc) {
   t = __fadd_rn(t, lo);
   hi = __fadd_rn(s, t);
   lo = __fsub_rn(t, __fsub_rn(hi, s));
+}
+
+// ---- RK4 stage update of the mixed path -------------------------------------
+// Each stage stores the next E (= lo + d) rather than d itself, so the stencil
+// of every stage reads two planes (hi, E); d is recovered as E - lo.  K1 and
+// K3 are recovered from d_2 and d_4, so the only accumulator written is
+// K12 = K1 + 2 K2 (stage 2):
+//   1: E' = lo + k/2 T
+//   2: K = (E - lo)(2/k) + 2 T;   E' = lo + k/2 T
+//   3: E' = lo + k T
+//   4: psi_out = psi + k/6 (K + 2 (E - lo)(1/k) + T)   (compensated)
+// e is E of this stage at the point (unused in stage 1), Kv the accumulator
+// (stage 4).  Writes eo (stages 1-3), Ko (stage 2) or (hio, loo) (stage 4).
+__device__ __forceinline__ void stage_update(const Consts<float>& c, int stage, float2 T,
+                                             float2 hi, float2 lo, float2 e, float2 Kv,
+                                             float2& eo, float2& Ko, float2& hio, float2& loo) {
+  if (stage == 1) {
+    eo = pfma(P2(c.k2), T, lo);
+  } else if (stage == 2) {
+    Ko = pfma(psub(e, lo), P2(c.kinv2), pmul(P2(2.f), T));
+    eo = pfma(P2(c.k2), T, lo);
+  } else if (stage == 3) {
+    eo = pfma(P2(c.k), T, lo);
+  } else {
+    float2 d = psub(e, lo);
+    float2 kt = pfma(P2(2.f), pmul(d, P2(c.kinv)), padd(Kv, T));
+    float2 inc = pmul(P2(c.k6), kt);
+    hio = hi;
+    loo = lo;
+    comp_add(hio.x, loo.x, inc.x);
+    comp_add(hio.y, loo.y, inc.y);
+  }
 }
 
 }  // namespace mixed

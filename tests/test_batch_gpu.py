@@ -33,7 +33,7 @@ def smooth_case(ndim, n, method, BC, seed):
     c = rng.uniform(-1, 1, size=ndim)
     U = (np.exp(-r2 / (2 + 10 * rng.random())) * np.exp(1j * sum(ci * g for ci, g in zip(c, grids)))
          + 0.3).astype(complex)
-    V = 0.005 * r2
+    V = 0.5 * r2 / r2.max()
     s = float(rng.choice([-1.0, 1.0]))
     a = float(rng.uniform(0.5, 2.0))
     k = 0.6 * W.linear_stability_k(ndim, method, h, a)
