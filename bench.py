@@ -399,6 +399,10 @@ def run_gpu(args, w):
     if fp64:
         result["fp64_path"] = fp64
         result["mixed_over_fp64"] = value / world / fp64["value"]
+    if rank == 0 and args.batch_solves > 0:
+        result["batched"] = run_batched(args)
+    if rank == 0 and args.serve_requests > 0:
+        result["serving"] = run_serving(args)
     if rank == 0 and world == 1 and args.cpu_sample_steps > 0:
         threads = cpu_threads_for(w)
         v, wall = cpu_sample(w, args.cpu_sample_steps, threads)
@@ -415,6 +419,90 @@ def run_gpu(args, w):
         dist.destroy_process_group()
 
 
+def run_batched(args):
+    """Uneven batch (512 solves: 60% 1D N in [256, 16384], 40% 2D side in
+    [64, 512], CD/2SHOC, mixed precision, 1000 steps): one persistent launch
+    for all solves vs one solve at a time through resident solvers with
+    graph-captured chunks."""
+    import nlsemagic_gb300 as ng
+    from nlsemagic_gb300 import workloads as W
+    insts = W.batch_instances(count=args.batch_solves, steps=args.batch_steps)
+    pts = float(sum(i.U.size for i in insts)) * args.batch_steps
+    w0 = insts[0]  # warm the persistent kernel on a tiny batch
+    b = ng.Batch(1 << 26)
+    b.add(w0.U, w0.V, w0.s, w0.a, w0.h * w0.h, w0.BC, 2, w0.k, w0.method, ng.PREC_MIXED)
+    b.run(2)
+    b.sync()
+    b.close()
+    b = ng.Batch(sum(ng.Batch.bytes_for(i.U.shape, ng.PREC_MIXED) for i in insts) + (1 << 20),
+                 max_solves=len(insts) + 1)
+    for i in insts:
+        b.add(i.U, i.V, i.s, i.a, i.h * i.h, i.BC, args.batch_steps, i.k, i.method, ng.PREC_MIXED)
+    t0 = time.perf_counter()
+    b.run(args.batch_steps)
+    b.sync()
+    t_batch = time.perf_counter() - t0
+    launches = b.last_launches
+    b.close()
+    log("batched: %d solves x %d steps in %.3f s" % (len(insts), args.batch_steps, t_batch))
+    # one solve at a time (a subset when large, scaled by its share of work)
+    # (solvers created and uploaded beforehand: only their launches are timed)
+    sub = insts[:args.batch_seq_sample] if args.batch_seq_sample else insts
+    solvers = []
+    for i in sub:
+        sv = ng.Solver(i.U.shape, method=i.method, precision=ng.PREC_MIXED, BC=i.BC, s=i.s, a=i.a,
+                       h2=i.h * i.h, k=i.k)
+        sv.upload(i.U, i.V)
+        sv.run(sv_warm := 8)  # captures the chunk graph outside the timed loop
+        sv.sync()
+        solvers.append(sv)
+    t0 = time.perf_counter()
+    for sv in solvers:
+        sv.run(args.batch_steps)
+        sv.sync()
+    t_seq = time.perf_counter() - t0
+    for sv in solvers:
+        sv.close()
+    del sv_warm
+    pts_sub = float(sum(i.U.size for i in sub)) * args.batch_steps
+    log("one-at-a-time: %d solves in %.3f s" % (len(sub), t_seq))
+    v_batch = pts / t_batch / 1e9
+    v_seq = pts_sub / t_seq / 1e9
+    return {"workload": "%d uneven 1D/2D solves, %d RK4 steps, mixed precision" % (
+                len(insts), args.batch_steps),
+            "value": v_batch, "unit": UNIT, "seconds": t_batch, "launches": launches,
+            "one_at_a_time": {"value": v_seq, "unit": UNIT, "solves_timed": len(sub),
+                              "seconds": t_seq},
+            "speedup": v_batch / v_seq}
+
+
+def run_serving(args):
+    """Continuous-batching request loop on a seeded Poisson stream (dims
+    1D:2D:3D = 5:4:1, sizes and step counts log-uniform, FP64 or mixed per
+    request), against serving the same stream one solve at a time."""
+    from nlsemagic_gb300 import workloads as W
+    from nlsemagic_gb300.serve import Server, serve_sequential
+    reqs = W.serving_requests(count=args.serve_requests, rate=args.serve_rate,
+                              n1=(512, 65536), n2=(64, 1024), n3=(32, args.serve_max3d),
+                              steps=(100, args.serve_max_steps))
+    srv = Server(pool_bytes=args.serve_pool_gb << 30, chunk_steps=args.serve_chunk)
+    summary, _ = srv.serve(reqs)
+    srv.close()
+    log("served: %s" % json.dumps(summary))
+    seq = serve_sequential(reqs)
+    log("sequential: %s" % json.dumps(seq))
+    return {"requests": len(reqs), "rate_per_s": args.serve_rate,
+            "dims_ratio": "5:4:1", "sizes": {"1d": [512, 65536], "2d": [64, 1024],
+                                             "3d": [32, args.serve_max3d]},
+            "steps": [100, args.serve_max_steps], "chunk_steps": args.serve_chunk,
+            "value": summary["gpt_steps_per_s"], "unit": UNIT,
+            "p50_latency_s": summary["p50_latency_s"], "p99_latency_s": summary["p99_latency_s"],
+            "p99_queue_s": summary["p99_queue_s"], "wall_s": summary["wall_s"],
+            "sequential": seq,
+            "throughput_over_sequential": summary["gpt_steps_per_busy_s"] /
+            seq["gpt_steps_per_busy_s"] if seq["gpt_steps_per_busy_s"] else None}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -426,6 +514,16 @@ def main():
     ap.add_argument("--graph-steps", type=int, default=10)
     ap.add_argument("--fp64-steps", type=int, default=20)
     ap.add_argument("--cpu-sample-steps", type=int, default=1)
+    ap.add_argument("--batch-solves", type=int, default=512)
+    ap.add_argument("--batch-steps", type=int, default=1000)
+    ap.add_argument("--batch-seq-sample", type=int, default=0,
+                    help="time only the first N solves one at a time (0: all)")
+    ap.add_argument("--serve-requests", type=int, default=200)
+    ap.add_argument("--serve-rate", type=float, default=20.0)
+    ap.add_argument("--serve-chunk", type=int, default=100)
+    ap.add_argument("--serve-max3d", type=int, default=128)
+    ap.add_argument("--serve-max-steps", type=int, default=2000)
+    ap.add_argument("--serve-pool-gb", type=int, default=64)
     args = ap.parse_args()
     from nlsemagic_gb300 import workloads as W
     rank, world, _ = dist_env()

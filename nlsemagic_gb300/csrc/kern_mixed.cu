@@ -1,15 +1,20 @@
 // Mixed-precision (FP32 stages, compensated state) stage launchers.
 #include "kern_gather.cuh"
 #include "kern_tiled.cuh"
+#include "kern_wide.cuh"
 #include "nlse_launch.h"
 
 namespace nlse {
+namespace wide {
+int g_zc_override = 0;
+}
 
 template <int DIM, int METHOD, int BC>
 static cudaError_t launch_one(const Geom& g, const Consts<float>& c, const MixedStageArgs& a,
                               int stage, cudaStream_t st, int kernel_kind) {
-  if (kernel_kind == KERNEL_TILED && tiled_supported(g, DIM)) {
-    return tiled::launch_mixed<DIM, METHOD, BC>(g, c, a, stage, st);
+  if (kernel_kind == KERNEL_TILED && tiled_supported(g, DIM) && DIM == 3 && BC != 4) {
+    tiled::MixedPol::Args A{a, c, stage, tiled::error_word()};
+    return wide::launch<METHOD, BC == 4 ? 1 : BC>(g, A, st);
   }
   long long blocks = (g.n + 255) / 256;
   if (blocks > 152LL * 32) blocks = 152LL * 32;

@@ -121,6 +121,7 @@ static Consts<double> consts_double(const nlse_problem* p) {
   c.k6 = k / 6.0;
   c.kinv = 1.0 / k;
   c.kinv2 = 2.0 / k;
+  c.a12lh2 = a / (12.0 * h2);
   c.msd_guard = (p->flags & NLSE_FLAG_MSD_GUARD) ? 1 : 0;
   return c;
 }
@@ -173,6 +174,7 @@ static Consts<float> consts_mixed(const nlse_problem* p) {
   c.k6 = (float)d.k6;
   c.kinv = (float)d.kinv;
   c.kinv2 = (float)d.kinv2;
+  c.a12lh2 = (float)d.a12lh2;
   c.msd_guard = d.msd_guard;
   return c;
 }

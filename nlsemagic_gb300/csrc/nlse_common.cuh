@@ -34,6 +34,7 @@ struct Consts {
   R a_6h2, a_12;       // 2D: a*(1/(6 h2)), a*(1/12); 3D: a/(6 h2), a/12
   R k, k2, k6;         // k, k/2, k/6
   R kinv, kinv2;       // 1/k, 2/k (mixed path only)
+  R a12lh2;            // a/(12 h2) (mixed path, wide fourth-order form)
   int msd_guard;       // MSD zero-neighbour guard
 };
 

@@ -14,10 +14,10 @@
 // small (|E| <~ |k F|), so it is summed directly.  Pointwise terms
 // (nonlinearity, potential, boundary formulas) use y = h + e in FP32.
 //
-// All arithmetic is written with explicit-rounding intrinsics, most of it on
-// packed complex pairs (__fadd2_rn / __ffma2_rn / __fmul2_rn, sm_100+), so
-// the results do not depend on the compiler's FMA contraction: every kernel
-// that uses these functions (gather, tiled, batched) produces the same bits.
+// All arithmetic is written with explicit-rounding intrinsics on complex
+// pairs, so the results do not depend on the compiler's FMA contraction:
+// every kernel that uses these functions (gather, tiled, batched) produces
+// the same bits for the same formula.
 // The formulas are those of the exact path (nlse_exact.cuh), rearranged only
 // as stated here.
 #pragma once
@@ -33,10 +33,27 @@ struct HE {
 
 __device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
 __device__ __forceinline__ float2 P2(float s) { return make_float2(s, s); }
+#ifdef NLSE_PACKED_F32X2
+// Packed pair instructions (sm_100+).  Same rounding as the scalar forms; on
+// GB300 they were measured to occupy the FP64 pipe, so they are off by default.
 __device__ __forceinline__ float2 padd(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 psub(float2 a, float2 b) { return __ffma2_rn(b, P2(-1.f), a); }
 __device__ __forceinline__ float2 pmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 pfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+#else
+__device__ __forceinline__ float2 padd(float2 a, float2 b) {
+  return f2(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y));
+}
+__device__ __forceinline__ float2 psub(float2 a, float2 b) {
+  return f2(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y));
+}
+__device__ __forceinline__ float2 pmul(float2 a, float2 b) {
+  return f2(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y));
+}
+__device__ __forceinline__ float2 pfma(float2 a, float2 b, float2 c) {
+  return f2(__fmaf_rn(a.x, b.x, c.x), __fmaf_rn(a.y, b.y, c.y));
+}
+#endif
 __device__ __forceinline__ float2 val(const HE& p) { return padd(p.h, p.e); }
 
 // sum_n (Y_n - Y_c) over NN neighbours
@@ -146,6 +163,22 @@ __device__ __forceinline__ float2 f_interior_2shoc(const Consts<float>& c, const
     lin = pfma(P2(c.a_6h2), sdg, pmul(P2(-c.a_12), t));
   }
   return rhs(lin, nl, y);
+}
+
+// ---- interior F, 2SHOC, wide form -----------------------------------------
+// Away from the boundary (every face neighbour interior) the compact scheme's
+// edge-neighbour terms cancel and it equals the standard wide fourth-order
+// Laplacian: per axis (-Y-2 + 16 Y-1 - 30 Y0 + 16 Y+1 - Y+2) / (12 h^2), i.e.
+//   a lap4 Y = a/(12 h^2) (16 sum_f (Y_f - Y_0) - sum_2 (Y_2 - Y_0))
+// over the 2*DIM face neighbours f and the 2*DIM points 2 cells away.
+template <int DIM>
+__device__ __forceinline__ float2 f_wide_2shoc(const Consts<float>& c, const HE& u0, float v,
+                                               const HE* fn, const HE* f2n) {
+  float2 y = val(u0);
+  float2 sf = lapsum<2 * DIM>(u0, fn);
+  float2 sd = lapsum<2 * DIM>(u0, f2n);
+  float2 lin = pmul(P2(c.a12lh2), pfma(P2(16.f), sf, pmul(P2(-1.f), sd)));
+  return rhs(lin, nl_term(c, y, v), y);
 }
 
 // ---- F at a boundary point -------------------------------------------------
