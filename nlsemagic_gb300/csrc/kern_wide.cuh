@@ -43,7 +43,11 @@ struct WShape {
   static constexpr int PX = TX + 4;               // [x0-2, x0+TX+2)
   static constexpr int PY = TY + 2 * H;           // [y0-H, y0+TY+H)
   static constexpr int P = 2;                     // planes in flight beyond the queue head
-  static constexpr int NU = H + P + 1;            // ring slots
+  // Ring slots.  The prologue stages planes zs-H .. zs+H+P-1 (2H+P planes)
+  // before any is released; in the loop the live planes are z .. z+H+P
+  // (H+P+1 <= 2H+P).  Refilling slot (z+H+P) % NU at iteration z reuses the
+  // slot of plane z-H, whose last read was at iteration z-H.
+  static constexpr int NU = 2 * H + P;
   static constexpr int PLANE = round_up(PX * PY * 8, 128);
   static constexpr int SLOT = 2 * PLANE;          // hi plane + E plane
   static constexpr int B_OFF = NU * SLOT;

@@ -1,0 +1,6 @@
+/* MEX gateway NLSE3D_TAKE_STEPS_2SHOC_CUDA_M: 3D, 2SHOC, mixed precision (nlse_mex_gateway.h). */
+#include <string.h>
+#define NLSE_MEX_NDIM 3
+#define NLSE_MEX_METHOD 2
+#define NLSE_MEX_PRECISION 3
+#include "nlse_mex_gateway.h"

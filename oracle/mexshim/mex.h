@@ -34,6 +34,8 @@ mxArray *mxCreateDoubleMatrix(mwSize m, mwSize n, mxComplexity c);
 mxArray *mxCreateNumericArray(mwSize ndim, const mwSize *dims, mxClassID cls,
                               mxComplexity c);
 int mexPrintf(const char *fmt, ...);
+/* Records the error (the driver below returns -3) instead of unwinding. */
+void mexErrMsgIdAndTxt(const char *id, const char *fmt, ...);
 
 /* Every reference file defines this entry point. */
 void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]);

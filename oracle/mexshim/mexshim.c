@@ -78,6 +78,18 @@ int mexPrintf(const char *fmt, ...) {
     return r;
 }
 
+static int g_mex_error = 0;
+
+void mexErrMsgIdAndTxt(const char *id, const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    fprintf(stderr, "%s: ", id);
+    vfprintf(stderr, fmt, ap);
+    fprintf(stderr, "\n");
+    va_end(ap);
+    g_mex_error = 1;
+}
+
 static void free_array(mxArray *a) {
     if (!a) return;
     free(a->pr);
@@ -92,18 +104,21 @@ static mxArray *make_scalar(double v) {
 }
 
 /*
- * ndims: 1, 2 or 3.  dims: {M} / {M, N} / {M, N, L} in MATLAB order
- * (first index fastest).  Ui may be NULL (real input).  Returns 0 on success.
+ * Calls the mexFunction linked into this shared object with nrhs arguments:
+ * (U, V, s, a, h2, BC, chunk_size, k) for nrhs = 8, plus (precision, method)
+ * for nrhs = 10 (the v2 gateways).  ndims: 1, 2 or 3.  dims: {M} / {M, N} /
+ * {M, N, L} in MATLAB order (first index fastest).  Ui may be NULL (real
+ * input).  Returns 0 on success, -3 if the gateway raised a MATLAB error.
  */
-int ref_take_steps(int ndims, const long long *dims, const double *Ur,
-                   const double *Ui, const double *V, double s, double a,
-                   double h2, int BC, int chunk, double k, double *out_r,
-                   double *out_i) {
+int mex_call_take_steps(int ndims, const long long *dims, const double *Ur, const double *Ui,
+                        const double *V, double s, double a, double h2, int BC, int chunk,
+                        double k, int precision, int method, int nrhs, double *out_r,
+                        double *out_i) {
     mwSize d[3];
     mwSize nd, n, i;
-    mxArray *prhs[8];
+    mxArray *prhs[10];
     mxArray *plhs[1];
-    if (ndims < 1 || ndims > 3) return -1;
+    if (ndims < 1 || ndims > 3 || (nrhs != 8 && nrhs != 10)) return -1;
     if (ndims == 1) {
         d[0] = (mwSize)dims[0];
         d[1] = 1;
@@ -124,10 +139,13 @@ int ref_take_steps(int ndims, const long long *dims, const double *Ur,
     prhs[5] = make_scalar((double)BC);
     prhs[6] = make_scalar((double)chunk);
     prhs[7] = make_scalar(k);
+    prhs[8] = make_scalar((double)precision);
+    prhs[9] = make_scalar((double)method);
     plhs[0] = NULL;
-    mexFunction(1, plhs, 8, (const mxArray **)prhs);
+    g_mex_error = 0;
+    mexFunction(1, plhs, nrhs, (const mxArray **)prhs);
     if (!plhs[0]) {
-        for (i = 0; i < 8; ++i) free_array(prhs[i]);
+        for (i = 0; i < 10; ++i) free_array(prhs[i]);
         return -2;
     }
     memcpy(out_r, plhs[0]->pr, n * sizeof(double));
@@ -136,6 +154,14 @@ int ref_take_steps(int ndims, const long long *dims, const double *Ur,
     else
         memset(out_i, 0, n * sizeof(double));
     free_array(plhs[0]);
-    for (i = 0; i < 8; ++i) free_array(prhs[i]);
-    return 0;
+    for (i = 0; i < 10; ++i) free_array(prhs[i]);
+    return g_mex_error ? -3 : 0;
+}
+
+/* The reference MEX signature U = NAME(U, V, s, a, h2, BC, chunk_size, k). */
+int ref_take_steps(int ndims, const long long *dims, const double *Ur, const double *Ui,
+                   const double *V, double s, double a, double h2, int BC, int chunk, double k,
+                   double *out_r, double *out_i) {
+    return mex_call_take_steps(ndims, dims, Ur, Ui, V, s, a, h2, BC, chunk, k, 0, 0, 8, out_r,
+                               out_i);
 }
