@@ -1,0 +1,167 @@
+"""Autotuner for the stage-kernel launch configuration.
+
+For one problem class (dimension, grid, method, precision, boundary code) it
+times RK4 steps of a resident :class:`~nlsemagic_gb300.api.Solver` on a
+smooth synthetic state for each candidate setting of the library's tuning
+knobs and keeps the fastest:
+
+* ``wide.zc``      z-chunk length of the mixed-precision 3D kernel (planes a
+                   CTA streams through; trades queue-fill overhead against the
+                   number of CTAs in flight),
+* ``graph.steps``  RK4 steps captured per CUDA graph (launch overhead against
+                   graph size; matters for small grids).
+
+Results are cached in a JSON file (``$NLSE_TUNE_CACHE`` or
+``~/.cache/nlse_gb300/tune.json``) keyed by device name and problem class;
+:func:`apply` sets the knobs from the cache before a workload runs.  The
+knobs are process-wide and are read when a stage launch is issued or a graph
+captured, so they apply to solvers created afterwards.
+"""
+from __future__ import annotations
+
+import ctypes
+import json
+import os
+import time
+
+import numpy as np
+
+from . import _lib
+from .api import Solver, grid_dims
+
+KNOBS = ("wide.zc", "graph.steps")
+
+
+def _lib_sig():
+    lib = _lib.load()
+    lib.nlse_tune_set.restype = ctypes.c_int
+    lib.nlse_tune_set.argtypes = [ctypes.c_char_p, ctypes.c_longlong]
+    lib.nlse_tune_get.restype = ctypes.c_int
+    lib.nlse_tune_get.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_longlong)]
+    return lib
+
+
+def set_knob(key, value):
+    _lib.check(_lib_sig().nlse_tune_set(key.encode(), int(value)))
+
+
+def get_knob(key):
+    v = ctypes.c_longlong()
+    _lib.check(_lib_sig().nlse_tune_get(key.encode(), ctypes.byref(v)))
+    return v.value
+
+
+def cache_path():
+    return os.environ.get("NLSE_TUNE_CACHE",
+                          os.path.join(os.path.expanduser("~"), ".cache", "nlse_gb300",
+                                       "tune.json"))
+
+
+def _device_name():
+    try:
+        import torch
+        return torch.cuda.get_device_name()
+    except Exception:
+        return "cuda"
+
+
+def problem_key(shape, method, precision, BC):
+    ndim, dims = grid_dims(shape)
+    return "%s|%dd|%s|m%d|p%d|bc%d" % (_device_name(), ndim, "x".join(str(d) for d in shape),
+                                       method, precision, BC)
+
+
+def _load_cache():
+    try:
+        with open(cache_path()) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _save_cache(c):
+    p = cache_path()
+    os.makedirs(os.path.dirname(p), exist_ok=True)
+    tmp = p + ".tmp%d" % os.getpid()
+    with open(tmp, "w") as f:
+        json.dump(c, f, indent=1, sort_keys=True)
+    os.replace(tmp, p)
+
+
+def _smooth_state(shape, h):
+    axes = [np.arange(n) * h - n * h / 2 for n in shape]
+    grids = np.meshgrid(*axes, indexing="ij")
+    r2 = sum(g * g for g in grids)
+    U = (np.tanh(np.sqrt(r2) + 0.5) * np.exp(1j * 0.1 * grids[0])).astype(np.complex128)
+    return U, 0.5 * r2 / max(r2.max(), 1e-30)
+
+
+def candidates(shape, precision):
+    ndim, dims = grid_dims(shape)
+    cands = []
+    zcs = [0]
+    if ndim == 3 and precision == 3:
+        L = dims[2]
+        zcs = sorted({z for z in (16, 32, 48, 64, 96, 128, 192, L) if 4 <= z <= L})
+    for zc in zcs:
+        for gs in (4, 10, 25):
+            cands.append({"wide.zc": zc, "graph.steps": gs})
+    return cands
+
+
+def time_config(shape, method, precision, BC, cfg, steps, h=0.3, reps=2):
+    for k, v in cfg.items():
+        set_knob(k, v)
+    U, V = _smooth_state(shape, h)
+    ndim, _ = grid_dims(shape)
+    from .workloads import linear_stability_k
+    k = 0.5 * linear_stability_k(ndim, method, h, 1.0)
+    with Solver(shape, method=method, precision=precision, BC=BC, s=-1.0, a=1.0, h2=h * h,
+                k=k) as s:
+        s.upload(U, V)
+        s.run(max(1, cfg.get("graph.steps", 8)))  # capture outside the timing
+        s.sync()
+        best = float("inf")
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            s.run(steps)
+            s.sync()
+            best = min(best, time.perf_counter() - t0)
+    return best
+
+
+def tune(shape, method=2, precision=3, BC=2, steps=20, force=False, verbose=False):
+    """Time every candidate, cache and return the best configuration."""
+    key = problem_key(shape, method, precision, BC)
+    cache = _load_cache()
+    if key in cache and not force:
+        return cache[key]
+    saved = {k: get_knob(k) for k in KNOBS}
+    results = []
+    try:
+        for cfg in candidates(shape, precision):
+            t = time_config(shape, method, precision, BC, cfg, steps)
+            results.append((t, cfg))
+            if verbose:
+                print("%-40s %.4f s" % (cfg, t))
+    finally:
+        for k, v in saved.items():
+            set_knob(k, v)
+    t, best = min(results, key=lambda r: r[0])
+    n = int(np.prod(shape))
+    entry = dict(best, seconds_per_step=t / steps, gpt_steps_per_s=n * steps / t / 1e9,
+                 candidates=len(results))
+    cache[key] = entry
+    _save_cache(cache)
+    return entry
+
+
+def apply(shape, method=2, precision=3, BC=2):
+    """Set the knobs from the cache for this problem class; returns the entry
+    used (or None when the class was never tuned)."""
+    entry = _load_cache().get(problem_key(shape, method, precision, BC))
+    if entry:
+        for k in KNOBS:
+            if k in entry:
+                set_knob(k, entry[k])
+    return entry

@@ -48,6 +48,45 @@ int set_error(int code, const char* fmt, ...) {
 }  // namespace nlse
 extern "C" const char* nlse_version(void) { return "nlse_gb300 1.0 (sm_103a)"; }
 
+// ---------------------------------------------------------------------------
+// tuning knobs (process-wide; read when a stage launch is issued or a graph is
+// captured, so they apply to solvers created or re-captured afterwards)
+// ---------------------------------------------------------------------------
+namespace nlse {
+namespace wide {
+extern int g_zc_override;
+}
+}  // namespace nlse
+static int g_default_graph_steps = 8;
+
+extern "C" int nlse_tune_set(const char* key, long long value) {
+  if (!key) return fail(NLSE_ERR_ARG, "key is NULL");
+  if (!strcmp(key, "wide.zc")) {
+    if (value < 0 || value > (1 << 20)) return fail(NLSE_ERR_ARG, "wide.zc out of range");
+    nlse::wide::g_zc_override = (int)value;
+    return NLSE_OK;
+  }
+  if (!strcmp(key, "graph.steps")) {
+    if (value < 0 || value > 100000) return fail(NLSE_ERR_ARG, "graph.steps out of range");
+    g_default_graph_steps = (int)value;
+    return NLSE_OK;
+  }
+  return fail(NLSE_ERR_ARG, "unknown tuning key '%s'", key);
+}
+
+extern "C" int nlse_tune_get(const char* key, long long* value) {
+  if (!key || !value) return fail(NLSE_ERR_ARG, "NULL argument");
+  if (!strcmp(key, "wide.zc")) {
+    *value = nlse::wide::g_zc_override;
+    return NLSE_OK;
+  }
+  if (!strcmp(key, "graph.steps")) {
+    *value = g_default_graph_steps;
+    return NLSE_OK;
+  }
+  return fail(NLSE_ERR_ARG, "unknown tuning key '%s'", key);
+}
+
 extern "C" double nlse_linear_stability_k(int ndim, int method, double h, double a) {
   double klin = h * h / ((double)ndim * sqrt(2.0) * a);
   if (method == 2) klin *= 0.75;
@@ -265,7 +304,7 @@ extern "C" int nlse_solver_create(const nlse_problem* p, nlse_solver** out) {
   s->cd = consts_double(p);
   s->cf = p->precision == NLSE_PREC_MIXED ? consts_mixed(p) : consts_single(p);
   s->kernel_kind = (p->flags & NLSE_FLAG_GATHER) ? KERNEL_GATHER : KERNEL_TILED;
-  s->graph_steps = 8;
+  s->graph_steps = g_default_graph_steps;
   cudaError_t e = cudaGetDevice(&s->device);
   if (e != cudaSuccess) {
     delete s;
