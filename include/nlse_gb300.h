@@ -216,6 +216,31 @@ int nlse_batch_stream(nlse_batch *b, void **stream);
 /* Kernel launches issued by the last nlse_batch_run (1 when any solve ran). */
 int nlse_batch_last_launches(nlse_batch *b);
 
+/* ------------------------------------------------------------------------
+ * Allocation-free FP64 chunk.  No counterpart in the reference: an addition
+ * for callers that must not allocate device memory -- work recorded while a
+ * stream is captured into a CUDA graph, plug-ins whose host application owns
+ * every device allocation (e.g. a MEX function on MATLAB gpuArray data), and
+ * real-time loops that may not allocate after start-up.
+ *
+ * Same problem description as nlse_take_steps, but the arrays are DEVICE
+ * pointers owned by the caller (planar doubles; dUi may be NULL) and the call
+ * is asynchronous on `stream` (a cudaStream_t; NULL = legacy default stream).
+ * precision must be NLSE_PREC_DOUBLE (results identical to nlse_take_steps).
+ * The RK4 scratch is a fixed device array inside the library holding
+ * NLSE_NOALLOC_MAX_POINTS grid points (16 MiB, held on every GPU that loads
+ * the library until the process exits); larger grids return
+ * NLSE_ERR_CAPACITY.  The first call on a device looks the array's address
+ * up once (no allocation); make that first call before any stream capture.
+ * All calls share the array and it keeps the last call's contents (nothing in
+ * it must start at zero): calls that overlap on the GPU race and must be
+ * serialised by the caller.
+ * ---------------------------------------------------------------------- */
+#define NLSE_NOALLOC_MAX_POINTS (1 << 18)
+int nlse_take_steps_noalloc(const nlse_problem *p, const double *dUr, const double *dUi,
+                            const double *dV, double *dOutr, double *dOuti, int chunk_size,
+                            void *stream);
+
 /* Linear stability limit of the time step used by the NLSEmagic drivers:
  * h^2 / (ndim * sqrt(2) * a) for CD, 3/4 of that for 2SHOC
  * (src/NLSEmagic3D/NLSEmagic3D.m:154-163). */

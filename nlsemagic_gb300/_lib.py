@@ -86,6 +86,8 @@ SIGNATURES = {
     "nlse_batch_stats": (_i, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_ll), ctypes.POINTER(_ll)]),
     "nlse_batch_stream": (_i, [_vp, ctypes.POINTER(_vp)]),
     "nlse_batch_last_launches": (_i, [_vp]),
+    "nlse_take_steps_noalloc": (_i, [ctypes.POINTER(Problem), _vp, _vp, _vp, _vp, _vp, _i,
+                                     _vp]),
 }
 for _dim, _dims in ((1, [_i]), (2, [_i, _i]), (3, [_i, _i, _i])):
     SIGNATURES["NLSE%dD_TAKE_STEPS_CUDA" % _dim] = (

@@ -33,6 +33,7 @@ UNITS = {
     "kern_util.cu": [],
     "nlse_abi.cu": [],
     "nlse_batch.cu": ["-fmad=false"],
+    "nlse_noalloc.cu": [],
 }
 
 
