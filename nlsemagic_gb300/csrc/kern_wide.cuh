@@ -100,13 +100,8 @@ __global__ void __launch_bounds__(TX* TY, 3) wide3d(Geom g, tiled::MixedPol::Arg
   auto gidx = [&](int xx, int yy, int zz) -> long long {
     return ((long long)zz * N + yy) * M + xx;
   };
-
-  // ---- shell planes of this chunk (z < H or z > L-1-H): gather form ----
-  for (int zz = z0; zz < z1; ++zz) {
-    if (zz >= H && zz <= L - 1 - H) continue;
-    if (in_grid) shell_point<METHOD, BC>(g, A, x, y, zz);
-  }
-  if (zs >= ze) return;  // no deep plane in this chunk
+  (void)edge_tile;
+  if (zs >= ze) return;  // no deep plane in this chunk (shell points: shell3d)
 
   if (TMA && (su32(smem) & 127u) != 0) {  // TMA destinations must be 128-byte aligned
     if (tid == 0) atomicExch(A.err, NLSE_ERR_STATE);
@@ -234,9 +229,55 @@ __global__ void __launch_bounds__(TX* TY, 3) wide3d(Geom g, tiled::MixedPol::Arg
         A.a.hi_out[p] = ho;
         A.a.lo_out[p] = lo2;
       }
-    } else if (edge_tile && in_grid) {
-      shell_point<METHOD, BC>(g, A, x, y, z);  // x or y within H of a face
     }
+  }
+}
+
+// Shell points (within H cells of a face) of a 3D grid, enumerated as
+//   z < H or z >= L-H: whole planes;
+//   else y < H or y >= N-H: whole rows;
+//   else x < H or x >= M-H: the 2H end points of a row;
+// each evaluated in gather form.  Runs after wide3d in the same stage; the
+// two kernels write disjoint points.
+template <int METHOD, int BC>
+__global__ void __launch_bounds__(256) shell3d(Geom g, tiled::MixedPol::Args A) {
+  constexpr int H = METHOD == 2 ? 2 : 1;
+  const long long M = g.M, N = g.N, L = g.L;
+  // a grid with a dimension <= 2H has no deep point: every point is shell
+  const bool thin = M <= 2 * H || N <= 2 * H || L <= 2 * H;
+  const long long nz = thin ? g.n : 2 * H * M * N;                  // shell planes
+  const long long ny = thin ? 0 : (L - 2 * H) * 2 * H * M;          // shell rows of deep planes
+  const long long nx = thin ? 0 : (L - 2 * H) * (N - 2 * H) * 2 * H;  // row ends
+  const long long total = nz + ny + nx;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    long long x, y, z;
+    if (thin) {
+      z = t / (M * N);
+      long long r = t - z * M * N;
+      y = r / M;
+      x = r - y * M;
+    } else if (t < nz) {
+      long long pl = t / (M * N), r = t - pl * M * N;
+      z = pl < H ? pl : L - 2 * H + pl;
+      y = r / M;
+      x = r - y * M;
+    } else if (t < nz + ny) {
+      long long u = t - nz;
+      long long row = u / M;
+      x = u - row * M;
+      long long zz = row / (2 * H), yr = row - zz * 2 * H;
+      z = H + zz;
+      y = yr < H ? yr : N - 2 * H + yr;
+    } else {
+      long long u = t - nz - ny;
+      long long row = u / (2 * H), xr = u - row * 2 * H;
+      long long zz = row / (N - 2 * H), yy = row - zz * (N - 2 * H);
+      z = H + zz;
+      y = H + yy;
+      x = xr < H ? xr : M - 2 * H + xr;
+    }
+    shell_point<METHOD, BC>(g, A, (int)x, (int)y, (int)z);
   }
 }
 
@@ -285,8 +326,17 @@ cudaError_t launch(const Geom& g, const tiled::MixedPol::Args& A, cudaStream_t s
   bool tma = tiled::make_map(&m0, A.a.hi_in, g, 1, SH::PX, SH::PY) &&
              tiled::make_map(&m1, ein, g, 1, SH::PX, SH::PY);
   int zc = g_zc_override > 0 ? g_zc_override : default_zc(g);
-  if (tma) return launch_k<METHOD, BC, true>(g, A, st, m0, m1, zc);
-  return launch_k<METHOD, BC, false>(g, A, st, m0, m1, zc);
+  cudaError_t e = tma ? launch_k<METHOD, BC, true>(g, A, st, m0, m1, zc)
+                      : launch_k<METHOD, BC, false>(g, A, st, m0, m1, zc);
+  if (e != cudaSuccess) return e;
+  constexpr int H = METHOD == 2 ? 2 : 1;
+  long long shell = g.n - (long long)(g.M - 2 * H) * (g.N - 2 * H) * (g.L - 2 * H);
+  if (g.M <= 2 * H || g.N <= 2 * H || g.L <= 2 * H) shell = g.n;
+  if (shell <= 0) return cudaSuccess;
+  long long blocks = (shell + 255) / 256;
+  if (blocks > 152LL * 16) blocks = 152LL * 16;
+  shell3d<METHOD, BC><<<(unsigned)blocks, 256, 0, st>>>(g, A);
+  return cudaGetLastError();
 }
 
 }  // namespace wide

@@ -549,7 +549,13 @@ extern "C" int nlse_solver_stream(nlse_solver* s, void** stream) {
   return NLSE_OK;
 }
 
-extern "C" int nlse_solver_launches_per_step(const nlse_solver* s) { return s ? 4 : 0; }
+extern "C" int nlse_solver_launches_per_step(const nlse_solver* s) {
+  if (!s) return 0;
+  // mixed-precision 3D grids on the tiled path: deep-point kernel + shell kernel per stage
+  bool two = s->prob.precision == NLSE_PREC_MIXED && s->kernel_kind == KERNEL_TILED &&
+             tiled_supported(s->g, s->g.ndim) && s->prob.bc != 4;
+  return two ? 8 : 4;
+}
 
 extern "C" long long nlse_solver_device_bytes(const nlse_solver* s) {
   return s ? (long long)s->bytes : 0;

@@ -97,14 +97,22 @@ __device__ __forceinline__ float2 onesided_sum(const HE* os) {
   return pfma(P2(-5.f), d1, pfma(P2(4.f), d2, pmul(P2(-1.f), d3)));
 }
 
-// MSD ratio in FP64 (boundary points only; |w|^2 of a small FP32 value would
-// underflow in FP32): cross = 0 -> (u.w)/|w|^2, cross = 1 -> (u_i w_r - u_r w_i)/|w|^2.
+// MSD ratio, cross = 0 -> (u.w)/|w|^2, cross = 1 -> (u_i w_r - u_r w_i)/|w|^2.
+// |w|^2 of a small FP32 value would underflow, so w is first scaled by an
+// exact power of two that brings its larger component into [0.5, 1):
+// (u.(s w)) / |s w|^2 * s, all in FP32 (no FP64 work on the boundary).
+// A zero w gives 0/0 = NaN, as the unguarded reference does; callers apply
+// the zero-neighbour guard first.
 __device__ __forceinline__ float msd_ratio(float2 u, float2 w, int cross) {
-  double wx = w.x, wy = w.y, ux = u.x, uy = u.y;
-  double num = cross ? __dsub_rn(__dmul_rn(uy, wx), __dmul_rn(ux, wy))
-                     : __dadd_rn(__dmul_rn(ux, wx), __dmul_rn(uy, wy));
-  double den = __dadd_rn(__dmul_rn(wx, wx), __dmul_rn(wy, wy));
-  return (float)__ddiv_rn(num, den);
+  float m = fmaxf(fabsf(w.x), fabsf(w.y));
+  int e = 0;
+  frexpf(m, &e);
+  float sc = ldexpf(1.f, -e);
+  float wx = __fmul_rn(w.x, sc), wy = __fmul_rn(w.y, sc);
+  float num = cross ? __fsub_rn(__fmul_rn(u.y, wx), __fmul_rn(u.x, wy))
+                    : __fmaf_rn(u.x, wx, __fmul_rn(u.y, wy));
+  float den = __fmaf_rn(wx, wx, __fmul_rn(wy, wy));
+  return __fmul_rn(__fdiv_rn(num, den), sc);
 }
 
 // ---- D at a boundary point -------------------------------------------------

@@ -194,3 +194,24 @@ def test_mixed_all_boundary_codes(gpu_lib, ndim, method, BC):
     want = orc(*args, 2)
     got = gpu(*args, 3)
     assert W.rel_l2(got, want) <= MIXED_TOL
+
+
+@pytest.mark.parametrize("shape", [(33, 5, 5), (4, 4, 30), (3, 40, 3), (36, 17, 9), (64, 40, 21),
+                                   (5, 6, 7), (70, 9, 33)])
+@pytest.mark.parametrize("method", [1, 2])
+@pytest.mark.parametrize("BC", [1, 2, 3])
+def test_mixed_3d_edge_shapes(gpu_lib, shape, method, BC):
+    # thin and odd grids: the tiled path (deep kernel + shell kernel, or
+    # plain loads where the row pitch rules out TMA) against the FP64 oracle
+    h = 0.3
+    axes = [-n * h / 2 + h * np.arange(n) for n in shape]
+    X, Y, Z = np.meshgrid(*axes, indexing="ij")
+    r2 = X * X + Y * Y + Z * Z
+    U = (np.exp(-r2 / 20.0) * np.exp(0.3j * X) + 0.4).astype(complex)
+    V = 0.3 * r2 / r2.max()
+    k = 0.5 * W.linear_stability_k(3, method, h, 1.0)
+    args = (U, V, -1.0, 1.0, h * h, BC, 12, k, method)
+    want = orc(*args, 2)
+    got = gpu(*args, 3)
+    assert W.rel_l2(got, want) <= MIXED_TOL
+    assert W.rel_l2(gpu(*args, 3, gather=True), want) <= MIXED_TOL
