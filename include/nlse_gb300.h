@@ -241,6 +241,18 @@ int nlse_take_steps_noalloc(const nlse_problem *p, const double *dUr, const doub
                             const double *dV, double *dOutr, double *dOuti, int chunk_size,
                             void *stream);
 
+/* ------------------------------------------------------------------------
+ * Launch tuning knobs (process-wide; no reference counterpart; set by the
+ * autotuner in nlsemagic_gb300/autotune.py).  They are read when a stage
+ * launch is issued or a CUDA graph captured, so they affect solvers created
+ * (or graphs captured) afterwards.  Keys:
+ *   "wide.zc"      z-chunk length of the mixed-precision 3D kernel (planes a
+ *                  CTA streams through); 0 = built-in heuristic.
+ *   "graph.steps"  RK4 steps per captured graph for new solvers (default 8).
+ * ---------------------------------------------------------------------- */
+int nlse_tune_set(const char *key, long long value);
+int nlse_tune_get(const char *key, long long *value);
+
 /* Linear stability limit of the time step used by the NLSEmagic drivers:
  * h^2 / (ndim * sqrt(2) * a) for CD, 3/4 of that for 2SHOC
  * (src/NLSEmagic3D/NLSEmagic3D.m:154-163). */

@@ -88,6 +88,8 @@ SIGNATURES = {
     "nlse_batch_last_launches": (_i, [_vp]),
     "nlse_take_steps_noalloc": (_i, [ctypes.POINTER(Problem), _vp, _vp, _vp, _vp, _vp, _i,
                                      _vp]),
+    "nlse_tune_set": (_i, [ctypes.c_char_p, _ll]),
+    "nlse_tune_get": (_i, [ctypes.c_char_p, ctypes.POINTER(_ll)]),
 }
 for _dim, _dims in ((1, [_i]), (2, [_i, _i]), (3, [_i, _i, _i])):
     SIGNATURES["NLSE%dD_TAKE_STEPS_CUDA" % _dim] = (

@@ -50,12 +50,20 @@ def test_library_exports_every_declared_symbol(lib):
 
 def test_python_signatures_cover_header(lib):
     # every declared symbol has a ctypes signature (so no call goes untyped)
-    assert set(declared_functions()) <= set(_lib.SIGNATURES) | {"nlse_batch_create",
-        "nlse_batch_destroy", "nlse_batch_run", "nlse_batch_add", "nlse_batch_download",
-        "nlse_batch_count", "nlse_batch_autotune"} | set(n for n in declared_functions()
-                                                     if n.startswith("nlse_serve")
-                                                     or n.startswith("nlse_batch")
-                                                     or n.startswith("nlse_noalloc"))
+    missing = set(declared_functions()) - set(_lib.SIGNATURES)
+    assert not missing, missing
+
+
+def test_tuning_knobs_roundtrip_and_validation(lib):
+    from nlsemagic_gb300 import autotune
+    old = autotune.get_knob("wide.zc")
+    autotune.set_knob("wide.zc", 48)
+    assert autotune.get_knob("wide.zc") == 48
+    autotune.set_knob("wide.zc", old)
+    with pytest.raises(_lib.NLSEError):
+        autotune.set_knob("no.such.knob", 1)
+    with pytest.raises(_lib.NLSEError):
+        autotune.set_knob("graph.steps", -3)
 
 
 def _call(lib, U, BC=2, method=1, precision=2, dims=None, h2=0.01, k=1e-3, chunk=1):
