@@ -342,7 +342,8 @@ def run_gpu(args, w):
     # ---- FP64 plain path on the same workload (for the mixed/FP64 ratio and
     # the error of the mixed path), a shorter run
     fp64 = None
-    if args.fp64_steps > 0 and rank == 0:
+    fp64_steps = steps if args.fp64_steps < 0 else args.fp64_steps
+    if fp64_steps > 0 and rank == 0:
         s64 = ng.Solver(w.U.shape, method=w.method, precision=ng.PREC_DOUBLE, BC=w.BC, s=w.s,
                         a=w.a, h2=w.h2, k=w.k)
         s64.set_graph_steps(args.graph_steps)
@@ -356,23 +357,23 @@ def run_gpu(args, w):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(st64)
-        s64.run(args.fp64_steps)
+        s64.run(fp64_steps)
         e1.record(st64)
         e1.synchronize()
         t64 = e0.elapsed_time(e1) / 1000.0
         smx.upload_device(Ur.data_ptr(), Ui.data_ptr(), Vd.data_ptr())
-        smx.run(args.fp64_steps)
-        err = None
-        try:
-            err = float(np.linalg.norm((smx.download() - s64.download()).ravel())
-                        / np.linalg.norm(s64.download().ravel()))
-        except Exception:
-            pass
-        fp64 = {"value": float(n) * args.fp64_steps / t64 / 1e9, "unit": UNIT,
-                "rk4_steps": args.fp64_steps,
-                "roofline_frac_of_measured_hbm": float(n) * args.fp64_steps * BYTES_FP64 / t64 /
+        smx.run(fp64_steps)
+        u64 = s64.download()
+        umx = smx.download()
+        err = float(np.linalg.norm((umx - u64).ravel()) / np.linalg.norm(u64.ravel()))
+        m64 = float(np.sum(np.abs(u64) ** 2))
+        fp64 = {"value": float(n) * fp64_steps / t64 / 1e9, "unit": UNIT,
+                "rk4_steps": fp64_steps,
+                "roofline_frac_of_measured_hbm": float(n) * fp64_steps * BYTES_FP64 / t64 /
                 1e9 / peaks()[0],
-                "mixed_rel_l2_vs_fp64_same_steps": err}
+                "mass_rel_drift": abs(m64 - mass0) / mass0,
+                "mixed_rel_l2_vs_fp64": err,
+                "mixed_rel_l2_tolerance": 1e-6}
         s64.close()
         smx.close()
 
@@ -385,9 +386,11 @@ def run_gpu(args, w):
         "frac": achieved / peak,
         "traffic": (traffic_ppt * n / 4.0) if traffic_ppt else None,
         "peak_kind": peak_kind,
-        "kernel": "RK4 stage kernels (4 launches per RK4 step)",
+        "kernel": "RK4 step: per stage the deep-point kernel (wide3d) and the shell "
+                  "kernels (shell_d, shell_f); %d launches per RK4 step, timed as one "
+                  "CUDA graph" % solver.launches_per_step,
         "algorithmic_bytes_per_point_step": BYTES_MIXED,
-        "algorithmic_bytes_per_launch": BYTES_MIXED / 4.0 * n,
+        "algorithmic_bytes_per_stage": BYTES_MIXED / 4.0 * n,
         "model_frac_240B": value * BYTES_MODEL_MIXED / world / peak,
     }
     result = {
@@ -526,7 +529,8 @@ def main():
     ap.add_argument("--grid", type=int, default=320)
     ap.add_argument("--rk4-steps", type=int, default=500)
     ap.add_argument("--graph-steps", type=int, default=10)
-    ap.add_argument("--fp64-steps", type=int, default=20)
+    ap.add_argument("--fp64-steps", type=int, default=-1,
+                    help="RK4 steps of the FP64 comparison run (-1: the workload's own)")
     ap.add_argument("--cpu-sample-steps", type=int, default=1)
     ap.add_argument("--batch-solves", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=1000)

@@ -32,22 +32,13 @@ from .api import Solver, grid_dims
 KNOBS = ("wide.zc", "graph.steps")
 
 
-def _lib_sig():
-    lib = _lib.load()
-    lib.nlse_tune_set.restype = ctypes.c_int
-    lib.nlse_tune_set.argtypes = [ctypes.c_char_p, ctypes.c_longlong]
-    lib.nlse_tune_get.restype = ctypes.c_int
-    lib.nlse_tune_get.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_longlong)]
-    return lib
-
-
 def set_knob(key, value):
-    _lib.check(_lib_sig().nlse_tune_set(key.encode(), int(value)))
+    _lib.check(_lib.load().nlse_tune_set(key.encode(), int(value)))
 
 
 def get_knob(key):
     v = ctypes.c_longlong()
-    _lib.check(_lib_sig().nlse_tune_get(key.encode(), ctypes.byref(v)))
+    _lib.check(_lib.load().nlse_tune_get(key.encode(), ctypes.byref(v)))
     return v.value
 
 

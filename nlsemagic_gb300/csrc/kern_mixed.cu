@@ -37,6 +37,18 @@ static cudaError_t by_bc(const Geom& g, int BC, const Consts<float>& c, const Mi
   }
 }
 
+bool mixed_wants_shell_scratch(const Geom& g, int method, int BC, int kernel_kind) {
+  return kernel_kind == KERNEL_TILED && g.ndim == 3 && tiled_supported(g, 3) && BC != 4 &&
+         method == 2;
+}
+
+int mixed_stage_launches(const Geom& g, int method, int BC, int kernel_kind, bool have_dsh) {
+  if (!(kernel_kind == KERNEL_TILED && g.ndim == 3 && tiled_supported(g, 3) && BC != 4)) return 1;
+  const int H = method == 2 ? 2 : 1;
+  const int deep = wide::shell_thin(g, H) ? 0 : 1;
+  return deep + 1 + (method == 2 && have_dsh ? 1 : 0);
+}
+
 cudaError_t launch_mixed_stage(const Geom& g, int method, int BC, const Consts<float>& c,
                                const MixedStageArgs& a, int stage, cudaStream_t st,
                                int kernel_kind) {

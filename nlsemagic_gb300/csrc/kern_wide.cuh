@@ -1,6 +1,9 @@
-// Mixed-precision 3D stage kernel, register-queue form.
+// Mixed-precision 3D stage kernels (FP32 stages, compensated hi/lo state).
 //
-// Away from the boundary the RK4 stage needs, per point, the stage input
+// A stage is split by point class:
+//
+// deep points (every coordinate at least H cells from a face; H = 1 for CD,
+// 2 for 2SHOC) -- wide3d.  There the RK4 stage needs the stage input
 // Y = hi + E at the point, its 6 face neighbours and (2SHOC) the 6 points two
 // cells away along the axes: 2SHOC's compact operator reduces there to the
 // standard wide fourth-order Laplacian (nlse_mixed.cuh, f_wide_2shoc).  One
@@ -9,16 +12,24 @@
 //     by TMA (cp.async.bulk.tensor.3d, one elected thread, mbarrier per slot,
 //     issued P planes ahead of use), from which a thread reads the in-plane
 //     neighbours of its point;
-//   - the z neighbours of a thread's own column are kept in a register queue
-//     (planes z-H .. z+H), so each plane value is read from shared memory
+//   - the z neighbours of a thread's own column are kept in registers, one
+//     entry per ring slot, so each plane value is read from shared memory
 //     once as a queue entry;
-//   - the points within H cells of a face (the shell: boundary points and,
-//     for 2SHOC, the first interior layer, where the compact scheme uses the
-//     boundary-condition D values) are evaluated with the gather-form
-//     functions (kern_gather.cuh), which recompute everything they need from
-//     global memory and depend on no other thread.
+//   - the z loop is unrolled by the ring length, so ring slots, mbarrier
+//     parities and register-queue entries are compile-time indices.
 // Every mbarrier wait is bounded (NLSE_ERR_TIMEOUT in the error word, copies
 // in flight drained, CTA returns).
+//
+// shell points (within H cells of a face) -- for CD one gather-form kernel
+// (shell3d, kern_gather.cuh functions); for 2SHOC two passes:
+//   shell_d: D = the CD2 Laplacian-plus-BC value at every point within 3
+//            cells of a face (the boundary-condition D on the faces),
+//            written to a scratch array;
+//   shell_f: F and the RK4 update at the shell points, the compact operator
+//            reading D from that array (and, for MSD faces, the inward
+//            neighbour's F from the same D values).
+// Each pass evaluates exactly the expressions of the gather form, so shell
+// results are the gather kernel's bit for bit.
 #pragma once
 
 #include "kern_gather.cuh"
@@ -36,18 +47,22 @@ using tiled::round_up;
 using tiled::su32;
 using tiled::tma_load_3d;
 
-template <int METHOD, int TX, int TY>
+typedef tiled::MixedPol::Args Args;
+
+template <int METHOD>
 struct WShape {
+  static constexpr int TX = 32, TY = 8, NT = TX * TY;
   static constexpr int H = METHOD == 2 ? 2 : 1;   // stencil reach along each axis
   static constexpr int XO = 2;                    // plane origin x0 - 2 (16-byte aligned)
   static constexpr int PX = TX + 4;               // [x0-2, x0+TX+2)
   static constexpr int PY = TY + 2 * H;           // [y0-H, y0+TY+H)
   static constexpr int P = 2;                     // planes in flight beyond the queue head
-  // Ring slots.  The prologue stages planes zs-H .. zs+H+P-1 (2H+P planes)
-  // before any is released; in the loop the live planes are z .. z+H+P
-  // (H+P+1 <= 2H+P).  Refilling slot (z+H+P) % NU at iteration z reuses the
-  // slot of plane z-H, whose last read was at iteration z-H.
-  static constexpr int NU = 2 * H + P;
+  // Ring slots.  The prologue stages 2H+P planes before any slot is reused.
+  // In the loop, iteration z refills the slot of plane z+H+P-NU; the last
+  // read of that plane is at iteration z+H+P-NU (as the centre plane), and
+  // the only barrier between it and the refill is that of iteration z-1,
+  // which precedes that iteration's reads -- so z+H+P-NU <= z-2.
+  static constexpr int NU = (2 * H + P) > (H + P + 2) ? (2 * H + P) : (H + P + 2);
   static constexpr int PLANE = round_up(PX * PY * 8, 128);
   static constexpr int SLOT = 2 * PLANE;          // hi plane + E plane
   static constexpr int B_OFF = NU * SLOT;
@@ -55,53 +70,29 @@ struct WShape {
   static constexpr unsigned TX_BYTES = (unsigned)(2 * PX * PY * 8);
 };
 
-// gather-form evaluation and update of one shell point (kept out of line so
-// that the streaming path keeps its registers)
-template <int METHOD, int BC>
-__device__ __noinline__ void shell_point(const Geom& g, const tiled::MixedPol::Args& A, int x,
-                                         int y, int z) {
-  const float2* Ein = A.stage == 1 ? A.a.lo_in : A.a.e_in;
-  mixed::YIn Y{A.a.hi_in, Ein};
-  long long p = ((long long)z * g.N + y) * g.M + x;
-  float2 T = mixed::f_at<3, METHOD, BC>(g, A.c, Y, A.a.V, z, y, x);
-  mixed::update(A.c, A.stage, p, T, A.a.hi_in, A.a.lo_in, A.a.e_in, A.a.K, A.a.e_out,
-                A.a.hi_out, A.a.lo_out);
-}
-
-template <int METHOD, int BC, int TX, int TY, bool TMA>
-__global__ void __launch_bounds__(TX* TY, 3) wide3d(Geom g, tiled::MixedPol::Args A, int zc,
-                                                    const __grid_constant__ CUtensorMap tm0,
-                                                    const __grid_constant__ CUtensorMap tm1) {
-  typedef WShape<METHOD, TX, TY> SH;
+template <int METHOD, int STAGE, bool TMA>
+__global__ void __launch_bounds__(256, 3) wide3d(Geom g, Args A, int zc,
+                                                 const __grid_constant__ CUtensorMap tm0,
+                                                 const __grid_constant__ CUtensorMap tm1) {
+  typedef WShape<METHOD> SH;
   typedef mixed::HE HE;
-  constexpr int H = SH::H, XO = SH::XO, PX = SH::PX, PY = SH::PY, NU = SH::NU, P = SH::P;
-  constexpr int NT = TX * TY;
-  constexpr int Q = 2 * H + 1;
+  constexpr int TX = SH::TX, TY = SH::TY, NT = SH::NT, H = SH::H, XO = SH::XO, PX = SH::PX,
+                PY = SH::PY, NU = SH::NU, P = SH::P;
 
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned long long* bars = reinterpret_cast<unsigned long long*>(smem + SH::B_OFF);
 
   const int M = g.M, N = g.N, L = g.L;
-  const int nbx = (M + TX - 1) / TX, nby = (N + TY - 1) / TY, nbz = (L + zc - 1) / zc;
-  const int bx = blockIdx.x, by = blockIdx.y, bz = blockIdx.z;
-  if (bx >= nbx || by >= nby || bz >= nbz) return;
-  const int x0 = bx * TX, y0 = by * TY, z0 = bz * zc;
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * zc;
+  if (x0 >= M || y0 >= N || z0 >= L) return;
   const int z1 = z0 + zc < L ? z0 + zc : L;  // owned planes [z0, z1)
+  const int zs = z0 > H ? z0 : H;            // deep planes of this chunk: [zs, ze)
+  const int ze = z1 < L - H ? z1 : L - H;
+  if (zs >= ze) return;
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
   const int x = x0 + tx, y = y0 + ty;
-  const bool in_grid = x < M && y < N;
-  const bool deep_xy = x >= H && x <= M - 1 - H && y >= H && y <= N - 1 - H;
-  const bool edge_tile = x0 < H || x0 + TX > M - 1 - H || y0 < H || y0 + TY > N - 1 - H;
-  // deep planes of this chunk: [zs, ze)
-  const int zs = z0 > H ? z0 : H;
-  const int ze = z1 < L - H ? z1 : L - H;
-
-  const float2* Ein = A.stage == 1 ? A.a.lo_in : A.a.e_in;
-  auto gidx = [&](int xx, int yy, int zz) -> long long {
-    return ((long long)zz * N + yy) * M + xx;
-  };
-  (void)edge_tile;
-  if (zs >= ze) return;  // no deep plane in this chunk (shell points: shell3d)
+  const bool deep = x >= H && x <= M - 1 - H && y >= H && y <= N - 1 - H;
+  const float2* Ein = STAGE == 1 ? A.a.lo_in : A.a.e_in;
 
   if (TMA && (su32(smem) & 127u) != 0) {  // TMA destinations must be 128-byte aligned
     if (tid == 0) atomicExch(A.err, NLSE_ERR_STATE);
@@ -113,22 +104,21 @@ __global__ void __launch_bounds__(TX* TY, 3) wide3d(Geom g, tiled::MixedPol::Arg
   }
   __syncthreads();
 
-  const int pfirst = zs - H, plast = ze - 1 + H;  // planes this CTA stages
-  auto hplane = [&](int zz) -> float2* {
-    return reinterpret_cast<float2*>(smem + (zz % NU) * SH::SLOT);
+  // plane zz lives in slot (zz - pfirst) % NU; its k-th use of that slot
+  // completes mbarrier phase k, k = (zz - pfirst) / NU
+  const int pfirst = zs - H, plast = ze - 1 + H;
+  auto hplane = [&](int s) -> float2* { return reinterpret_cast<float2*>(smem + s * SH::SLOT); };
+  auto eplane = [&](int s) -> float2* {
+    return reinterpret_cast<float2*>(smem + s * SH::SLOT + SH::PLANE);
   };
-  auto eplane = [&](int zz) -> float2* {
-    return reinterpret_cast<float2*>(smem + (zz % NU) * SH::SLOT + SH::PLANE);
-  };
-  auto issue = [&](int zz) {
-    if (zz < pfirst || zz > plast) return;
+  auto issue = [&](int zz, int s) {
+    if (zz > plast) return;
     if (TMA) {
       if (tid == 0) {
-        unsigned long long* b = &bars[zz % NU];
-        fence_proxy_async();
-        mbar_expect_tx(b, SH::TX_BYTES);
-        tma_load_3d(hplane(zz), &tm0, x0 - XO, y0 - H, zz, b);
-        tma_load_3d(eplane(zz), &tm1, x0 - XO, y0 - H, zz, b);
+        fence_proxy_async();  // earlier generic reads of the slot before the async write
+        mbar_expect_tx(&bars[s], SH::TX_BYTES);
+        tma_load_3d(hplane(s), &tm0, x0 - XO, y0 - H, zz, &bars[s]);
+        tma_load_3d(eplane(s), &tm1, x0 - XO, y0 - H, zz, &bars[s]);
       }
     } else {
       for (int t = tid; t < PX * PY; t += NT) {
@@ -136,206 +126,353 @@ __global__ void __launch_bounds__(TX* TY, 3) wide3d(Geom g, tiled::MixedPol::Arg
         int gx = x0 - XO + ux, gy = y0 - H + uy;
         float2 h = make_float2(0.f, 0.f), e = h;
         if (gx >= 0 && gx < M && gy >= 0 && gy < N) {
-          long long p = gidx(gx, gy, zz);
+          long long p = ((long long)zz * N + gy) * M + gx;
           h = A.a.hi_in[p];
           e = Ein[p];
         }
-        hplane(zz)[t] = h;
-        eplane(zz)[t] = e;
+        hplane(s)[t] = h;
+        eplane(s)[t] = e;
       }
     }
   };
-  auto await = [&](int zz) -> bool {
-    if (!TMA || zz < pfirst || zz > plast) return true;
-    bool ok = mbar_wait(&bars[zz % NU], (unsigned)(((zz - pfirst) / NU) & 1));
-    if (!ok) atomicExch(A.err, NLSE_ERR_TIMEOUT);
-    return ok;
-  };
+  // bounded wait for every plane issued up to `upto` (error path only)
   auto drain = [&](int upto) {
-    if (TMA && tid == 0)
-      for (int zz = pfirst; zz <= upto && zz <= plast; ++zz)
-        mbar_wait(&bars[zz % NU], (unsigned)(((zz - pfirst) / NU) & 1));
+    if (!TMA || tid != 0) return;
+    if (upto > plast) upto = plast;
+    int from = upto - NU + 1 > pfirst ? upto - NU + 1 : pfirst;
+    for (int zz = from; zz <= upto; ++zz)
+      mbar_wait(&bars[(zz - pfirst) % NU], (unsigned)(((zz - pfirst) / NU) & 1));
   };
 
-  const int ux = tx + XO, uy = ty + H;
-  const int own = uy * PX + ux;
-  HE q[Q];  // own column, planes z-H .. z+H
+  const int own = (ty + H) * PX + tx + XO;
+  HE q[NU];  // q[s]: this thread's column value of the plane in slot s
 
-  // ---- prologue: stage planes zs-H .. zs+H+P-1, fill the queue up to zs+H-1
-  for (int zz = pfirst; zz <= zs + H + P - 1; ++zz) issue(zz);
-  if (!TMA) __syncthreads();
+  // ---- prologue: stage planes pfirst .. pfirst+2H+P-1 (slots 0..2H+P-1),
+  // queue planes pfirst .. pfirst+2H-1
+#pragma unroll
+  for (int t = 0; t < 2 * H + P; ++t) issue(pfirst + t, t);
   {
     bool ok = true;
-    for (int zz = pfirst; zz <= zs + H - 1; ++zz) ok &= await(zz);
+    if (TMA) {
+#pragma unroll
+      for (int t = 0; t < 2 * H; ++t) ok &= mbar_wait(&bars[t], 0u);
+      if (!ok) atomicExch(A.err, NLSE_ERR_TIMEOUT);
+    }
     if (__syncthreads_or(!ok)) {
-      drain(zs + H + P - 1);
+      drain(pfirst + 2 * H + P - 1);
       return;
     }
 #pragma unroll
-    for (int t = 0; t < Q - 1; ++t) {
-      q[t + 1].h = hplane(zs - H + t)[own];
-      q[t + 1].e = eplane(zs - H + t)[own];
+    for (int t = 0; t < 2 * H; ++t) {
+      q[t].h = hplane(t)[own];
+      q[t].e = eplane(t)[own];
     }
+    __syncthreads();  // slot 0 is refilled in the first iteration (2SHOC)
   }
 
-  for (int z = zs; z < ze; ++z) {
-    __syncthreads();  // plane z-1 is no longer read: its slot may be refilled
-    issue(z + H + P);
-    // pointwise operands of the deep point, fetched before the wait
-    const long long p = gidx(x, y, z);
-    const bool deep = in_grid && deep_xy;
-    float v = 0.f;
-    float2 lo = make_float2(0.f, 0.f), kv = lo;
-    if (deep) {
-      v = A.a.V[p];
-      if (A.stage >= 2) lo = A.a.lo_in[p];
-      if (A.stage == 4) kv = A.a.K[p];
-    }
-    bool ok = await(z + H);
-    if (!TMA) __syncthreads();
-    if (__syncthreads_or(!ok)) {
-      drain(z + H + P);
-      return;
-    }
+  const long long MN = (long long)M * N;
+  const long long pxy = (long long)y * M + x;
+  for (int zb = zs; zb < ze; zb += NU) {
+    const unsigned blk = (unsigned)((zb - zs) / NU) & 1u;
 #pragma unroll
-    for (int t = 0; t < Q - 1; ++t) q[t] = q[t + 1];
-    q[Q - 1].h = hplane(z + H)[own];
-    q[Q - 1].e = eplane(z + H)[own];
-
-    if (deep) {
-      const float2* hp = hplane(z);
-      const float2* ep = eplane(z);
-      const HE& u0 = q[H];
-      float2 T;
-      if (METHOD == 1) {
-        HE nb[6] = {q[2], q[0], {hp[own + PX], ep[own + PX]}, {hp[own - PX], ep[own - PX]},
-                    {hp[own + 1], ep[own + 1]}, {hp[own - 1], ep[own - 1]}};
-        T = mixed::f_interior_cd<3>(A.c, u0, v, nb);
-      } else {
-        HE fn[6] = {q[3], q[1], {hp[own + PX], ep[own + PX]}, {hp[own - PX], ep[own - PX]},
-                    {hp[own + 1], ep[own + 1]}, {hp[own - 1], ep[own - 1]}};
-        HE f2n[6] = {q[4], q[0], {hp[own + 2 * PX], ep[own + 2 * PX]},
-                     {hp[own - 2 * PX], ep[own - 2 * PX]}, {hp[own + 2], ep[own + 2]},
-                     {hp[own - 2], ep[own - 2]}};
-        T = mixed::f_wide_2shoc<3>(A.c, u0, v, fn, f2n);
+    for (int u = 0; u < NU; ++u) {
+      const int z = zb + u;
+      if (z >= ze) break;
+      const int sc = (u + H) % NU;      // slot of plane z
+      const int sn = (u + 2 * H) % NU;  // slot of plane z+H (queue head)
+      issue(z + H + P, (u + 2 * H + P) % NU);
+      // pointwise operands of the deep point, fetched before the wait
+      const long long p = (long long)z * MN + pxy;
+      float v = 0.f;
+      float2 lo = make_float2(0.f, 0.f), kv = lo;
+      if (deep) {
+        v = A.a.V[p];
+        if (STAGE >= 2) lo = A.a.lo_in[p];
+        if (STAGE == 4) kv = A.a.K[p];
       }
-      if (A.stage == 1) lo = u0.e;
-      float2 eo, ko, ho, lo2;
-      mixed::stage_update(A.c, A.stage, T, u0.h, lo, u0.e, kv, eo, ko, ho, lo2);
-      if (A.stage == 2) A.a.K[p] = ko;
-      if (A.stage < 4) {
-        A.a.e_out[p] = eo;
-      } else {
-        A.a.hi_out[p] = ho;
-        A.a.lo_out[p] = lo2;
+      bool ok = true;
+      if (TMA) {
+        ok = mbar_wait(&bars[sn], blk ^ (unsigned)((u + 2 * H) / NU));
+        if (!ok) atomicExch(A.err, NLSE_ERR_TIMEOUT);
+      }
+      if (__syncthreads_or(!ok)) {
+        drain(z + H + P);
+        return;
+      }
+      q[sn].h = hplane(sn)[own];
+      q[sn].e = eplane(sn)[own];
+
+      if (deep) {
+        const float2* hp = hplane(sc);
+        const float2* ep = eplane(sc);
+        const HE& u0 = q[sc];
+        float2 T;
+        if (METHOD == 1) {
+          HE nb[6] = {q[(sc + 1) % NU],           q[(sc + NU - 1) % NU],
+                      {hp[own + PX], ep[own + PX]}, {hp[own - PX], ep[own - PX]},
+                      {hp[own + 1], ep[own + 1]},   {hp[own - 1], ep[own - 1]}};
+          T = mixed::f_interior_cd<3>(A.c, u0, v, nb);
+        } else {
+          HE fn[6] = {q[(sc + 1) % NU],           q[(sc + NU - 1) % NU],
+                      {hp[own + PX], ep[own + PX]}, {hp[own - PX], ep[own - PX]},
+                      {hp[own + 1], ep[own + 1]},   {hp[own - 1], ep[own - 1]}};
+          HE f2n[6] = {q[(sc + 2) % NU],
+                       q[(sc + NU - 2) % NU],
+                       {hp[own + 2 * PX], ep[own + 2 * PX]},
+                       {hp[own - 2 * PX], ep[own - 2 * PX]},
+                       {hp[own + 2], ep[own + 2]},
+                       {hp[own - 2], ep[own - 2]}};
+          T = mixed::f_wide_2shoc<3>(A.c, u0, v, fn, f2n);
+        }
+        if (STAGE == 1) lo = u0.e;
+        float2 eo, ko, ho, lo2;
+        mixed::stage_update(A.c, STAGE, T, u0.h, lo, u0.e, kv, eo, ko, ho, lo2);
+        if (STAGE == 2) A.a.K[p] = ko;
+        if (STAGE < 4) {
+          A.a.e_out[p] = eo;
+        } else {
+          A.a.hi_out[p] = ho;
+          A.a.lo_out[p] = lo2;
+        }
       }
     }
   }
 }
 
-// Shell points (within H cells of a face) of a 3D grid, enumerated as
-//   z < H or z >= L-H: whole planes;
-//   else y < H or y >= N-H: whole rows;
-//   else x < H or x >= M-H: the 2H end points of a row;
-// each evaluated in gather form.  Runs after wide3d in the same stage; the
-// two kernels write disjoint points.
-template <int METHOD, int BC>
-__global__ void __launch_bounds__(256) shell3d(Geom g, tiled::MixedPol::Args A) {
-  constexpr int H = METHOD == 2 ? 2 : 1;
+// ---- shell enumeration ------------------------------------------------------
+// The points within W cells of a face of an M x N x L grid, enumerated as
+//   z < W or z >= L-W: whole planes;
+//   else y < W or y >= N-W: whole rows;
+//   else x < W or x >= M-W: the 2W end points of a row.
+// A grid with a dimension <= 2W is all shell.
+__host__ __device__ inline bool shell_thin(const Geom& g, int W) {
+  return g.M <= 2 * W || g.N <= 2 * W || g.L <= 2 * W;
+}
+
+__host__ __device__ inline long long shell_count(const Geom& g, int W) {
+  if (shell_thin(g, W)) return g.n;
+  return g.n - (long long)(g.M - 2 * W) * (g.N - 2 * W) * (g.L - 2 * W);
+}
+
+__device__ __forceinline__ void shell_coord(const Geom& g, int W, long long t, int& x, int& y,
+                                            int& z) {
   const long long M = g.M, N = g.N, L = g.L;
-  // a grid with a dimension <= 2H has no deep point: every point is shell
-  const bool thin = M <= 2 * H || N <= 2 * H || L <= 2 * H;
-  const long long nz = thin ? g.n : 2 * H * M * N;                  // shell planes
-  const long long ny = thin ? 0 : (L - 2 * H) * 2 * H * M;          // shell rows of deep planes
-  const long long nx = thin ? 0 : (L - 2 * H) * (N - 2 * H) * 2 * H;  // row ends
-  const long long total = nz + ny + nx;
+  if (shell_thin(g, W)) {
+    long long zz = t / (M * N), r = t - zz * M * N;
+    z = (int)zz;
+    y = (int)(r / M);
+    x = (int)(r - (long long)y * M);
+    return;
+  }
+  const long long nz = 2 * W * M * N;                  // shell planes
+  const long long ny = (L - 2 * W) * 2 * W * M;        // shell rows of the other planes
+  if (t < nz) {
+    long long pl = t / (M * N), r = t - pl * M * N;
+    z = (int)(pl < W ? pl : L - 2 * W + pl);
+    y = (int)(r / M);
+    x = (int)(r - (long long)y * M);
+  } else if (t < nz + ny) {
+    long long u = t - nz;
+    long long row = u / M;
+    x = (int)(u - row * M);
+    long long zz = row / (2 * W), yr = row - zz * 2 * W;
+    z = (int)(W + zz);
+    y = (int)(yr < W ? yr : N - 2 * W + yr);
+  } else {
+    long long u = t - nz - ny;
+    long long row = u / (2 * W), xr = u - row * 2 * W;
+    long long zz = row / (N - 2 * W), yy = row - zz * (N - 2 * W);
+    z = (int)(W + zz);
+    y = (int)(W + yy);
+    x = (int)(xr < W ? xr : M - 2 * W + xr);
+  }
+}
+
+// ---- CD shell: gather form ---------------------------------------------------
+template <int METHOD, int BC>
+__global__ void __launch_bounds__(256) shell3d(Geom g, Args A) {
+  constexpr int H = METHOD == 2 ? 2 : 1;
+  const float2* Ein = A.stage == 1 ? A.a.lo_in : A.a.e_in;
+  mixed::YIn Y{A.a.hi_in, Ein};
+  const long long total = shell_count(g, H);
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
        t += (long long)gridDim.x * blockDim.x) {
-    long long x, y, z;
-    if (thin) {
-      z = t / (M * N);
-      long long r = t - z * M * N;
-      y = r / M;
-      x = r - y * M;
-    } else if (t < nz) {
-      long long pl = t / (M * N), r = t - pl * M * N;
-      z = pl < H ? pl : L - 2 * H + pl;
-      y = r / M;
-      x = r - y * M;
-    } else if (t < nz + ny) {
-      long long u = t - nz;
-      long long row = u / M;
-      x = u - row * M;
-      long long zz = row / (2 * H), yr = row - zz * 2 * H;
-      z = H + zz;
-      y = yr < H ? yr : N - 2 * H + yr;
-    } else {
-      long long u = t - nz - ny;
-      long long row = u / (2 * H), xr = u - row * 2 * H;
-      long long zz = row / (N - 2 * H), yy = row - zz * (N - 2 * H);
-      z = H + zz;
-      y = H + yy;
-      x = xr < H ? xr : M - 2 * H + xr;
-    }
-    shell_point<METHOD, BC>(g, A, (int)x, (int)y, (int)z);
+    int x, y, z;
+    shell_coord(g, H, t, x, y, z);
+    long long p = lin(g, z, y, x);
+    float2 T = mixed::f_at<3, METHOD, BC>(g, A.c, Y, A.a.V, z, y, x);
+    mixed::update(A.c, A.stage, p, T, A.a.hi_in, A.a.lo_in, A.a.e_in, A.a.K, A.a.e_out,
+                  A.a.hi_out, A.a.lo_out);
   }
 }
 
-template <int METHOD, int BC, bool TMA>
-cudaError_t launch_k(const Geom& g, const tiled::MixedPol::Args& A, cudaStream_t st,
-                     const CUtensorMap& m0, const CUtensorMap& m1, int zc) {
-  constexpr int TX = 32, TY = 8;
-  typedef WShape<METHOD, TX, TY> SH;
-  auto kern = wide3d<METHOD, BC, TX, TY, TMA>;
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         SH::SMEM);
-    if (e != cudaSuccess) return e;
-    attr_set = true;
+// ---- 2SHOC shell, pass 1: D within 3 cells of a face ------------------------
+template <int BC>
+__global__ void __launch_bounds__(256) shell_d(Geom g, Args A) {
+  const float2* Ein = A.stage == 1 ? A.a.lo_in : A.a.e_in;
+  mixed::YIn Y{A.a.hi_in, Ein};
+  float2* D = A.a.dsh;
+  const long long total = shell_count(g, 3);
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    int x, y, z;
+    shell_coord(g, 3, t, x, y, z);
+    D[lin(g, z, y, x)] = mixed::d_at<3, BC>(g, A.c, Y, A.a.V, z, y, x);
   }
-  dim3 grid((g.M + TX - 1) / TX, (g.N + TY - 1) / TY, (g.L + zc - 1) / zc), block(TX, TY);
-  kern<<<grid, block, SH::SMEM, st>>>(g, A, zc, m0, m1);
+}
+
+// compact 2SHOC F at an interior point (z, y, x) = (i, j, k) with the D
+// values taken from D[] (same operands, same order as mixed::f_int)
+__device__ __forceinline__ float2 f2shoc_dbuf(const Geom& g, const Consts<float>& c,
+                                              const mixed::YIn& Y, const float* V,
+                                              const float2* D, int i, int j, int k) {
+  const long long p = lin(g, i, j, k);
+  const long long M = g.M, P = (long long)g.M * g.N;
+  mixed::HE u0 = Y.at(p);
+  float2 dn[6] = {D[p + P], D[p - P], D[p + M], D[p - M], D[p + 1], D[p - 1]};
+  mixed::HE ed[12] = {Y.at(p + P + M), Y.at(p + M + 1), Y.at(p + P + 1),  Y.at(p - P - M),
+                      Y.at(p - M - 1), Y.at(p - P - 1), Y.at(p + P - M),  Y.at(p + M - 1),
+                      Y.at(p + P - 1), Y.at(p - P + M), Y.at(p - M + 1),  Y.at(p - P + 1)};
+  return mixed::f_interior_2shoc<3>(c, u0, V[p], D[p], dn, ed);
+}
+
+// ---- 2SHOC shell, pass 2: F and the update within 2 cells of a face ---------
+template <int BC>
+__global__ void __launch_bounds__(256) shell_f(Geom g, Args A) {
+  const float2* Ein = A.stage == 1 ? A.a.lo_in : A.a.e_in;
+  mixed::YIn Y{A.a.hi_in, Ein};
+  const float2* D = A.a.dsh;
+  const long long total = shell_count(g, 2);
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    int x, y, z;
+    shell_coord(g, 2, t, x, y, z);
+    const long long p = lin(g, z, y, x);
+    float2 T;
+    if (is_interior(g, z, y, x)) {
+      T = f2shoc_dbuf(g, A.c, Y, A.a.V, D, z, y, x);
+    } else {
+      long long q = msd_neighbour(g, z, y, x);
+      mixed::HE ub = Y.at(p), uq = Y.at(q);
+      float2 fq = make_float2(0.f, 0.f);
+      if (BC == 2) {
+        int qi, qj, qk;
+        decompose(g, q, qi, qj, qk);
+        fq = f2shoc_dbuf(g, A.c, Y, A.a.V, D, qi, qj, qk);
+      }
+      T = mixed::f_boundary<2, BC>(A.c, ub, A.a.V[p], uq, fq, nullptr);
+    }
+    mixed::update(A.c, A.stage, p, T, A.a.hi_in, A.a.lo_in, A.a.e_in, A.a.K, A.a.e_out,
+                  A.a.hi_out, A.a.lo_out);
+  }
+}
+
+// ---- launch --------------------------------------------------------------------
+extern int g_zc_override;  // autotuner hook (0: chosen by default_zc)
+
+inline int sm_count() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+      n = 1;
+  }
+  return n;
+}
+
+// z chunk length.  CTAs of a stage all cost about (chunk + 2H) plane steps
+// (the chunk plus the queue fill), and the block scheduler hands them to SMs
+// as slots free up, so the stage takes about
+//   ceil(columns * chunks / SMs) * (ceil(L / chunks) + 2H)
+// plane steps; chunks are chosen to minimise that while giving every SM at
+// least `occ` resident CTAs.
+inline int default_zc(const Geom& g, int H, int occ) {
+  const long long cols = (long long)((g.M + 31) / 32) * ((g.N + 7) / 8);
+  const long long nsm = sm_count();
+  long long best_cost = -1;
+  int best = g.L;
+  for (int nbz = 1; nbz <= g.L; ++nbz) {
+    const int zc = (g.L + nbz - 1) / nbz;
+    if (nbz > 1 && zc == (g.L + nbz - 2) / (nbz - 1)) continue;  // same chunk length
+    if (zc < 4) break;
+    const long long ctas = cols * ((g.L + zc - 1) / zc);
+    long long cost = (ctas + nsm - 1) / nsm * (zc + 2 * H);
+    if (ctas < nsm * occ) cost = cost * 4;  // too few CTAs to hide latency
+    if (best_cost < 0 || cost < best_cost) {
+      best_cost = cost;
+      best = zc;
+    }
+  }
+  return best;
+}
+
+template <int METHOD, int STAGE, bool TMA>
+cudaError_t launch_deep(const Geom& g, const Args& A, cudaStream_t st, const CUtensorMap& m0,
+                        const CUtensorMap& m1) {
+  typedef WShape<METHOD> SH;
+  auto kern = wide3d<METHOD, STAGE, TMA>;
+  static int occ = 0;
+  if (!occ) {
+    cudaError_t e =
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SH::SMEM);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, SH::NT, SH::SMEM);
+    if (e != cudaSuccess || occ < 1) occ = 1;
+  }
+  const int zc = g_zc_override > 0 ? g_zc_override : default_zc(g, SH::H, occ);
+  dim3 grid((g.M + SH::TX - 1) / SH::TX, (g.N + SH::TY - 1) / SH::TY, (g.L + zc - 1) / zc);
+  kern<<<grid, dim3(SH::TX, SH::TY), SH::SMEM, st>>>(g, A, zc, m0, m1);
   return cudaGetLastError();
 }
 
-// z chunk length: enough CTAs for a few waves at 3 CTAs per SM, and chunks
-// long enough that the 2H-plane queue fill stays a small overhead.
-inline int default_zc(const Geom& g) {
-  long long xy = (long long)((g.M + 31) / 32) * ((g.N + 7) / 8);
-  long long want = 152LL * 9;
-  int zc = g.L;
-  if (xy < want) {
-    long long nz = (want + xy - 1) / xy;
-    zc = (int)((g.L + nz - 1) / nz);
+template <int METHOD, bool TMA>
+cudaError_t launch_deep_stage(const Geom& g, const Args& A, cudaStream_t st, const CUtensorMap& m0,
+                              const CUtensorMap& m1) {
+  switch (A.stage) {
+    case 1: return launch_deep<METHOD, 1, TMA>(g, A, st, m0, m1);
+    case 2: return launch_deep<METHOD, 2, TMA>(g, A, st, m0, m1);
+    case 3: return launch_deep<METHOD, 3, TMA>(g, A, st, m0, m1);
+    case 4: return launch_deep<METHOD, 4, TMA>(g, A, st, m0, m1);
   }
-  if (zc < 16) zc = 16;
-  if (zc > g.L) zc = g.L;
-  return zc;
+  return cudaErrorInvalidValue;
 }
 
-extern int g_zc_override;  // autotuner hook (0: default)
+inline unsigned shell_blocks(long long pts) {
+  long long b = (pts + 255) / 256;
+  const long long cap = (long long)sm_count() * 16;
+  return (unsigned)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
+// Number of kernel launches of one stage (deep + shell kernels).
+inline int launches_per_stage(int method, bool have_dsh) { return method == 2 && have_dsh ? 3 : 2; }
 
 template <int METHOD, int BC>
-cudaError_t launch(const Geom& g, const tiled::MixedPol::Args& A, cudaStream_t st) {
-  typedef WShape<METHOD, 32, 8> SH;
-  CUtensorMap m0, m1;
-  memset(&m0, 0, sizeof(m0));
-  memset(&m1, 0, sizeof(m1));
-  const void* ein = A.stage == 1 ? (const void*)A.a.lo_in : (const void*)A.a.e_in;
-  bool tma = tiled::make_map(&m0, A.a.hi_in, g, 1, SH::PX, SH::PY) &&
-             tiled::make_map(&m1, ein, g, 1, SH::PX, SH::PY);
-  int zc = g_zc_override > 0 ? g_zc_override : default_zc(g);
-  cudaError_t e = tma ? launch_k<METHOD, BC, true>(g, A, st, m0, m1, zc)
-                      : launch_k<METHOD, BC, false>(g, A, st, m0, m1, zc);
-  if (e != cudaSuccess) return e;
-  constexpr int H = METHOD == 2 ? 2 : 1;
-  long long shell = g.n - (long long)(g.M - 2 * H) * (g.N - 2 * H) * (g.L - 2 * H);
-  if (g.M <= 2 * H || g.N <= 2 * H || g.L <= 2 * H) shell = g.n;
-  if (shell <= 0) return cudaSuccess;
-  long long blocks = (shell + 255) / 256;
-  if (blocks > 152LL * 16) blocks = 152LL * 16;
-  shell3d<METHOD, BC><<<(unsigned)blocks, 256, 0, st>>>(g, A);
+cudaError_t launch(const Geom& g, const Args& A, cudaStream_t st) {
+  typedef WShape<METHOD> SH;
+  constexpr int H = SH::H;
+  const bool two_pass = METHOD == 2 && A.a.dsh != nullptr;
+  if (two_pass) {  // D on the shell first; it only reads the stage input
+    shell_d<BC><<<shell_blocks(shell_count(g, 3)), 256, 0, st>>>(g, A);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  if (!shell_thin(g, H)) {
+    CUtensorMap m0, m1;
+    memset(&m0, 0, sizeof(m0));
+    memset(&m1, 0, sizeof(m1));
+    const void* ein = A.stage == 1 ? (const void*)A.a.lo_in : (const void*)A.a.e_in;
+    bool tma = tiled::make_map(&m0, A.a.hi_in, g, 1, SH::PX, SH::PY) &&
+               tiled::make_map(&m1, ein, g, 1, SH::PX, SH::PY);
+    cudaError_t e = tma ? launch_deep_stage<METHOD, true>(g, A, st, m0, m1)
+                        : launch_deep_stage<METHOD, false>(g, A, st, m0, m1);
+    if (e != cudaSuccess) return e;
+  }
+  const unsigned nb = shell_blocks(shell_count(g, H));
+  if (two_pass)
+    shell_f<BC><<<nb, 256, 0, st>>>(g, A);
+  else
+    shell3d<METHOD, BC><<<nb, 256, 0, st>>>(g, A);
   return cudaGetLastError();
 }
 

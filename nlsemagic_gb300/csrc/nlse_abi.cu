@@ -237,7 +237,7 @@ struct nlse_solver {
   // exact precisions
   void *psi, *K, *ya, *yb, *V;
   // mixed precision
-  float2 *hi[2], *lo[2], *mK, *da, *db;
+  float2 *hi[2], *lo[2], *mK, *da, *db, *dsh;
   float* Vf;
   int cur;
   // device staging for planar transfers: re, im, V (n doubles each)
@@ -283,7 +283,7 @@ extern "C" int nlse_solver_destroy(nlse_solver* s) {
   if (s->stream) cudaStreamSynchronize(s->stream);
   free_graphs(s);
   void* ptrs[] = {s->psi, s->K, s->ya, s->yb, s->V, s->hi[0], s->hi[1], s->lo[0], s->lo[1],
-                  s->mK, s->da, s->db, s->Vf, s->stage, s->d_mass, s->d_bad};
+                  s->mK, s->da, s->db, s->dsh, s->Vf, s->stage, s->d_mass, s->d_bad};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -337,6 +337,8 @@ extern "C" int nlse_solver_create(const nlse_problem* p, nlse_solver** out) {
     if (!r) r = dalloc(s, (void**)&s->da, sizeof(float2) * n);
     if (!r) r = dalloc(s, (void**)&s->db, sizeof(float2) * n);
     if (!r) r = dalloc(s, (void**)&s->Vf, sizeof(float) * n);
+    if (!r && mixed_wants_shell_scratch(s->g, p->method, p->bc, s->kernel_kind))
+      r = dalloc(s, (void**)&s->dsh, sizeof(float2) * n);
   }
   if (!r) r = dalloc(s, (void**)&s->d_mass, sizeof(double));
   if (!r) r = dalloc(s, (void**)&s->d_bad, sizeof(int));
@@ -465,10 +467,12 @@ static int enqueue_step(nlse_solver* s) {
                                     s->kernel_kind);
   } else {
     int c = s->cur;
-    MixedStageArgs a1{s->hi[c], s->lo[c], nullptr, s->Vf, s->mK, s->da, nullptr, nullptr};
-    MixedStageArgs a2{s->hi[c], s->lo[c], s->da, s->Vf, s->mK, s->db, nullptr, nullptr};
-    MixedStageArgs a3{s->hi[c], s->lo[c], s->db, s->Vf, s->mK, s->da, nullptr, nullptr};
-    MixedStageArgs a4{s->hi[c], s->lo[c], s->da, s->Vf, s->mK, nullptr, s->hi[1 - c], s->lo[1 - c]};
+    float2* D = s->dsh;
+    MixedStageArgs a1{s->hi[c], s->lo[c], nullptr, s->Vf, s->mK, s->da, nullptr, nullptr, D};
+    MixedStageArgs a2{s->hi[c], s->lo[c], s->da, s->Vf, s->mK, s->db, nullptr, nullptr, D};
+    MixedStageArgs a3{s->hi[c], s->lo[c], s->db, s->Vf, s->mK, s->da, nullptr, nullptr, D};
+    MixedStageArgs a4{s->hi[c], s->lo[c], s->da, s->Vf, s->mK, nullptr, s->hi[1 - c], s->lo[1 - c],
+                      D};
     const MixedStageArgs* as[4] = {&a1, &a2, &a3, &a4};
     for (int st = 1; st <= 4 && e == cudaSuccess; ++st)
       e = launch_mixed_stage(s->g, p.method, p.bc, s->cf, *as[st - 1], st, s->stream,
@@ -551,10 +555,10 @@ extern "C" int nlse_solver_stream(nlse_solver* s, void** stream) {
 
 extern "C" int nlse_solver_launches_per_step(const nlse_solver* s) {
   if (!s) return 0;
-  // mixed-precision 3D grids on the tiled path: deep-point kernel + shell kernel per stage
-  bool two = s->prob.precision == NLSE_PREC_MIXED && s->kernel_kind == KERNEL_TILED &&
-             tiled_supported(s->g, s->g.ndim) && s->prob.bc != 4;
-  return two ? 8 : 4;
+  if (s->prob.precision != NLSE_PREC_MIXED) return 4;
+  // mixed-precision 3D grids on the tiled path: deep-point kernel + shell kernel(s) per stage
+  return 4 * mixed_stage_launches(s->g, s->prob.method, s->prob.bc, s->kernel_kind,
+                                  s->dsh != nullptr);
 }
 
 extern "C" long long nlse_solver_device_bytes(const nlse_solver* s) {

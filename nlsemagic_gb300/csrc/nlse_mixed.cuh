@@ -99,20 +99,21 @@ __device__ __forceinline__ float2 onesided_sum(const HE* os) {
 
 // MSD ratio, cross = 0 -> (u.w)/|w|^2, cross = 1 -> (u_i w_r - u_r w_i)/|w|^2.
 // |w|^2 of a small FP32 value would underflow, so w is first scaled by an
-// exact power of two that brings its larger component into [0.5, 1):
+// exact power of two 2^-e that brings its larger component into [0.5, 1):
 // (u.(s w)) / |s w|^2 * s, all in FP32 (no FP64 work on the boundary).
+// The scaling is applied with ldexpf on the values themselves: for a
+// subnormal w, e < -126 and the factor 2^-e alone is not representable.
 // A zero w gives 0/0 = NaN, as the unguarded reference does; callers apply
 // the zero-neighbour guard first.
 __device__ __forceinline__ float msd_ratio(float2 u, float2 w, int cross) {
   float m = fmaxf(fabsf(w.x), fabsf(w.y));
   int e = 0;
   frexpf(m, &e);
-  float sc = ldexpf(1.f, -e);
-  float wx = __fmul_rn(w.x, sc), wy = __fmul_rn(w.y, sc);
+  float wx = ldexpf(w.x, -e), wy = ldexpf(w.y, -e);
   float num = cross ? __fsub_rn(__fmul_rn(u.y, wx), __fmul_rn(u.x, wy))
                     : __fmaf_rn(u.x, wx, __fmul_rn(u.y, wy));
   float den = __fmaf_rn(wx, wx, __fmul_rn(wy, wy));
-  return __fmul_rn(__fdiv_rn(num, den), sc);
+  return ldexpf(__fdiv_rn(num, den), -e);
 }
 
 // ---- D at a boundary point -------------------------------------------------

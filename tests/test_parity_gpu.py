@@ -196,6 +196,28 @@ def test_mixed_all_boundary_codes(gpu_lib, ndim, method, BC):
     assert W.rel_l2(got, want) <= MIXED_TOL
 
 
+@pytest.mark.parametrize("ndim", [1, 2, 3])
+@pytest.mark.parametrize("method", [1, 2])
+def test_mixed_msd_subnormal_boundary(gpu_lib, ndim, method):
+    # A state that decays to FP32-subnormal magnitudes (~1e-40) at the faces
+    # and to FP32 zero at the corners, as a trapped condensate does where
+    # V > 1: the MSD ratio's exponent scaling must stay finite there.
+    n = {1: 120, 2: 40, 3: 20}[ndim]
+    h = 0.3
+    x = -n * h / 2 + h * np.arange(n)
+    grids = np.meshgrid(*([x] * ndim), indexing="ij")
+    r2 = sum(g * g for g in grids)
+    U = (np.exp(-92.0 * r2 / (n * h / 2) ** 2) * np.exp(0.2j * grids[0])).astype(complex)
+    V = 0.1 * r2 / r2.max()
+    k = 0.5 * W.linear_stability_k(ndim, method, h, 1.0)
+    args = (U, V, -1.0, 1.0, h * h, 2, 15, k, method)
+    want = orc(*args, 2)
+    for gather in (False, True):
+        got = gpu(*args, 3, gather=gather)
+        assert np.all(np.isfinite(got))
+        assert W.rel_l2(got, want) <= MIXED_TOL
+
+
 @pytest.mark.parametrize("shape", [(33, 5, 5), (4, 4, 30), (3, 40, 3), (36, 17, 9), (64, 40, 21),
                                    (5, 6, 7), (70, 9, 33)])
 @pytest.mark.parametrize("method", [1, 2])
