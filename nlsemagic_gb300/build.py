@@ -29,7 +29,6 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "--extended-lambda", "-Xcompiler", "
 UNITS = {
     "kern_exact.cu": ["-fmad=false"],
     "kern_mixed.cu": [],
-    "kern_stream3d.cu": [],
     "kern_util.cu": [],
     "nlse_abi.cu": [],
     "nlse_batch.cu": ["-fmad=false"],
@@ -61,14 +60,22 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     nv = nvcc()
     hdrs = _headers()
     units = [u for u in UNITS if os.path.exists(os.path.join(CSRC, u))]
+    # extra nvcc flags (e.g. -DNLSE_WIDE_MIN_BLOCKS=4); a change forces a rebuild
+    extra = os.environ.get("NLSE_NVCC_FLAGS", "").split()
+    stamp = os.path.join(BUILD, "flags.txt")
+    old_flags = open(stamp).read() if os.path.exists(stamp) else ""
+    if old_flags != " ".join(extra):
+        force = True
+        if os.path.exists(stamp):
+            os.remove(stamp)
     objs = []
 
     def compile_one(u):
         src = os.path.join(CSRC, u)
         obj = os.path.join(BUILD, u.replace(".cu", ".o"))
         if force or ptxas_info or _stale(obj, [src, __file__] + hdrs):
-            cmd = [nv] + ARCH + COMMON + UNITS[u] + (["-Xptxas", "-v"] if ptxas_info else []) + \
-                  ["-c", src, "-o", obj + ".tmp"]
+            cmd = [nv] + ARCH + COMMON + UNITS[u] + extra + \
+                  (["-Xptxas", "-v"] if ptxas_info else []) + ["-c", src, "-o", obj + ".tmp"]
             r = subprocess.run(cmd, capture_output=True, text=True)
             if r.returncode != 0:
                 raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (u, " ".join(cmd), r.stderr))
@@ -86,6 +93,8 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
         os.replace(tmp, LIB)
+    with open(stamp, "w") as f:
+        f.write(" ".join(extra))
     return LIB
 
 

@@ -13,6 +13,14 @@
 namespace nlse {
 
 __device__ __forceinline__ void decompose(const Geom& g, long long p, int& i, int& j, int& k) {
+  if (g.n <= 0x7fffffffLL) {  // 32-bit division (64-bit division is emulated)
+    const unsigned u = (unsigned)p, M = (unsigned)g.M, N = (unsigned)g.N;
+    const unsigned r = u / M;
+    k = (int)(u - r * M);
+    i = (int)(r / N);
+    j = (int)(r - (unsigned)i * N);
+    return;
+  }
   k = (int)(p % g.M);
   long long r = p / g.M;
   j = (int)(r % g.N);
@@ -97,7 +105,7 @@ __device__ C2<R> f_at(const Geom& g, const Consts<R>& c, const C2<R>* U, const R
   C2<R> fq = {0, 0};
   if (BC == 2) {
     int qi, qj, qk;
-    decompose(g, q, qi, qj, qk);
+    msd_coords(g, i, j, k, qi, qj, qk);
     fq = f_int<R, DIM, METHOD, BC>(g, c, U, V, qi, qj, qk);
   }
   return f_bnd<R, BC>(c, U[b], V[b], U[q], fq);
@@ -180,7 +188,7 @@ __device__ float2 d_at(const Geom& g, const Consts<float>& c, const YIn& Y, cons
   HE os[4];
   if (BC == 2) {
     int qi, qj, qk;
-    decompose(g, q, qi, qj, qk);
+    msd_coords(g, i, j, k, qi, qj, qk);
     dq = d_int<DIM>(g, c, Y, qi, qj, qk);
   }
   if (BC == 4) one_sided(g, Y, k, os);
@@ -262,7 +270,7 @@ __device__ float2 f_at(const Geom& g, const Consts<float>& c, const YIn& Y, cons
   HE os[4];
   if (BC == 2) {
     int qi, qj, qk;
-    decompose(g, q, qi, qj, qk);
+    msd_coords(g, i, j, k, qi, qj, qk);
     fq = f_int<DIM, METHOD, BC>(g, c, Y, V, qi, qj, qk);
   }
   if (BC == 4) one_sided(g, Y, k, os);

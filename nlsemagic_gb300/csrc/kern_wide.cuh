@@ -70,8 +70,13 @@ struct WShape {
   static constexpr unsigned TX_BYTES = (unsigned)(2 * PX * PY * 8);
 };
 
+// resident CTAs per SM the deep kernel is compiled for (register budget)
+#ifndef NLSE_WIDE_MIN_BLOCKS
+#define NLSE_WIDE_MIN_BLOCKS 3
+#endif
+
 template <int METHOD, int STAGE, bool TMA>
-__global__ void __launch_bounds__(256, 3) wide3d(Geom g, Args A, int zc,
+__global__ void __launch_bounds__(256, NLSE_WIDE_MIN_BLOCKS) wide3d(Geom g, Args A, int zc,
                                                  const __grid_constant__ CUtensorMap tm0,
                                                  const __grid_constant__ CUtensorMap tm1) {
   typedef WShape<METHOD> SH;
@@ -254,33 +259,72 @@ __host__ __device__ inline long long shell_count(const Geom& g, int W) {
   return g.n - (long long)(g.M - 2 * W) * (g.N - 2 * W) * (g.L - 2 * W);
 }
 
-__device__ __forceinline__ void shell_coord(const Geom& g, int W, long long t, int& x, int& y,
+// Host-built index map of the W-cell shell: t -> (x, y, z).  Counts below
+// 2^31 use 32-bit multiply-shift division (FastDiv); larger ones 64-bit.
+template <int W>
+struct ShellMap {
+  int M, N, L;
+  bool thin, idx32;
+  long long nz, ny, total;
+  FastDiv fMN, fM, fN2;
+  explicit ShellMap(const Geom& g) : M(g.M), N(g.N), L(g.L) {
+    thin = shell_thin(g, W);
+    total = shell_count(g, W);
+    nz = thin ? total : 2LL * W * g.M * g.N;
+    ny = thin ? 0 : (long long)(g.L - 2 * W) * 2 * W * g.M;
+    idx32 = g.n <= 0x7fffffffLL;
+    if (idx32) {
+      fMN = FastDiv((unsigned)(g.M * g.N));
+      fM = FastDiv((unsigned)g.M);
+      fN2 = FastDiv((unsigned)(thin ? 1 : g.N - 2 * W));
+    }
+  }
+};
+
+template <int W>
+__device__ __forceinline__ void shell_coord(const ShellMap<W>& s, long long t, int& x, int& y,
                                             int& z) {
-  const long long M = g.M, N = g.N, L = g.L;
-  if (shell_thin(g, W)) {
-    long long zz = t / (M * N), r = t - zz * M * N;
-    z = (int)zz;
-    y = (int)(r / M);
-    x = (int)(r - (long long)y * M);
+  const int M = s.M, N = s.N, L = s.L;
+  if (s.idx32) {
+    const unsigned u = (unsigned)t, MN = (unsigned)(M * N);
+    if (s.thin || t < s.nz) {
+      const unsigned pl = s.fMN.div(u), r = u - pl * MN;
+      z = s.thin || pl < (unsigned)W ? (int)pl : L - 2 * W + (int)pl;
+      y = (int)s.fM.div(r);
+      x = (int)(r - (unsigned)y * M);
+    } else if (t < s.nz + s.ny) {
+      const unsigned v = u - (unsigned)s.nz;
+      const unsigned row = s.fM.div(v);
+      x = (int)(v - row * M);
+      const unsigned zz = row / (2 * W), yr = row - zz * (2 * W);
+      z = W + (int)zz;
+      y = yr < (unsigned)W ? (int)yr : N - 2 * W + (int)yr;
+    } else {
+      const unsigned v = u - (unsigned)(s.nz + s.ny);
+      const unsigned row = v / (2 * W), xr = v - row * (2 * W);
+      const unsigned zz = s.fN2.div(row), yy = row - zz * (unsigned)(N - 2 * W);
+      z = W + (int)zz;
+      y = W + (int)yy;
+      x = xr < (unsigned)W ? (int)xr : M - 2 * W + (int)xr;
+    }
     return;
   }
-  const long long nz = 2 * W * M * N;                  // shell planes
-  const long long ny = (L - 2 * W) * 2 * W * M;        // shell rows of the other planes
-  if (t < nz) {
-    long long pl = t / (M * N), r = t - pl * M * N;
-    z = (int)(pl < W ? pl : L - 2 * W + pl);
-    y = (int)(r / M);
-    x = (int)(r - (long long)y * M);
-  } else if (t < nz + ny) {
-    long long u = t - nz;
-    long long row = u / M;
-    x = (int)(u - row * M);
+  const long long LM = M, LMN = (long long)M * N;
+  if (s.thin || t < s.nz) {
+    long long pl = t / LMN, r = t - pl * LMN;
+    z = (int)(s.thin || pl < W ? pl : L - 2 * W + pl);
+    y = (int)(r / LM);
+    x = (int)(r - (long long)y * LM);
+  } else if (t < s.nz + s.ny) {
+    long long v = t - s.nz;
+    long long row = v / LM;
+    x = (int)(v - row * LM);
     long long zz = row / (2 * W), yr = row - zz * 2 * W;
     z = (int)(W + zz);
     y = (int)(yr < W ? yr : N - 2 * W + yr);
   } else {
-    long long u = t - nz - ny;
-    long long row = u / (2 * W), xr = u - row * 2 * W;
+    long long v = t - s.nz - s.ny;
+    long long row = v / (2 * W), xr = v - row * 2 * W;
     long long zz = row / (N - 2 * W), yy = row - zz * (N - 2 * W);
     z = (int)(W + zz);
     y = (int)(W + yy);
@@ -290,15 +334,14 @@ __device__ __forceinline__ void shell_coord(const Geom& g, int W, long long t, i
 
 // ---- CD shell: gather form ---------------------------------------------------
 template <int METHOD, int BC>
-__global__ void __launch_bounds__(256) shell3d(Geom g, Args A) {
-  constexpr int H = METHOD == 2 ? 2 : 1;
+__global__ void __launch_bounds__(256) shell3d(Geom g, Args A,
+                                               const ShellMap<METHOD == 2 ? 2 : 1> sm) {
   const float2* Ein = A.stage == 1 ? A.a.lo_in : A.a.e_in;
   mixed::YIn Y{A.a.hi_in, Ein};
-  const long long total = shell_count(g, H);
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < sm.total;
        t += (long long)gridDim.x * blockDim.x) {
     int x, y, z;
-    shell_coord(g, H, t, x, y, z);
+    shell_coord(sm, t, x, y, z);
     long long p = lin(g, z, y, x);
     float2 T = mixed::f_at<3, METHOD, BC>(g, A.c, Y, A.a.V, z, y, x);
     mixed::update(A.c, A.stage, p, T, A.a.hi_in, A.a.lo_in, A.a.e_in, A.a.K, A.a.e_out,
@@ -308,15 +351,14 @@ __global__ void __launch_bounds__(256) shell3d(Geom g, Args A) {
 
 // ---- 2SHOC shell, pass 1: D within 3 cells of a face ------------------------
 template <int BC>
-__global__ void __launch_bounds__(256) shell_d(Geom g, Args A) {
+__global__ void __launch_bounds__(256) shell_d(Geom g, Args A, const ShellMap<3> sm) {
   const float2* Ein = A.stage == 1 ? A.a.lo_in : A.a.e_in;
   mixed::YIn Y{A.a.hi_in, Ein};
   float2* D = A.a.dsh;
-  const long long total = shell_count(g, 3);
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < sm.total;
        t += (long long)gridDim.x * blockDim.x) {
     int x, y, z;
-    shell_coord(g, 3, t, x, y, z);
+    shell_coord(sm, t, x, y, z);
     D[lin(g, z, y, x)] = mixed::d_at<3, BC>(g, A.c, Y, A.a.V, z, y, x);
   }
 }
@@ -338,28 +380,24 @@ __device__ __forceinline__ float2 f2shoc_dbuf(const Geom& g, const Consts<float>
 
 // ---- 2SHOC shell, pass 2: F and the update within 2 cells of a face ---------
 template <int BC>
-__global__ void __launch_bounds__(256) shell_f(Geom g, Args A) {
+__global__ void __launch_bounds__(256) shell_f(Geom g, Args A, const ShellMap<2> sm) {
   const float2* Ein = A.stage == 1 ? A.a.lo_in : A.a.e_in;
   mixed::YIn Y{A.a.hi_in, Ein};
   const float2* D = A.a.dsh;
-  const long long total = shell_count(g, 2);
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < sm.total;
        t += (long long)gridDim.x * blockDim.x) {
     int x, y, z;
-    shell_coord(g, 2, t, x, y, z);
+    shell_coord(sm, t, x, y, z);
     const long long p = lin(g, z, y, x);
     float2 T;
     if (is_interior(g, z, y, x)) {
       T = f2shoc_dbuf(g, A.c, Y, A.a.V, D, z, y, x);
     } else {
-      long long q = msd_neighbour(g, z, y, x);
-      mixed::HE ub = Y.at(p), uq = Y.at(q);
+      int qi, qj, qk;
+      msd_coords(g, z, y, x, qi, qj, qk);
+      mixed::HE ub = Y.at(p), uq = Y.at(lin(g, qi, qj, qk));
       float2 fq = make_float2(0.f, 0.f);
-      if (BC == 2) {
-        int qi, qj, qk;
-        decompose(g, q, qi, qj, qk);
-        fq = f2shoc_dbuf(g, A.c, Y, A.a.V, D, qi, qj, qk);
-      }
+      if (BC == 2) fq = f2shoc_dbuf(g, A.c, Y, A.a.V, D, qi, qj, qk);
       T = mixed::f_boundary<2, BC>(A.c, ub, A.a.V[p], uq, fq, nullptr);
     }
     mixed::update(A.c, A.stage, p, T, A.a.hi_in, A.a.lo_in, A.a.e_in, A.a.K, A.a.e_out,
@@ -453,7 +491,8 @@ cudaError_t launch(const Geom& g, const Args& A, cudaStream_t st) {
   constexpr int H = SH::H;
   const bool two_pass = METHOD == 2 && A.a.dsh != nullptr;
   if (two_pass) {  // D on the shell first; it only reads the stage input
-    shell_d<BC><<<shell_blocks(shell_count(g, 3)), 256, 0, st>>>(g, A);
+    const ShellMap<3> sm(g);
+    shell_d<BC><<<shell_blocks(sm.total), 256, 0, st>>>(g, A, sm);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
@@ -468,11 +507,12 @@ cudaError_t launch(const Geom& g, const Args& A, cudaStream_t st) {
                         : launch_deep_stage<METHOD, false>(g, A, st, m0, m1);
     if (e != cudaSuccess) return e;
   }
-  const unsigned nb = shell_blocks(shell_count(g, H));
+  const ShellMap<H> sm(g);
+  const unsigned nb = shell_blocks(sm.total);
   if (two_pass)
-    shell_f<BC><<<nb, 256, 0, st>>>(g, A);
+    shell_f<BC><<<nb, 256, 0, st>>>(g, A, ShellMap<2>(g));
   else
-    shell3d<METHOD, BC><<<nb, 256, 0, st>>>(g, A);
+    shell3d<METHOD, BC><<<nb, 256, 0, st>>>(g, A, sm);
   return cudaGetLastError();
 }
 

@@ -65,6 +65,27 @@ __host__ __device__ inline int clamp_in(int x, int n) {
 // coordinate moved one cell inward (the face / edge / corner rule of
 // src/NLSEmagic3D/NLSE3D_TAKE_STEPS_CD.c:103-166 and
 // src_old/NLSE2D_v1/NLSE2D_TAKE_STEPS_CD.c:81-127).
+__host__ __device__ inline void msd_coords(const Geom& g, int i, int j, int k, int& qi, int& qj,
+                                           int& qk) {
+  qk = clamp_in(k, g.M);
+  qj = g.ndim >= 2 ? clamp_in(j, g.N) : j;
+  qi = g.ndim >= 3 ? clamp_in(i, g.L) : i;
+}
+
+// Division of 32-bit n < 2^31 by a divisor fixed at launch, as a multiply-high
+// and a shift (Granlund & Montgomery, "Division by invariant integers using
+// multiplication", 1994): l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1,
+// n / d = (umulhi(n, m) + n) >> l.
+struct FastDiv {
+  unsigned d, m, l;
+  __host__ __device__ FastDiv() : d(1), m(1), l(0) {}
+  __host__ explicit FastDiv(unsigned dv) : d(dv ? dv : 1), m(1), l(0) {
+    while ((1ull << l) < d) ++l;
+    m = (unsigned)(((1ull << 32) * ((1ull << l) - d)) / d + 1);
+  }
+  __device__ __forceinline__ unsigned div(unsigned n) const { return (__umulhi(n, m) + n) >> l; }
+};
+
 __host__ __device__ inline long long msd_neighbour(const Geom& g, int i, int j, int k) {
   int qk = clamp_in(k, g.M);
   int qj = g.ndim >= 2 ? clamp_in(j, g.N) : j;
