@@ -37,16 +37,23 @@ static cudaError_t by_bc(const Geom& g, int BC, const Consts<float>& c, const Mi
   }
 }
 
-bool mixed_wants_shell_scratch(const Geom& g, int method, int BC, int kernel_kind) {
-  return kernel_kind == KERNEL_TILED && g.ndim == 3 && tiled_supported(g, 3) && BC != 4 &&
-         method == 2;
+static bool wide_path(const Geom& g, int BC, int kernel_kind) {
+  return kernel_kind == KERNEL_TILED && g.ndim == 3 && tiled_supported(g, 3) && BC != 4;
 }
 
-int mixed_stage_launches(const Geom& g, int method, int BC, int kernel_kind, bool have_dsh) {
-  if (!(kernel_kind == KERNEL_TILED && g.ndim == 3 && tiled_supported(g, 3) && BC != 4)) return 1;
-  const int H = method == 2 ? 2 : 1;
-  const int deep = wide::shell_thin(g, H) ? 0 : 1;
-  return deep + 1 + (method == 2 && have_dsh ? 1 : 0);
+int mixed_stage_launches(const Geom& g, int method, int BC, int kernel_kind) {
+  if (!wide_path(g, BC, kernel_kind)) return 1;
+  return method == 2 ? 3 : 2;  // (ghosts,) interior, faces
+}
+
+long long mixed_ghost_entries(const Geom& g, int method, int BC, int kernel_kind) {
+  if (!wide_path(g, BC, kernel_kind) || method != 2) return 0;
+  return wide::GhostLayout(g).total;
+}
+
+long long mixed_fq_entries(const Geom& g, int method, int BC, int kernel_kind) {
+  if (!wide_path(g, BC, kernel_kind) || method != 2 || BC != 2) return 0;
+  return g.n;
 }
 
 cudaError_t launch_mixed_stage(const Geom& g, int method, int BC, const Consts<float>& c,

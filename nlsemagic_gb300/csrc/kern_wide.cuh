@@ -1,17 +1,29 @@
 // Mixed-precision 3D stage kernels (FP32 stages, compensated hi/lo state).
 //
-// A stage is split by point class:
+// A stage is split by point class.
 //
-// deep points (every coordinate at least H cells from a face; H = 1 for CD,
-// 2 for 2SHOC) -- wide3d.  There the RK4 stage needs the stage input
-// Y = hi + E at the point, its 6 face neighbours and (2SHOC) the 6 points two
-// cells away along the axes: 2SHOC's compact operator reduces there to the
-// standard wide fourth-order Laplacian (nlse_mixed.cuh, f_wide_2shoc).  One
-// CTA owns a TX x TY column and streams through a chunk of z planes:
+// Interior points (every coordinate in [1, n-2]) -- wide3d.  Away from the
+// faces 2SHOC's compact operator equals the wide fourth-order Laplacian
+//   a/(12 h^2) (16 sum_f (Y_f - Y_0) - sum_2 (Y_2 - Y_0))
+// over the 6 face neighbours f and the 6 points 2 cells away (the edge terms
+// cancel; nlse_mixed.cuh, f_wide_2shoc), so D is never formed.  At a point
+// next to a face the compact operator uses the boundary-condition D of the
+// face point b instead of the interior D; it still equals the wide form if
+// the point one cell outside b holds the ghost value
+//   G = Y_b + h^2 D_bc(b) - (Y_q - Y_b) - sum_t (Y_t - Y_b),
+// q = b's inward neighbour, t = b's 4 in-face neighbours: the interior D
+// formula at b then yields D_bc(b), and the ghost enters the wide form and
+// the D's it replaces with opposite signs.  (Algebraic identity; checked in
+// FP64 against the compact form for BCs 1-3, edges and corners included.)
+// The ghosts are computed per stage by ghost3d into a small face array and
+// patched into the staged planes (x, y faces) or the register queue (z faces).
+//
+// One CTA owns a TX x TY column and streams through a chunk of z planes:
 //   - each plane (with a 2-cell x/y halo) is staged into a shared-memory ring
 //     by TMA (cp.async.bulk.tensor.3d, one elected thread, mbarrier per slot,
-//     issued P planes ahead of use), from which a thread reads the in-plane
-//     neighbours of its point;
+//     issued P planes ahead of use; planes -1 and L are out of range and
+//     zero-filled), from which a thread reads the in-plane neighbours of its
+//     point;
 //   - the z neighbours of a thread's own column are kept in registers, one
 //     entry per ring slot, so each plane value is read from shared memory
 //     once as a queue entry;
@@ -20,16 +32,9 @@
 // Every mbarrier wait is bounded (NLSE_ERR_TIMEOUT in the error word, copies
 // in flight drained, CTA returns).
 //
-// shell points (within H cells of a face) -- for CD one gather-form kernel
-// (shell3d, kern_gather.cuh functions); for 2SHOC two passes:
-//   shell_d: D = the CD2 Laplacian-plus-BC value at every point within 3
-//            cells of a face (the boundary-condition D on the faces),
-//            written to a scratch array;
-//   shell_f: F and the RK4 update at the shell points, the compact operator
-//            reading D from that array (and, for MSD faces, the inward
-//            neighbour's F from the same D values).
-// Each pass evaluates exactly the expressions of the gather form, so shell
-// results are the gather kernel's bit for bit.
+// Face points -- face2shoc (2SHOC: the boundary-condition F; for MSD from the
+// inward neighbour's F, which wide3d stores for the points next to a face)
+// or shell3d (CD: gather form).
 #pragma once
 
 #include "kern_gather.cuh"
@@ -70,15 +75,40 @@ struct WShape {
   static constexpr unsigned TX_BYTES = (unsigned)(2 * PX * PY * 8);
 };
 
-// resident CTAs per SM the deep kernel is compiled for (register budget)
+// Ghost array layout: one entry (hi, E as float4) per point of each face,
+// indexed by the two in-face coordinates; only face-interior entries (both
+// in-face coordinates in [1, n-2]) are used.
+struct GhostLayout {
+  long long xlo, xhi, ylo, yhi, zlo, zhi, total;  // x faces: y + N z; y: x + M z; z: x + M y
+  __host__ __device__ GhostLayout() : xlo(0), xhi(0), ylo(0), yhi(0), zlo(0), zhi(0), total(0) {}
+  __host__ explicit GhostLayout(const Geom& g) {
+    const long long M = g.M, N = g.N, L = g.L;
+    xlo = 0;
+    xhi = N * L;
+    ylo = 2 * N * L;
+    yhi = ylo + M * L;
+    zlo = yhi + M * L;
+    zhi = zlo + M * N;
+    total = zhi + M * N;
+  }
+};
+
+__device__ __forceinline__ mixed::HE he_of(float4 v) {
+  mixed::HE r;
+  r.h = make_float2(v.x, v.y);
+  r.e = make_float2(v.z, v.w);
+  return r;
+}
+
+// resident CTAs per SM the interior kernel is compiled for (register budget)
 #ifndef NLSE_WIDE_MIN_BLOCKS
-#define NLSE_WIDE_MIN_BLOCKS 3
+#define NLSE_WIDE_MIN_BLOCKS 4
 #endif
 
 template <int METHOD, int STAGE, bool TMA>
-__global__ void __launch_bounds__(256, NLSE_WIDE_MIN_BLOCKS) wide3d(Geom g, Args A, int zc,
-                                                 const __grid_constant__ CUtensorMap tm0,
-                                                 const __grid_constant__ CUtensorMap tm1) {
+__global__ void __launch_bounds__(256, NLSE_WIDE_MIN_BLOCKS) wide3d(
+    Geom g, Args A, int zc, GhostLayout gl, const __grid_constant__ CUtensorMap tm0,
+    const __grid_constant__ CUtensorMap tm1) {
   typedef WShape<METHOD> SH;
   typedef mixed::HE HE;
   constexpr int TX = SH::TX, TY = SH::TY, NT = SH::NT, H = SH::H, XO = SH::XO, PX = SH::PX,
@@ -91,13 +121,16 @@ __global__ void __launch_bounds__(256, NLSE_WIDE_MIN_BLOCKS) wide3d(Geom g, Args
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * zc;
   if (x0 >= M || y0 >= N || z0 >= L) return;
   const int z1 = z0 + zc < L ? z0 + zc : L;  // owned planes [z0, z1)
-  const int zs = z0 > H ? z0 : H;            // deep planes of this chunk: [zs, ze)
-  const int ze = z1 < L - H ? z1 : L - H;
+  const int zs = z0 > 1 ? z0 : 1;            // interior planes of this chunk: [zs, ze)
+  const int ze = z1 < L - 1 ? z1 : L - 1;
   if (zs >= ze) return;
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
   const int x = x0 + tx, y = y0 + ty;
-  const bool deep = x >= H && x <= M - 1 - H && y >= H && y <= N - 1 - H;
+  const bool inner = x >= 1 && x <= M - 2 && y >= 1 && y <= N - 2;
+  // 2SHOC CTAs whose column touches an x or y face patch ghosts into the halo
+  const bool edge = METHOD == 2 && (x0 == 0 || x0 + TX > M - 1 || y0 == 0 || y0 + TY > N - 1);
   const float2* Ein = STAGE == 1 ? A.a.lo_in : A.a.e_in;
+  const float4* GH = A.a.gh;
 
   if (TMA && (su32(smem) & 127u) != 0) {  // TMA destinations must be 128-byte aligned
     if (tid == 0) atomicExch(A.err, NLSE_ERR_STATE);
@@ -120,7 +153,7 @@ __global__ void __launch_bounds__(256, NLSE_WIDE_MIN_BLOCKS) wide3d(Geom g, Args
     if (zz > plast) return;
     if (TMA) {
       if (tid == 0) {
-        fence_proxy_async();  // earlier generic reads of the slot before the async write
+        fence_proxy_async();  // earlier generic accesses of the slot before the async write
         mbar_expect_tx(&bars[s], SH::TX_BYTES);
         tma_load_3d(hplane(s), &tm0, x0 - XO, y0 - H, zz, &bars[s]);
         tma_load_3d(eplane(s), &tm1, x0 - XO, y0 - H, zz, &bars[s]);
@@ -130,7 +163,7 @@ __global__ void __launch_bounds__(256, NLSE_WIDE_MIN_BLOCKS) wide3d(Geom g, Args
         int ux = t % PX, uy = t / PX;
         int gx = x0 - XO + ux, gy = y0 - H + uy;
         float2 h = make_float2(0.f, 0.f), e = h;
-        if (gx >= 0 && gx < M && gy >= 0 && gy < N) {
+        if (zz >= 0 && zz < L && gx >= 0 && gx < M && gy >= 0 && gy < N) {
           long long p = ((long long)zz * N + gy) * M + gx;
           h = A.a.hi_in[p];
           e = Ein[p];
@@ -150,10 +183,46 @@ __global__ void __launch_bounds__(256, NLSE_WIDE_MIN_BLOCKS) wide3d(Geom g, Args
   };
 
   const int own = (ty + H) * PX + tx + XO;
+  // this thread's column value of plane zz (slot s); outside a z face (2SHOC)
+  // the ghost value of the face point below / above
+  auto qload = [&](int zz, int s) -> HE {
+    if (METHOD == 2 && (zz < 0 || zz >= L)) {
+      HE r;
+      r.h = r.e = make_float2(0.f, 0.f);
+      if (inner) r = he_of(GH[(zz < 0 ? gl.zlo : gl.zhi) + x + (long long)M * y]);
+      return r;
+    }
+    HE r;
+    r.h = hplane(s)[own];
+    r.e = eplane(s)[own];
+    return r;
+  };
+  // write the x / y face ghosts of plane zz (slot s) into its halo cells
+  auto patch = [&](int zz, int s) {
+    if (METHOD != 2 || !edge || zz < 1 || zz > L - 2) return;
+    float2* hp = hplane(s);
+    float2* ep = eplane(s);
+    bool wrote = false;
+    auto put = [&](int i, float4 v) {
+      hp[i] = make_float2(v.x, v.y);
+      ep[i] = make_float2(v.z, v.w);
+      wrote = true;
+    };
+    if (y >= 1 && y <= N - 2) {
+      if (x == 0) put((ty + H) * PX + XO - 1, GH[gl.xlo + y + (long long)N * zz]);
+      if (x == M - 1) put((ty + H) * PX + tx + XO + 1, GH[gl.xhi + y + (long long)N * zz]);
+    }
+    if (x >= 1 && x <= M - 2) {
+      if (y == 0) put((H - 1) * PX + tx + XO, GH[gl.ylo + x + (long long)M * zz]);
+      if (y == N - 1) put((ty + H + 1) * PX + tx + XO, GH[gl.yhi + x + (long long)M * zz]);
+    }
+    if (TMA && wrote) fence_proxy_async();  // before a later TMA refill of the slot
+  };
+
   HE q[NU];  // q[s]: this thread's column value of the plane in slot s
 
   // ---- prologue: stage planes pfirst .. pfirst+2H+P-1 (slots 0..2H+P-1),
-  // queue planes pfirst .. pfirst+2H-1
+  // queue planes pfirst .. pfirst+2H-1, patch the first two centre planes
 #pragma unroll
   for (int t = 0; t < 2 * H + P; ++t) issue(pfirst + t, t);
   {
@@ -168,11 +237,10 @@ __global__ void __launch_bounds__(256, NLSE_WIDE_MIN_BLOCKS) wide3d(Geom g, Args
       return;
     }
 #pragma unroll
-    for (int t = 0; t < 2 * H; ++t) {
-      q[t].h = hplane(t)[own];
-      q[t].e = eplane(t)[own];
-    }
-    __syncthreads();  // slot 0 is refilled in the first iteration (2SHOC)
+    for (int t = 0; t < 2 * H; ++t) q[t] = qload(pfirst + t, t);
+#pragma unroll
+    for (int t = H; t < 2 * H; ++t) patch(pfirst + t, t);
+    __syncthreads();  // slot 0 is refilled in the first iteration (2SHOC); patches visible
   }
 
   const long long MN = (long long)M * N;
@@ -186,11 +254,11 @@ __global__ void __launch_bounds__(256, NLSE_WIDE_MIN_BLOCKS) wide3d(Geom g, Args
       const int sc = (u + H) % NU;      // slot of plane z
       const int sn = (u + 2 * H) % NU;  // slot of plane z+H (queue head)
       issue(z + H + P, (u + 2 * H + P) % NU);
-      // pointwise operands of the deep point, fetched before the wait
+      // pointwise operands of the interior point, fetched before the wait
       const long long p = (long long)z * MN + pxy;
       float v = 0.f;
       float2 lo = make_float2(0.f, 0.f), kv = lo;
-      if (deep) {
+      if (inner) {
         v = A.a.V[p];
         if (STAGE >= 2) lo = A.a.lo_in[p];
         if (STAGE == 4) kv = A.a.K[p];
@@ -204,10 +272,10 @@ __global__ void __launch_bounds__(256, NLSE_WIDE_MIN_BLOCKS) wide3d(Geom g, Args
         drain(z + H + P);
         return;
       }
-      q[sn].h = hplane(sn)[own];
-      q[sn].e = eplane(sn)[own];
+      q[sn] = qload(z + H, sn);
+      patch(z + H, sn);  // read two iterations on, after two barriers
 
-      if (deep) {
+      if (inner) {
         const float2* hp = hplane(sc);
         const float2* ep = eplane(sc);
         const HE& u0 = q[sc];
@@ -228,6 +296,9 @@ __global__ void __launch_bounds__(256, NLSE_WIDE_MIN_BLOCKS) wide3d(Geom g, Args
                        {hp[own + 2], ep[own + 2]},
                        {hp[own - 2], ep[own - 2]}};
           T = mixed::f_wide_2shoc<3>(A.c, u0, v, fn, f2n);
+          // F next to a face, for the MSD formula of the face points
+          if (A.a.fq && (x == 1 || x == M - 2 || y == 1 || y == N - 2 || z == 1 || z == L - 2))
+            A.a.fq[p] = T;
         }
         if (STAGE == 1) lo = u0.e;
         float2 eo, ko, ho, lo2;
@@ -332,10 +403,9 @@ __device__ __forceinline__ void shell_coord(const ShellMap<W>& s, long long t, i
   }
 }
 
-// ---- CD shell: gather form ---------------------------------------------------
+// ---- CD: face points in gather form ----------------------------------------
 template <int METHOD, int BC>
-__global__ void __launch_bounds__(256) shell3d(Geom g, Args A,
-                                               const ShellMap<METHOD == 2 ? 2 : 1> sm) {
+__global__ void __launch_bounds__(256) shell3d(Geom g, Args A, const ShellMap<1> sm) {
   const float2* Ein = A.stage == 1 ? A.a.lo_in : A.a.e_in;
   mixed::YIn Y{A.a.hi_in, Ein};
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < sm.total;
@@ -349,57 +419,76 @@ __global__ void __launch_bounds__(256) shell3d(Geom g, Args A,
   }
 }
 
-// ---- 2SHOC shell, pass 1: D within 3 cells of a face ------------------------
+// ---- 2SHOC: ghost values outside the faces ----------------------------------
+// For every face-interior point b (exactly one boundary coordinate):
+//   G = (h_b, E_b + delta),  delta = h^2 D_bc(b) - (Y_q - Y_b) - sum_t (Y_t - Y_b)
+// with D_bc the boundary-condition D of the compact scheme (mixed::d_boundary,
+// for MSD from the interior D at q).  Edge and corner points have no ghost.
 template <int BC>
-__global__ void __launch_bounds__(256) shell_d(Geom g, Args A, const ShellMap<3> sm) {
+__global__ void __launch_bounds__(256) ghost3d(Geom g, Args A, const ShellMap<1> sm,
+                                               GhostLayout gl) {
   const float2* Ein = A.stage == 1 ? A.a.lo_in : A.a.e_in;
   mixed::YIn Y{A.a.hi_in, Ein};
-  float2* D = A.a.dsh;
+  const int M = g.M, N = g.N, L = g.L;
+  const long long P = (long long)M * N;
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < sm.total;
        t += (long long)gridDim.x * blockDim.x) {
     int x, y, z;
     shell_coord(sm, t, x, y, z);
-    D[lin(g, z, y, x)] = mixed::d_at<3, BC>(g, A.c, Y, A.a.V, z, y, x);
+    const bool bx = x == 0 || x == M - 1, by = y == 0 || y == N - 1, bz = z == 0 || z == L - 1;
+    if ((int)bx + (int)by + (int)bz != 1) continue;
+    const long long pb = lin(g, z, y, x);
+    long long dn, t1, t2, gi;  // inward step, in-face steps, ghost index
+    if (bx) {
+      dn = x == 0 ? 1 : -1;
+      t1 = M;
+      t2 = P;
+      gi = (x == 0 ? gl.xlo : gl.xhi) + y + (long long)N * z;
+    } else if (by) {
+      dn = y == 0 ? M : -(long long)M;
+      t1 = 1;
+      t2 = P;
+      gi = (y == 0 ? gl.ylo : gl.yhi) + x + (long long)M * z;
+    } else {
+      dn = z == 0 ? P : -P;
+      t1 = 1;
+      t2 = M;
+      gi = (z == 0 ? gl.zlo : gl.zhi) + x + (long long)M * y;
+    }
+    const long long pq = pb + dn;
+    const mixed::HE ub = Y.at(pb), uq = Y.at(pq);
+    float2 dq = make_float2(0.f, 0.f);
+    if (BC == 2) {
+      mixed::HE nq[6] = {Y.at(pq + P), Y.at(pq - P), Y.at(pq + M),
+                         Y.at(pq - M), Y.at(pq + 1), Y.at(pq - 1)};
+      dq = mixed::d_interior<3>(A.c, uq, nq);
+    }
+    const float2 dbc = mixed::d_boundary<BC>(A.c, ub, A.a.V[pb], uq, A.a.V[pq], dq, nullptr);
+    mixed::HE tn[4] = {Y.at(pb + t1), Y.at(pb - t1), Y.at(pb + t2), Y.at(pb - t2)};
+    const float2 st = mixed::lapsum<4>(ub, tn);
+    const float2 sq = mixed::lapsum<1>(ub, &uq);
+    const float2 delta = mixed::psub(mixed::pmul(mixed::P2(A.c.h2), dbc), mixed::padd(sq, st));
+    const float2 ge = mixed::padd(ub.e, delta);
+    A.a.gh[gi] = make_float4(ub.h.x, ub.h.y, ge.x, ge.y);
   }
 }
 
-// compact 2SHOC F at an interior point (z, y, x) = (i, j, k) with the D
-// values taken from D[] (same operands, same order as mixed::f_int)
-__device__ __forceinline__ float2 f2shoc_dbuf(const Geom& g, const Consts<float>& c,
-                                              const mixed::YIn& Y, const float* V,
-                                              const float2* D, int i, int j, int k) {
-  const long long p = lin(g, i, j, k);
-  const long long M = g.M, P = (long long)g.M * g.N;
-  mixed::HE u0 = Y.at(p);
-  float2 dn[6] = {D[p + P], D[p - P], D[p + M], D[p - M], D[p + 1], D[p - 1]};
-  mixed::HE ed[12] = {Y.at(p + P + M), Y.at(p + M + 1), Y.at(p + P + 1),  Y.at(p - P - M),
-                      Y.at(p - M - 1), Y.at(p - P - 1), Y.at(p + P - M),  Y.at(p + M - 1),
-                      Y.at(p + P - 1), Y.at(p - P + M), Y.at(p - M + 1),  Y.at(p - P + 1)};
-  return mixed::f_interior_2shoc<3>(c, u0, V[p], D[p], dn, ed);
-}
-
-// ---- 2SHOC shell, pass 2: F and the update within 2 cells of a face ---------
+// ---- 2SHOC: face points ------------------------------------------------------
 template <int BC>
-__global__ void __launch_bounds__(256) shell_f(Geom g, Args A, const ShellMap<2> sm) {
+__global__ void __launch_bounds__(256) face2shoc(Geom g, Args A, const ShellMap<1> sm) {
   const float2* Ein = A.stage == 1 ? A.a.lo_in : A.a.e_in;
   mixed::YIn Y{A.a.hi_in, Ein};
-  const float2* D = A.a.dsh;
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < sm.total;
        t += (long long)gridDim.x * blockDim.x) {
     int x, y, z;
     shell_coord(sm, t, x, y, z);
     const long long p = lin(g, z, y, x);
-    float2 T;
-    if (is_interior(g, z, y, x)) {
-      T = f2shoc_dbuf(g, A.c, Y, A.a.V, D, z, y, x);
-    } else {
-      int qi, qj, qk;
-      msd_coords(g, z, y, x, qi, qj, qk);
-      mixed::HE ub = Y.at(p), uq = Y.at(lin(g, qi, qj, qk));
-      float2 fq = make_float2(0.f, 0.f);
-      if (BC == 2) fq = f2shoc_dbuf(g, A.c, Y, A.a.V, D, qi, qj, qk);
-      T = mixed::f_boundary<2, BC>(A.c, ub, A.a.V[p], uq, fq, nullptr);
-    }
+    int qi, qj, qk;
+    msd_coords(g, z, y, x, qi, qj, qk);
+    const long long q = lin(g, qi, qj, qk);
+    const mixed::HE ub = Y.at(p), uq = Y.at(q);
+    const float2 fq = BC == 2 ? A.a.fq[q] : make_float2(0.f, 0.f);
+    const float2 T = mixed::f_boundary<2, BC>(A.c, ub, A.a.V[p], uq, fq, nullptr);
     mixed::update(A.c, A.stage, p, T, A.a.hi_in, A.a.lo_in, A.a.e_in, A.a.K, A.a.e_out,
                   A.a.hi_out, A.a.lo_out);
   }
@@ -422,7 +511,7 @@ inline int sm_count() {
 // z chunk length.  CTAs of a stage all cost about (chunk + 2H) plane steps
 // (the chunk plus the queue fill), and the block scheduler hands them to SMs
 // as slots free up, so the stage takes about
-//   ceil(columns * chunks / SMs) * (ceil(L / chunks) + 2H)
+//   ceil(CTAs / SMs) * (ceil(L / chunks) + 2H)
 // plane steps; chunks are chosen to minimise that while giving every SM at
 // least `occ` resident CTAs.
 inline int default_zc(const Geom& g, int H, int occ) {
@@ -446,8 +535,8 @@ inline int default_zc(const Geom& g, int H, int occ) {
 }
 
 template <int METHOD, int STAGE, bool TMA>
-cudaError_t launch_deep(const Geom& g, const Args& A, cudaStream_t st, const CUtensorMap& m0,
-                        const CUtensorMap& m1) {
+cudaError_t launch_inner(const Geom& g, const Args& A, cudaStream_t st, const CUtensorMap& m0,
+                         const CUtensorMap& m1) {
   typedef WShape<METHOD> SH;
   auto kern = wide3d<METHOD, STAGE, TMA>;
   static int occ = 0;
@@ -460,59 +549,55 @@ cudaError_t launch_deep(const Geom& g, const Args& A, cudaStream_t st, const CUt
   }
   const int zc = g_zc_override > 0 ? g_zc_override : default_zc(g, SH::H, occ);
   dim3 grid((g.M + SH::TX - 1) / SH::TX, (g.N + SH::TY - 1) / SH::TY, (g.L + zc - 1) / zc);
-  kern<<<grid, dim3(SH::TX, SH::TY), SH::SMEM, st>>>(g, A, zc, m0, m1);
+  kern<<<grid, dim3(SH::TX, SH::TY), SH::SMEM, st>>>(g, A, zc, GhostLayout(g), m0, m1);
   return cudaGetLastError();
 }
 
 template <int METHOD, bool TMA>
-cudaError_t launch_deep_stage(const Geom& g, const Args& A, cudaStream_t st, const CUtensorMap& m0,
-                              const CUtensorMap& m1) {
+cudaError_t launch_inner_stage(const Geom& g, const Args& A, cudaStream_t st,
+                               const CUtensorMap& m0, const CUtensorMap& m1) {
   switch (A.stage) {
-    case 1: return launch_deep<METHOD, 1, TMA>(g, A, st, m0, m1);
-    case 2: return launch_deep<METHOD, 2, TMA>(g, A, st, m0, m1);
-    case 3: return launch_deep<METHOD, 3, TMA>(g, A, st, m0, m1);
-    case 4: return launch_deep<METHOD, 4, TMA>(g, A, st, m0, m1);
+    case 1: return launch_inner<METHOD, 1, TMA>(g, A, st, m0, m1);
+    case 2: return launch_inner<METHOD, 2, TMA>(g, A, st, m0, m1);
+    case 3: return launch_inner<METHOD, 3, TMA>(g, A, st, m0, m1);
+    case 4: return launch_inner<METHOD, 4, TMA>(g, A, st, m0, m1);
   }
   return cudaErrorInvalidValue;
 }
 
-inline unsigned shell_blocks(long long pts) {
+inline unsigned face_blocks(long long pts) {
   long long b = (pts + 255) / 256;
   const long long cap = (long long)sm_count() * 16;
   return (unsigned)(b < 1 ? 1 : (b > cap ? cap : b));
 }
 
-// Number of kernel launches of one stage (deep + shell kernels).
-inline int launches_per_stage(int method, bool have_dsh) { return method == 2 && have_dsh ? 3 : 2; }
-
+// 3D grids, every dimension >= 3.  2SHOC needs A.a.gh (and A.a.fq for MSD).
 template <int METHOD, int BC>
 cudaError_t launch(const Geom& g, const Args& A, cudaStream_t st) {
   typedef WShape<METHOD> SH;
-  constexpr int H = SH::H;
-  const bool two_pass = METHOD == 2 && A.a.dsh != nullptr;
-  if (two_pass) {  // D on the shell first; it only reads the stage input
-    const ShellMap<3> sm(g);
-    shell_d<BC><<<shell_blocks(sm.total), 256, 0, st>>>(g, A, sm);
+  const ShellMap<1> faces(g);
+  const unsigned nb = face_blocks(faces.total);
+  if (METHOD == 2) {
+    if (!A.a.gh || (BC == 2 && !A.a.fq)) return cudaErrorInvalidValue;
+    ghost3d<BC><<<nb, 256, 0, st>>>(g, A, faces, GhostLayout(g));
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
-  if (!shell_thin(g, H)) {
+  {
     CUtensorMap m0, m1;
     memset(&m0, 0, sizeof(m0));
     memset(&m1, 0, sizeof(m1));
     const void* ein = A.stage == 1 ? (const void*)A.a.lo_in : (const void*)A.a.e_in;
     bool tma = tiled::make_map(&m0, A.a.hi_in, g, 1, SH::PX, SH::PY) &&
                tiled::make_map(&m1, ein, g, 1, SH::PX, SH::PY);
-    cudaError_t e = tma ? launch_deep_stage<METHOD, true>(g, A, st, m0, m1)
-                        : launch_deep_stage<METHOD, false>(g, A, st, m0, m1);
+    cudaError_t e = tma ? launch_inner_stage<METHOD, true>(g, A, st, m0, m1)
+                        : launch_inner_stage<METHOD, false>(g, A, st, m0, m1);
     if (e != cudaSuccess) return e;
   }
-  const ShellMap<H> sm(g);
-  const unsigned nb = shell_blocks(sm.total);
-  if (two_pass)
-    shell_f<BC><<<nb, 256, 0, st>>>(g, A, ShellMap<2>(g));
+  if (METHOD == 2)
+    face2shoc<BC><<<nb, 256, 0, st>>>(g, A, faces);
   else
-    shell3d<METHOD, BC><<<nb, 256, 0, st>>>(g, A, sm);
+    shell3d<METHOD, BC><<<nb, 256, 0, st>>>(g, A, faces);
   return cudaGetLastError();
 }
 

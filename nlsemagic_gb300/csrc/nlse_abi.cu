@@ -161,6 +161,7 @@ static Consts<double> consts_double(const nlse_problem* p) {
   c.kinv = 1.0 / k;
   c.kinv2 = 2.0 / k;
   c.a12lh2 = a / (12.0 * h2);
+  c.h2 = h2;
   c.msd_guard = (p->flags & NLSE_FLAG_MSD_GUARD) ? 1 : 0;
   return c;
 }
@@ -190,6 +191,7 @@ static Consts<float> consts_single(const nlse_problem* p) {
   c.k6 = k / 6.0f;
   c.kinv = 1.0f / k;
   c.kinv2 = 2.0f / k;
+  c.h2 = h2;
   c.msd_guard = (p->flags & NLSE_FLAG_MSD_GUARD) ? 1 : 0;
   return c;
 }
@@ -214,6 +216,7 @@ static Consts<float> consts_mixed(const nlse_problem* p) {
   c.kinv = (float)d.kinv;
   c.kinv2 = (float)d.kinv2;
   c.a12lh2 = (float)d.a12lh2;
+  c.h2 = (float)d.h2;
   c.msd_guard = d.msd_guard;
   return c;
 }
@@ -237,7 +240,8 @@ struct nlse_solver {
   // exact precisions
   void *psi, *K, *ya, *yb, *V;
   // mixed precision
-  float2 *hi[2], *lo[2], *mK, *da, *db, *dsh;
+  float2 *hi[2], *lo[2], *mK, *da, *db, *fq;
+  float4* gh;
   float* Vf;
   int cur;
   // device staging for planar transfers: re, im, V (n doubles each)
@@ -283,7 +287,7 @@ extern "C" int nlse_solver_destroy(nlse_solver* s) {
   if (s->stream) cudaStreamSynchronize(s->stream);
   free_graphs(s);
   void* ptrs[] = {s->psi, s->K, s->ya, s->yb, s->V, s->hi[0], s->hi[1], s->lo[0], s->lo[1],
-                  s->mK, s->da, s->db, s->dsh, s->Vf, s->stage, s->d_mass, s->d_bad};
+                  s->mK, s->da, s->db, s->fq, s->gh, s->Vf, s->stage, s->d_mass, s->d_bad};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -337,8 +341,10 @@ extern "C" int nlse_solver_create(const nlse_problem* p, nlse_solver** out) {
     if (!r) r = dalloc(s, (void**)&s->da, sizeof(float2) * n);
     if (!r) r = dalloc(s, (void**)&s->db, sizeof(float2) * n);
     if (!r) r = dalloc(s, (void**)&s->Vf, sizeof(float) * n);
-    if (!r && mixed_wants_shell_scratch(s->g, p->method, p->bc, s->kernel_kind))
-      r = dalloc(s, (void**)&s->dsh, sizeof(float2) * n);
+    const long long ng = mixed_ghost_entries(s->g, p->method, p->bc, s->kernel_kind);
+    const long long nf = mixed_fq_entries(s->g, p->method, p->bc, s->kernel_kind);
+    if (!r && ng) r = dalloc(s, (void**)&s->gh, sizeof(float4) * ng);
+    if (!r && nf) r = dalloc(s, (void**)&s->fq, sizeof(float2) * nf);
   }
   if (!r) r = dalloc(s, (void**)&s->d_mass, sizeof(double));
   if (!r) r = dalloc(s, (void**)&s->d_bad, sizeof(int));
@@ -467,12 +473,13 @@ static int enqueue_step(nlse_solver* s) {
                                     s->kernel_kind);
   } else {
     int c = s->cur;
-    float2* D = s->dsh;
-    MixedStageArgs a1{s->hi[c], s->lo[c], nullptr, s->Vf, s->mK, s->da, nullptr, nullptr, D};
-    MixedStageArgs a2{s->hi[c], s->lo[c], s->da, s->Vf, s->mK, s->db, nullptr, nullptr, D};
-    MixedStageArgs a3{s->hi[c], s->lo[c], s->db, s->Vf, s->mK, s->da, nullptr, nullptr, D};
+    float4* G = s->gh;
+    float2* F = s->fq;
+    MixedStageArgs a1{s->hi[c], s->lo[c], nullptr, s->Vf, s->mK, s->da, nullptr, nullptr, G, F};
+    MixedStageArgs a2{s->hi[c], s->lo[c], s->da, s->Vf, s->mK, s->db, nullptr, nullptr, G, F};
+    MixedStageArgs a3{s->hi[c], s->lo[c], s->db, s->Vf, s->mK, s->da, nullptr, nullptr, G, F};
     MixedStageArgs a4{s->hi[c], s->lo[c], s->da, s->Vf, s->mK, nullptr, s->hi[1 - c], s->lo[1 - c],
-                      D};
+                      G, F};
     const MixedStageArgs* as[4] = {&a1, &a2, &a3, &a4};
     for (int st = 1; st <= 4 && e == cudaSuccess; ++st)
       e = launch_mixed_stage(s->g, p.method, p.bc, s->cf, *as[st - 1], st, s->stream,
@@ -557,8 +564,7 @@ extern "C" int nlse_solver_launches_per_step(const nlse_solver* s) {
   if (!s) return 0;
   if (s->prob.precision != NLSE_PREC_MIXED) return 4;
   // mixed-precision 3D grids on the tiled path: deep-point kernel + shell kernel(s) per stage
-  return 4 * mixed_stage_launches(s->g, s->prob.method, s->prob.bc, s->kernel_kind,
-                                  s->dsh != nullptr);
+  return 4 * mixed_stage_launches(s->g, s->prob.method, s->prob.bc, s->kernel_kind);
 }
 
 extern "C" long long nlse_solver_device_bytes(const nlse_solver* s) {

@@ -35,6 +35,7 @@ struct Consts {
   R k, k2, k6;         // k, k/2, k/6
   R kinv, kinv2;       // 1/k, 2/k (mixed path only)
   R a12lh2;            // a/(12 h2) (mixed path, wide fourth-order form)
+  R h2;                // h^2 (mixed path, 2SHOC ghost values)
   int msd_guard;       // MSD zero-neighbour guard
 };
 

@@ -28,7 +28,9 @@ struct MixedStageArgs {
   float2* e_out;      // next stage input E
   float2* hi_out;      // stage 4 output (a different buffer from hi_in)
   float2* lo_out;
-  float2* dsh;         // scratch for D on the shell of 3D 2SHOC grids (n points), or null
+  // 3D 2SHOC on the tiled path (null otherwise):
+  float4* gh;          // ghost values (hi, E) one cell outside each face, mixed_ghost_entries()
+  float2* fq;          // F at the points next to a face (n entries, MSD only)
 };
 
 template <typename R>
@@ -40,10 +42,12 @@ cudaError_t launch_mixed_stage(const Geom& g, int method, int BC, const Consts<f
                                const MixedStageArgs& a, int stage, cudaStream_t st,
                                int kernel_kind);
 
-// Kernel launches one mixed stage issues (launch_mixed_stage), and whether
-// the tiled 3D path wants the shell scratch array MixedStageArgs::dsh.
-int mixed_stage_launches(const Geom& g, int method, int BC, int kernel_kind, bool have_dsh);
-bool mixed_wants_shell_scratch(const Geom& g, int method, int BC, int kernel_kind);
+// Kernel launches one mixed stage issues (launch_mixed_stage), and the
+// scratch the tiled 3D 2SHOC path needs: ghost entries (float4) and F
+// entries (float2) for MixedStageArgs::gh / ::fq (0 when not needed).
+int mixed_stage_launches(const Geom& g, int method, int BC, int kernel_kind);
+long long mixed_ghost_entries(const Geom& g, int method, int BC, int kernel_kind);
+long long mixed_fq_entries(const Geom& g, int method, int BC, int kernel_kind);
 
 // Layout conversions and reductions (kern_util.cu).
 cudaError_t planar_to_c2d(const double* re, const double* im, C2<double>* out, long long n,
