@@ -542,7 +542,15 @@ def main():
     ap.add_argument("--serve-max3d", type=int, default=128)
     ap.add_argument("--serve-max-steps", type=int, default=2000)
     ap.add_argument("--serve-pool-gb", type=int, default=64)
+    ap.add_argument("--only", choices=["batched", "serving"], default=None,
+                    help="run one auxiliary section alone and print its JSON (for profiling)")
     args = ap.parse_args()
+    if args.only:
+        import nlsemagic_gb300 as ng
+        ng.load()
+        out = run_batched(args) if args.only == "batched" else run_serving(args)
+        print(json.dumps({"section": args.only, **out}), flush=True)
+        return
     from nlsemagic_gb300 import workloads as W
     rank, world, _ = dist_env()
     w = W.vortex_rings_3d(seed=1002 + rank, n=args.grid, method=2, steps=args.rk4_steps)

@@ -615,8 +615,12 @@ static bool same_scalars(const nlse_problem& a, const nlse_problem& b) {
          a.k == b.k && a.flags == b.flags;
 }
 
+// Same device buffers: grid, precision, and what the stage kernels allocate
+// scratch for (method, boundary code, kernel kind).
 static bool same_layout(const nlse_problem& a, const nlse_problem& b) {
-  if (a.ndim != b.ndim || a.precision != b.precision) return false;
+  if (a.ndim != b.ndim || a.precision != b.precision || a.method != b.method || a.bc != b.bc ||
+      (a.flags & NLSE_FLAG_GATHER) != (b.flags & NLSE_FLAG_GATHER))
+    return false;
   for (int d = 0; d < a.ndim; ++d)
     if (a.dims[d] != b.dims[d]) return false;
   return true;
