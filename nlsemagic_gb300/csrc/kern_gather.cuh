@@ -111,6 +111,46 @@ __device__ C2<R> f_at(const Geom& g, const Consts<R>& c, const C2<R>* U, const R
   return f_bnd<R, BC>(c, U[b], V[b], U[q], fq);
 }
 
+// 2SHOC F with the stage's D values read from D[] (filled by d_at for every
+// point of the grid) instead of recomputed: the same operands in the same
+// order as f_int / f_at, hence the same bits.
+template <typename R, int DIM, int BC>
+__device__ C2<R> f_int_d(const Geom& g, const Consts<R>& c, const C2<R>* U, const R* V,
+                         const C2<R>* D, int i, int j, int k) {
+  long long p = lin(g, i, j, k);
+  const long long M = g.M, P = g.P;
+  if (DIM == 1) return f_2shoc_1d<R>(c, U[p], V[p], D[p], D[p + 1], D[p - 1]);
+  if (DIM == 2) {
+    C2<R> dn[4] = {D[p + M], D[p - M], D[p + 1], D[p - 1]};
+    C2<R> dg[4] = {U[p + M + 1], U[p + M - 1], U[p - M + 1], U[p - M - 1]};
+    return f_2shoc_2d<R>(c, U[p], V[p], D[p], dn, dg);
+  }
+  C2<R> dn[6] = {D[p + P], D[p - P], D[p + M], D[p - M], D[p + 1], D[p - 1]};
+  C2<R> e[12] = {U[p + P + M], U[p + M + 1], U[p + P + 1], U[p - P - M], U[p - M - 1], U[p - P - 1],
+                 U[p + P - M], U[p + M - 1], U[p + P - 1], U[p - P + M], U[p - M + 1], U[p - P + 1]};
+  return f_2shoc_3d<R>(c, U[p], V[p], D[p], dn, e);
+}
+
+template <typename R, int DIM, int BC>
+__device__ C2<R> f_at_d(const Geom& g, const Consts<R>& c, const C2<R>* U, const R* V,
+                        const C2<R>* D, int i, int j, int k) {
+  if (is_interior(g, i, j, k)) return f_int_d<R, DIM, BC>(g, c, U, V, D, i, j, k);
+  long long b = lin(g, i, j, k);
+  if (BC == 4) {
+    const long long N = g.M;
+    if (b == 0) return f_onesided<R, 2>(c, U[0], V[0], U[3], U[2], U[1], U[0]);
+    return f_onesided<R, 2>(c, U[N - 1], V[N - 1], U[N - 4], U[N - 3], U[N - 2], U[N - 1]);
+  }
+  long long q = msd_neighbour(g, i, j, k);
+  C2<R> fq = {0, 0};
+  if (BC == 2) {
+    int qi, qj, qk;
+    msd_coords(g, i, j, k, qi, qj, qk);
+    fq = f_int_d<R, DIM, BC>(g, c, U, V, D, qi, qj, qk);
+  }
+  return f_bnd<R, BC>(c, U[b], V[b], U[q], fq);
+}
+
 template <typename R, int DIM, int METHOD, int BC>
 __global__ void __launch_bounds__(256) gather_stage(Geom g, Consts<R> c,
                                                     const C2<R>* __restrict__ Yin,
@@ -275,6 +315,68 @@ __device__ float2 f_at(const Geom& g, const Consts<float>& c, const YIn& Y, cons
   }
   if (BC == 4) one_sided(g, Y, k, os);
   return f_boundary<METHOD, BC>(c, ub, V[b], uq, fq, os);
+}
+
+// 2SHOC F with the stage's D values read from D[] (see exact::f_int_d).
+template <int DIM, int BC>
+__device__ float2 f_int_d(const Geom& g, const Consts<float>& c, const YIn& Y, const float* V,
+                          const float2* D, int i, int j, int k) {
+  long long p = lin(g, i, j, k);
+  const long long M = g.M, P = (long long)g.M * g.N;
+  HE u0 = Y.at(p);
+  float2 dn[6];
+  HE ed[12];
+  if (DIM == 1) {
+    dn[0] = D[p + 1];
+    dn[1] = D[p - 1];
+  } else if (DIM == 2) {
+    dn[0] = D[p + M];
+    dn[1] = D[p - M];
+    dn[2] = D[p + 1];
+    dn[3] = D[p - 1];
+    ed[0] = Y.at(p + M + 1);
+    ed[1] = Y.at(p + M - 1);
+    ed[2] = Y.at(p - M + 1);
+    ed[3] = Y.at(p - M - 1);
+  } else {
+    dn[0] = D[p + P];
+    dn[1] = D[p - P];
+    dn[2] = D[p + M];
+    dn[3] = D[p - M];
+    dn[4] = D[p + 1];
+    dn[5] = D[p - 1];
+    ed[0] = Y.at(p + P + M);
+    ed[1] = Y.at(p + M + 1);
+    ed[2] = Y.at(p + P + 1);
+    ed[3] = Y.at(p - P - M);
+    ed[4] = Y.at(p - M - 1);
+    ed[5] = Y.at(p - P - 1);
+    ed[6] = Y.at(p + P - M);
+    ed[7] = Y.at(p + M - 1);
+    ed[8] = Y.at(p + P - 1);
+    ed[9] = Y.at(p - P + M);
+    ed[10] = Y.at(p - M + 1);
+    ed[11] = Y.at(p - P + 1);
+  }
+  return f_interior_2shoc<DIM>(c, u0, V[p], D[p], dn, ed);
+}
+
+template <int DIM, int BC>
+__device__ float2 f_at_d(const Geom& g, const Consts<float>& c, const YIn& Y, const float* V,
+                         const float2* D, int i, int j, int k) {
+  if (is_interior(g, i, j, k)) return f_int_d<DIM, BC>(g, c, Y, V, D, i, j, k);
+  long long b = lin(g, i, j, k);
+  long long q = msd_neighbour(g, i, j, k);
+  HE ub = Y.at(b), uq = Y.at(q);
+  float2 fq = make_float2(0.f, 0.f);
+  HE os[4];
+  if (BC == 2) {
+    int qi, qj, qk;
+    msd_coords(g, i, j, k, qi, qj, qk);
+    fq = f_int_d<DIM, BC>(g, c, Y, V, D, qi, qj, qk);
+  }
+  if (BC == 4) one_sided(g, Y, k, os);
+  return f_boundary<2, BC>(c, ub, V[b], uq, fq, os);
 }
 
 // Mixed RK4 stage update at point p (E format, see nlse_mixed.cuh).

@@ -15,8 +15,9 @@
 // formula at b then yields D_bc(b), and the ghost enters the wide form and
 // the D's it replaces with opposite signs.  (Algebraic identity; checked in
 // FP64 against the compact form for BCs 1-3, edges and corners included.)
-// The ghosts are computed per stage by ghost3d into a small face array and
-// patched into the staged planes (x, y faces) or the register queue (z faces).
+// The ghosts are computed per stage by ghost3d into a small face array; a
+// point next to a face takes its +-2 neighbour across that face from there
+// (x, y faces) or its register queue holds it (z faces).
 //
 // One CTA owns a TX x TY column and streams through a chunk of z planes:
 //   - each plane (with a 2-cell x/y halo) is staged into a shared-memory ring
@@ -127,8 +128,9 @@ __global__ void __launch_bounds__(256, NLSE_WIDE_MIN_BLOCKS) wide3d(
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
   const int x = x0 + tx, y = y0 + ty;
   const bool inner = x >= 1 && x <= M - 2 && y >= 1 && y <= N - 2;
-  // 2SHOC CTAs whose column touches an x or y face patch ghosts into the halo
-  const bool edge = METHOD == 2 && (x0 == 0 || x0 + TX > M - 1 || y0 == 0 || y0 + TY > N - 1);
+  // 2SHOC: threads next to an x / y face take their +-2 neighbour across
+  // that face from the ghost array (CTA-uniform pre-check)
+  const bool edge = METHOD == 2 && (x0 == 0 || x0 + TX > M - 2 || y0 == 0 || y0 + TY > N - 2);
   const float2* Ein = STAGE == 1 ? A.a.lo_in : A.a.e_in;
   const float4* GH = A.a.gh;
 
@@ -197,32 +199,10 @@ __global__ void __launch_bounds__(256, NLSE_WIDE_MIN_BLOCKS) wide3d(
     r.e = eplane(s)[own];
     return r;
   };
-  // write the x / y face ghosts of plane zz (slot s) into its halo cells
-  auto patch = [&](int zz, int s) {
-    if (METHOD != 2 || !edge || zz < 1 || zz > L - 2) return;
-    float2* hp = hplane(s);
-    float2* ep = eplane(s);
-    bool wrote = false;
-    auto put = [&](int i, float4 v) {
-      hp[i] = make_float2(v.x, v.y);
-      ep[i] = make_float2(v.z, v.w);
-      wrote = true;
-    };
-    if (y >= 1 && y <= N - 2) {
-      if (x == 0) put((ty + H) * PX + XO - 1, GH[gl.xlo + y + (long long)N * zz]);
-      if (x == M - 1) put((ty + H) * PX + tx + XO + 1, GH[gl.xhi + y + (long long)N * zz]);
-    }
-    if (x >= 1 && x <= M - 2) {
-      if (y == 0) put((H - 1) * PX + tx + XO, GH[gl.ylo + x + (long long)M * zz]);
-      if (y == N - 1) put((ty + H + 1) * PX + tx + XO, GH[gl.yhi + x + (long long)M * zz]);
-    }
-    if (TMA && wrote) fence_proxy_async();  // before a later TMA refill of the slot
-  };
-
   HE q[NU];  // q[s]: this thread's column value of the plane in slot s
 
   // ---- prologue: stage planes pfirst .. pfirst+2H+P-1 (slots 0..2H+P-1),
-  // queue planes pfirst .. pfirst+2H-1, patch the first two centre planes
+  // queue planes pfirst .. pfirst+2H-1
 #pragma unroll
   for (int t = 0; t < 2 * H + P; ++t) issue(pfirst + t, t);
   {
@@ -238,9 +218,7 @@ __global__ void __launch_bounds__(256, NLSE_WIDE_MIN_BLOCKS) wide3d(
     }
 #pragma unroll
     for (int t = 0; t < 2 * H; ++t) q[t] = qload(pfirst + t, t);
-#pragma unroll
-    for (int t = H; t < 2 * H; ++t) patch(pfirst + t, t);
-    __syncthreads();  // slot 0 is refilled in the first iteration (2SHOC); patches visible
+    __syncthreads();  // slot 0 is refilled in the first iteration (2SHOC)
   }
 
   const long long MN = (long long)M * N;
@@ -258,10 +236,17 @@ __global__ void __launch_bounds__(256, NLSE_WIDE_MIN_BLOCKS) wide3d(
       const long long p = (long long)z * MN + pxy;
       float v = 0.f;
       float2 lo = make_float2(0.f, 0.f), kv = lo;
+      float4 gxl, gxh, gyl, gyh;  // ghosts across the x / y faces (2SHOC, next to a face)
       if (inner) {
         v = A.a.V[p];
         if (STAGE >= 2) lo = A.a.lo_in[p];
         if (STAGE == 4) kv = A.a.K[p];
+        if (METHOD == 2 && edge) {
+          if (x == 1) gxl = GH[gl.xlo + y + (long long)N * z];
+          if (x == M - 2) gxh = GH[gl.xhi + y + (long long)N * z];
+          if (y == 1) gyl = GH[gl.ylo + x + (long long)M * z];
+          if (y == N - 2) gyh = GH[gl.yhi + x + (long long)M * z];
+        }
       }
       bool ok = true;
       if (TMA) {
@@ -273,7 +258,6 @@ __global__ void __launch_bounds__(256, NLSE_WIDE_MIN_BLOCKS) wide3d(
         return;
       }
       q[sn] = qload(z + H, sn);
-      patch(z + H, sn);  // read two iterations on, after two barriers
 
       if (inner) {
         const float2* hp = hplane(sc);
@@ -295,6 +279,12 @@ __global__ void __launch_bounds__(256, NLSE_WIDE_MIN_BLOCKS) wide3d(
                        {hp[own - 2 * PX], ep[own - 2 * PX]},
                        {hp[own + 2], ep[own + 2]},
                        {hp[own - 2], ep[own - 2]}};
+          if (edge) {
+            if (y == N - 2) f2n[2] = he_of(gyh);
+            if (y == 1) f2n[3] = he_of(gyl);
+            if (x == M - 2) f2n[4] = he_of(gxh);
+            if (x == 1) f2n[5] = he_of(gxl);
+          }
           T = mixed::f_wide_2shoc<3>(A.c, u0, v, fn, f2n);
           // F next to a face, for the MSD formula of the face points
           if (A.a.fq && (x == 1 || x == M - 2 || y == 1 || y == N - 2 || z == 1 || z == L - 2))

@@ -43,6 +43,7 @@ struct BSolve {
   Consts<float> cf;
   void* buf[8];
   // exact: psi, K, ya, yb, V ; mixed: hi0, hi1, lo0, lo1, K, da, db, V
+  void* dsc;  // 2SHOC: the stage's D at every point (C2<double> / float2), else null
 };
 
 struct BTile {
@@ -52,80 +53,142 @@ struct BTile {
 };
 
 // ---------------------------------------------------------------- device --
+// Per RK4 stage a 2SHOC solve runs two phases: D at every point into dsc
+// (d_at, boundary-condition D on the faces), then -- after a grid barrier --
+// F from those D values and the stage update (f_at_d).  CD solves only run
+// the second phase.  Both phases evaluate the gather-form expressions, so
+// the results equal the single-solve kernels' bit for bit.
 
-template <typename R, int DIM, int METHOD, int BC>
-__device__ __noinline__ void tile_exact(const BSolve& s, int stage, long long p0, long long p1) {
-  typedef C2<R> T2;
-  T2* psi = (T2*)s.buf[0];
-  T2* K = (T2*)s.buf[1];
+// exact (FP64) stage input / output buffers of a stage
+struct ExactIO {
+  C2<double> *psi, *K, *Yout;
+  const C2<double>* Yin;
+  const double* V;
+};
+__device__ __forceinline__ ExactIO exact_io(const BSolve& s, int stage) {
+  typedef C2<double> T2;
+  ExactIO io;
+  io.psi = (T2*)s.buf[0];
+  io.K = (T2*)s.buf[1];
   T2* ya = (T2*)s.buf[2];
   T2* yb = (T2*)s.buf[3];
-  const R* V = (const R*)s.buf[4];
-  const T2* Yin = stage == 1 ? psi : (stage == 3 ? yb : ya);
-  T2* Yout = stage == 2 ? yb : ya;
-  const Consts<R>& c = *reinterpret_cast<const Consts<R>*>(&s.cd);
+  io.V = (const double*)s.buf[4];
+  io.Yin = stage == 1 ? io.psi : (stage == 3 ? yb : ya);
+  io.Yout = stage == 2 ? yb : ya;
+  return io;
+}
+
+struct MixedIO {
+  const float2 *hi_in, *lo_in, *d_in;
+  float2 *hi_out, *lo_out, *K, *d_out;
+  const float* V;
+};
+__device__ __forceinline__ MixedIO mixed_io(const BSolve& s, int stage, int par) {
+  MixedIO io;
+  io.hi_in = (const float2*)s.buf[par];
+  io.lo_in = (const float2*)s.buf[2 + par];
+  io.hi_out = (float2*)s.buf[1 - par];
+  io.lo_out = (float2*)s.buf[3 - par];
+  io.K = (float2*)s.buf[4];
+  float2* da = (float2*)s.buf[5];
+  float2* db = (float2*)s.buf[6];
+  io.V = (const float*)s.buf[7];
+  io.d_in = stage == 3 ? db : da;
+  io.d_out = stage == 2 ? db : da;
+  return io;
+}
+
+template <int DIM, int BC>
+__device__ __noinline__ void dtile_exact(const BSolve& s, int stage, long long p0, long long p1) {
+  const ExactIO io = exact_io(s, stage);
+  const Consts<double>& c = s.cd;
+  C2<double>* D = (C2<double>*)s.dsc;
   for (long long p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
     int i, j, k;
     decompose(s.g, p, i, j, k);
-    T2 T = exact::f_at<R, DIM, METHOD, BC>(s.g, c, Yin, V, i, j, k);
-    exact::update<R>(c, stage, p, T, psi, K, Yout);
+    D[p] = exact::d_at<double, DIM, BC>(s.g, c, io.Yin, io.V, i, j, k);
   }
 }
 
 template <int DIM, int METHOD, int BC>
-__device__ __noinline__ void tile_mixed(const BSolve& s, int stage, int par, long long p0,
-                                        long long p1) {
-  const float2* hi_in = (const float2*)s.buf[par];
-  const float2* lo_in = (const float2*)s.buf[2 + par];
-  float2* hi_out = (float2*)s.buf[1 - par];
-  float2* lo_out = (float2*)s.buf[3 - par];
-  float2* K = (float2*)s.buf[4];
-  float2* da = (float2*)s.buf[5];
-  float2* db = (float2*)s.buf[6];
-  const float* V = (const float*)s.buf[7];
-  const float2* d_in = stage == 3 ? db : da;
-  float2* d_out = stage == 2 ? db : da;
-  mixed::YIn Y{hi_in, stage == 1 ? lo_in : d_in};
+__device__ __noinline__ void ftile_exact(const BSolve& s, int stage, long long p0, long long p1) {
+  const ExactIO io = exact_io(s, stage);
+  const Consts<double>& c = s.cd;
+  const C2<double>* D = (const C2<double>*)s.dsc;
   for (long long p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
     int i, j, k;
     decompose(s.g, p, i, j, k);
-    float2 T = mixed::f_at<DIM, METHOD, BC>(s.g, s.cf, Y, V, i, j, k);
-    mixed::update(s.cf, stage, p, T, hi_in, lo_in, d_in, K, d_out, hi_out, lo_out);
+    C2<double> T = METHOD == 2 ? exact::f_at_d<double, DIM, BC>(s.g, c, io.Yin, io.V, D, i, j, k)
+                               : exact::f_at<double, DIM, 1, BC>(s.g, c, io.Yin, io.V, i, j, k);
+    exact::update<double>(c, stage, p, T, io.psi, io.K, io.Yout);
   }
 }
 
-template <int DIM, int METHOD>
-__device__ void by_bc(const BSolve& s, int stage, int par, long long p0, long long p1) {
-  if (s.prec == NLSE_PREC_DOUBLE) {
-    switch (s.bc) {
-      case 1: tile_exact<double, DIM, METHOD, 1>(s, stage, p0, p1); break;
-      case 2: tile_exact<double, DIM, METHOD, 2>(s, stage, p0, p1); break;
-      case 3: tile_exact<double, DIM, METHOD, 3>(s, stage, p0, p1); break;
-      default:
-        if (DIM == 1) tile_exact<double, 1, METHOD, 4>(s, stage, p0, p1);
-        break;
-    }
+template <int DIM, int BC>
+__device__ __noinline__ void dtile_mixed(const BSolve& s, int stage, int par, long long p0,
+                                         long long p1) {
+  const MixedIO io = mixed_io(s, stage, par);
+  mixed::YIn Y{io.hi_in, stage == 1 ? io.lo_in : io.d_in};
+  float2* D = (float2*)s.dsc;
+  for (long long p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
+    int i, j, k;
+    decompose(s.g, p, i, j, k);
+    D[p] = mixed::d_at<DIM, BC>(s.g, s.cf, Y, io.V, i, j, k);
+  }
+}
+
+template <int DIM, int METHOD, int BC>
+__device__ __noinline__ void ftile_mixed(const BSolve& s, int stage, int par, long long p0,
+                                         long long p1) {
+  const MixedIO io = mixed_io(s, stage, par);
+  mixed::YIn Y{io.hi_in, stage == 1 ? io.lo_in : io.d_in};
+  const float2* D = (const float2*)s.dsc;
+  for (long long p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
+    int i, j, k;
+    decompose(s.g, p, i, j, k);
+    float2 T = METHOD == 2 ? mixed::f_at_d<DIM, BC>(s.g, s.cf, Y, io.V, D, i, j, k)
+                           : mixed::f_at<DIM, 1, BC>(s.g, s.cf, Y, io.V, i, j, k);
+    mixed::update(s.cf, stage, p, T, io.hi_in, io.lo_in, io.d_in, io.K, io.d_out, io.hi_out,
+                  io.lo_out);
+  }
+}
+
+// phase 0: D (2SHOC solves), phase 1: F + update
+template <int CLS, int DIM, int METHOD, int BC>
+__device__ __forceinline__ void tile_one(const BSolve& s, int ph, int stage, int par, long long p0,
+                                         long long p1) {
+  if (CLS == NLSE_PREC_DOUBLE) {
+    if (ph == 0) dtile_exact<DIM, BC>(s, stage, p0, p1);
+    else ftile_exact<DIM, METHOD, BC>(s, stage, p0, p1);
   } else {
-    switch (s.bc) {
-      case 1: tile_mixed<DIM, METHOD, 1>(s, stage, par, p0, p1); break;
-      case 2: tile_mixed<DIM, METHOD, 2>(s, stage, par, p0, p1); break;
-      case 3: tile_mixed<DIM, METHOD, 3>(s, stage, par, p0, p1); break;
-      default:
-        if (DIM == 1) tile_mixed<1, METHOD, 4>(s, stage, par, p0, p1);
-        break;
-    }
+    if (ph == 0) dtile_mixed<DIM, BC>(s, stage, par, p0, p1);
+    else ftile_mixed<DIM, METHOD, BC>(s, stage, par, p0, p1);
   }
 }
 
-__device__ void process_tile(const BSolve& s, int stage, int par, long long p0, long long p1) {
+template <int CLS, int DIM, int METHOD>
+__device__ void by_bc(const BSolve& s, int ph, int stage, int par, long long p0, long long p1) {
+  switch (s.bc) {
+    case 1: tile_one<CLS, DIM, METHOD, 1>(s, ph, stage, par, p0, p1); break;
+    case 2: tile_one<CLS, DIM, METHOD, 2>(s, ph, stage, par, p0, p1); break;
+    case 3: tile_one<CLS, DIM, METHOD, 3>(s, ph, stage, par, p0, p1); break;
+    default:
+      if (DIM == 1) tile_one<CLS, 1, METHOD, 4>(s, ph, stage, par, p0, p1);
+      break;
+  }
+}
+
+template <int CLS>
+__device__ void process_tile(const BSolve& s, int ph, int stage, int par, long long p0,
+                             long long p1) {
   if (s.method == 1) {
-    if (s.g.ndim == 1) by_bc<1, 1>(s, stage, par, p0, p1);
-    else if (s.g.ndim == 2) by_bc<2, 1>(s, stage, par, p0, p1);
-    else by_bc<3, 1>(s, stage, par, p0, p1);
+    if (s.g.ndim == 1) by_bc<CLS, 1, 1>(s, ph, stage, par, p0, p1);
+    else if (s.g.ndim == 2) by_bc<CLS, 2, 1>(s, ph, stage, par, p0, p1);
+    else by_bc<CLS, 3, 1>(s, ph, stage, par, p0, p1);
   } else {
-    if (s.g.ndim == 1) by_bc<1, 2>(s, stage, par, p0, p1);
-    else if (s.g.ndim == 2) by_bc<2, 2>(s, stage, par, p0, p1);
-    else by_bc<3, 2>(s, stage, par, p0, p1);
+    if (s.g.ndim == 1) by_bc<CLS, 1, 2>(s, ph, stage, par, p0, p1);
+    else if (s.g.ndim == 2) by_bc<CLS, 2, 2>(s, ph, stage, par, p0, p1);
+    else by_bc<CLS, 3, 2>(s, ph, stage, par, p0, p1);
   }
 }
 
@@ -170,37 +233,44 @@ __device__ bool grid_barrier(BarrierState* bar, int* err, long long budget) {
   return s_ok != 0;
 }
 
-__global__ void __launch_bounds__(BT) batch_kernel(const BSolve* __restrict__ solves,
-                                                   const BTile* __restrict__ tiles, int ntiles,
-                                                   int steps, unsigned* qctr, BarrierState* bar,
-                                                   int* err, long long budget) {
+// One launch per precision class.  tiles[0, ntiles_d) are the tiles of the
+// 2SHOC solves (phase 0 runs over them), tiles[0, ntiles) all tiles.
+template <int CLS>
+__global__ void __launch_bounds__(BT, CLS == NLSE_PREC_MIXED ? 4 : 3) batch_kernel(const BSolve* __restrict__ solves,
+                                                      const BTile* __restrict__ tiles, int ntiles,
+                                                      int ntiles_d, int steps, unsigned* qctr,
+                                                      BarrierState* bar, int* err,
+                                                      long long budget) {
   __shared__ BSolve s;
   __shared__ int s_t;
   for (int step = 0; step < steps; ++step) {
     for (int stage = 1; stage <= 4; ++stage) {
-      const int pass = step * 4 + stage - 1;
-      while (true) {
-        if (threadIdx.x == 0) s_t = (int)atomicAdd(&qctr[pass], 1u);
-        __syncthreads();
-        const int t = s_t;
-        if (t >= ntiles) break;
-        const BTile tl = tiles[t];
-        // cooperative copy of the solve descriptor into shared memory
-        {
-          const int* src = reinterpret_cast<const int*>(&solves[tl.solve]);
-          int* dst = reinterpret_cast<int*>(&s);
-          for (int w = threadIdx.x; w < (int)(sizeof(BSolve) / sizeof(int)); w += blockDim.x)
-            dst[w] = src[w];
+      for (int ph = ntiles_d > 0 ? 0 : 1; ph < 2; ++ph) {
+        const int pass = (step * 4 + stage - 1) * 2 + ph;
+        const int nt = ph == 0 ? ntiles_d : ntiles;
+        while (true) {
+          if (threadIdx.x == 0) s_t = (int)atomicAdd(&qctr[pass], 1u);
+          __syncthreads();
+          const int t = s_t;
+          if (t >= nt) break;
+          const BTile tl = tiles[t];
+          // cooperative copy of the solve descriptor into shared memory
+          {
+            const int* src = reinterpret_cast<const int*>(&solves[tl.solve]);
+            int* dst = reinterpret_cast<int*>(&s);
+            for (int w = threadIdx.x; w < (int)(sizeof(BSolve) / sizeof(int)); w += blockDim.x)
+              dst[w] = src[w];
+          }
+          __syncthreads();
+          if (step < s.steps_left) {
+            long long p1 = tl.start + TILE;
+            if (p1 > s.g.n) p1 = s.g.n;
+            process_tile<CLS>(s, ph, stage, s.cur ^ (step & 1), tl.start, p1);
+          }
+          __syncthreads();
         }
-        __syncthreads();
-        if (step < s.steps_left) {
-          long long p1 = tl.start + TILE;
-          if (p1 > s.g.n) p1 = s.g.n;
-          process_tile(s, stage, s.cur ^ (step & 1), tl.start, p1);
-        }
-        __syncthreads();
+        if (!grid_barrier(bar, err, budget)) return;
       }
-      if (!grid_barrier(bar, err, budget)) return;
     }
   }
 }
@@ -255,10 +325,12 @@ struct nlse_batch {
   // staging for transfers (planar doubles)
   double* stage = nullptr;
   size_t stage_cap = 0;
-  int max_blocks = 0;
+  int max_blocks[2] = {0, 0};  // per class: FP64, mixed
   int last_launches = 0;
 };
 
+// Buffers of one solve in the pool: the state buffers (BSolve::buf) and,
+// for 2SHOC, the D scratch (BSolve::dsc) last.
 static bool layout(const nlse_problem* p, size_t* sizes, int* nbuf) {
   long long n = p->dims[0] * (p->ndim >= 2 ? p->dims[1] : 1) * (p->ndim >= 3 ? p->dims[2] : 1);
   if (p->precision == NLSE_PREC_DOUBLE) {
@@ -272,11 +344,12 @@ static bool layout(const nlse_problem* p, size_t* sizes, int* nbuf) {
   } else {
     return false;
   }
+  if (p->method == 2) sizes[(*nbuf)++] = (p->precision == NLSE_PREC_DOUBLE ? 16 : 8) * (size_t)n;
   return true;
 }
 
 extern "C" long long nlse_batch_bytes_for(const nlse_problem* p) {
-  size_t sz[8];
+  size_t sz[9];
   int nb = 0;
   if (!p || !layout(p, sz, &nb)) return -1;
   size_t tot = 0;
@@ -359,11 +432,14 @@ extern "C" int nlse_batch_create(long long pool_bytes, int max_solves, nlse_batc
   }
   cudaMemsetAsync(b->d_bar, 0, sizeof(BarrierState), b->stream);
   cudaMemsetAsync(b->d_err, 0, sizeof(int), b->stream);
-  int sms = 0, per_sm = 0;
+  int sms = 0, per64 = 0, permx = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, BT, 0);
-  if (per_sm < 1) return cleanup(nlse::set_error(NLSE_ERR_CUDA, "batch kernel cannot be resident"));
-  b->max_blocks = sms * per_sm;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per64, batch_kernel<NLSE_PREC_DOUBLE>, BT, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&permx, batch_kernel<NLSE_PREC_MIXED>, BT, 0);
+  if (per64 < 1 || permx < 1)
+    return cleanup(nlse::set_error(NLSE_ERR_CUDA, "batch kernel cannot be resident"));
+  b->max_blocks[0] = sms * per64;
+  b->max_blocks[1] = sms * permx;
   (void)rc;
   *out = b;
   return NLSE_OK;
@@ -396,7 +472,7 @@ extern "C" int nlse_batch_add(nlse_batch* b, const nlse_problem* p, const double
       break;
     }
   if (idx < 0) return nlse::set_error(NLSE_ERR_CAPACITY, "no free batch slot");
-  size_t sz[8];
+  size_t sz[9];
   int nb = 0;
   layout(p, sz, &nb);
   size_t tot = (size_t)nlse_batch_bytes_for(p);
@@ -422,8 +498,12 @@ extern "C" int nlse_batch_add(nlse_batch* b, const nlse_problem* p, const double
   S.d.steps_left = nsteps;
   nlse_fill_consts(p, &S.d.cd, &S.d.cf);
   size_t o = off;
+  const int nstate = p->method == 2 ? nb - 1 : nb;
   for (int t = 0; t < nb; ++t) {
-    S.d.buf[t] = b->pool + o;
+    if (t < nstate)
+      S.d.buf[t] = b->pool + o;
+    else
+      S.d.dsc = b->pool + o;
     o += al(sz[t]);
   }
   // upload
@@ -451,6 +531,8 @@ extern "C" int nlse_batch_add(nlse_batch* b, const nlse_problem* p, const double
   return NLSE_OK;
 }
 
+// One cooperative launch per precision class present; the classes run one
+// after the other on the batch stream.
 extern "C" int nlse_batch_run(nlse_batch* b, int max_steps) {
   if (!b || max_steps < 0) return nlse::set_error(NLSE_ERR_ARG, "bad argument");
   BTRY(cudaSetDevice(b->device));
@@ -459,73 +541,92 @@ extern "C" int nlse_batch_run(nlse_batch* b, int max_steps) {
   int err = 0;
   BTRY(cudaMemcpy(&err, b->d_err, sizeof(int), cudaMemcpyDeviceToHost));
   if (err) return nlse::set_error(err, "a previous batch launch gave up waiting at a grid barrier");
-  // solve table + tile list of the solves that still run
-  int nsolves = 0;
-  long long ntiles = 0;
-  int steps = 0;
-  std::vector<int> which;
-  for (size_t t = 0; t < b->slots.size(); ++t) {
-    Slot& S = b->slots[t];
-    if (!S.used || S.d.steps_left <= 0) continue;
-    which.push_back((int)t);
-    ntiles += (S.d.g.n + TILE - 1) / TILE;
-    long long adv = S.d.steps_left < max_steps ? S.d.steps_left : max_steps;
-    if (adv > steps) steps = (int)adv;
-  }
-  if (which.empty() || steps == 0) return NLSE_OK;
-  if (ntiles > (1LL << 31) - 1) return nlse::set_error(NLSE_ERR_CAPACITY, "too many tiles");
-  if ((size_t)ntiles > b->tiles_cap) {
+  // per class: the solves that still run, 2SHOC first; steps = longest advance
+  std::vector<int> which[2];
+  long long ntiles[2] = {0, 0}, ntiles_d[2] = {0, 0};
+  int steps[2] = {0, 0};
+  for (int pass = 0; pass < 2; ++pass)  // 2SHOC solves, then CD solves
+    for (size_t t = 0; t < b->slots.size(); ++t) {
+      Slot& S = b->slots[t];
+      if (!S.used || S.d.steps_left <= 0 || (S.d.method == 2) != (pass == 0)) continue;
+      const int c = S.d.prec == NLSE_PREC_DOUBLE ? 0 : 1;
+      which[c].push_back((int)t);
+      const long long nt = (S.d.g.n + TILE - 1) / TILE;
+      ntiles[c] += nt;
+      if (pass == 0) ntiles_d[c] += nt;
+      long long adv = S.d.steps_left < max_steps ? S.d.steps_left : max_steps;
+      if (adv > steps[c]) steps[c] = (int)adv;
+    }
+  const long long total_tiles = ntiles[0] + ntiles[1];
+  if (total_tiles == 0 || (steps[0] == 0 && steps[1] == 0)) return NLSE_OK;
+  if (total_tiles > (1LL << 31) - 1) return nlse::set_error(NLSE_ERR_CAPACITY, "too many tiles");
+  if ((size_t)total_tiles > b->tiles_cap) {
     if (b->d_tiles) cudaFree(b->d_tiles);
     if (b->h_tiles) cudaFreeHost(b->h_tiles);
     b->d_tiles = nullptr;
     b->h_tiles = nullptr;
-    size_t cap = (size_t)ntiles * 2;
+    size_t cap = (size_t)total_tiles * 2;
     BTRY(cudaMalloc(&b->d_tiles, sizeof(BTile) * cap));
     BTRY(cudaMallocHost(&b->h_tiles, sizeof(BTile) * cap));
     b->tiles_cap = cap;
   }
-  size_t passes = (size_t)steps * 4;
+  const size_t passes = (size_t)(steps[0] > steps[1] ? steps[0] : steps[1]) * 8;
   if (passes > b->qctr_cap) {
     if (b->d_qctr) cudaFree(b->d_qctr);
     b->d_qctr = nullptr;
     BTRY(cudaMalloc(&b->d_qctr, sizeof(unsigned) * passes));
     b->qctr_cap = passes;
   }
+  // solve table and tile lists (class 0 tiles, then class 1 tiles)
+  int nsolves = 0;
   long long tt = 0;
-  for (int id : which) {
-    Slot& S = b->slots[id];
-    b->h_solves[nsolves] = S.d;
-    long long nt = (S.d.g.n + TILE - 1) / TILE;
-    for (long long q = 0; q < nt; ++q) {
-      b->h_tiles[tt].solve = nsolves;
-      b->h_tiles[tt].pad = 0;
-      b->h_tiles[tt].start = q * TILE;
-      ++tt;
+  for (int c = 0; c < 2; ++c)
+    for (int id : which[c]) {
+      Slot& S = b->slots[id];
+      b->h_solves[nsolves] = S.d;
+      const long long nt = (S.d.g.n + TILE - 1) / TILE;
+      for (long long q = 0; q < nt; ++q) {
+        b->h_tiles[tt].solve = nsolves;
+        b->h_tiles[tt].pad = 0;
+        b->h_tiles[tt].start = q * TILE;
+        ++tt;
+      }
+      ++nsolves;
     }
-    ++nsolves;
-  }
   BTRY(cudaMemcpyAsync(b->d_solves, b->h_solves, sizeof(BSolve) * nsolves, cudaMemcpyHostToDevice,
                        b->stream));
-  BTRY(cudaMemcpyAsync(b->d_tiles, b->h_tiles, sizeof(BTile) * ntiles, cudaMemcpyHostToDevice,
+  BTRY(cudaMemcpyAsync(b->d_tiles, b->h_tiles, sizeof(BTile) * total_tiles, cudaMemcpyHostToDevice,
                        b->stream));
-  BTRY(cudaMemsetAsync(b->d_qctr, 0, sizeof(unsigned) * passes, b->stream));
-  BTRY(cudaMemsetAsync(b->d_bar, 0, sizeof(BarrierState), b->stream));
-  int blocks = b->max_blocks;
-  if ((long long)blocks > ntiles) blocks = (int)ntiles;
-  int nt_i = (int)ntiles;
   long long budget = 100000000000LL;  // clock cycles a CTA may wait at one barrier
-  void* args[] = {&b->d_solves, &b->d_tiles, &nt_i, &steps, &b->d_qctr, &b->d_bar, &b->d_err,
-                  &budget};
-  BTRY(cudaLaunchCooperativeKernel((const void*)batch_kernel, dim3(blocks), dim3(BT), args, 0,
-                                   b->stream));
-  b->last_launches = 1;
-  // host bookkeeping of the steps each solve advanced in this launch
-  for (int id : which) {
-    Slot& S = b->slots[id];
-    long long adv = S.d.steps_left < steps ? S.d.steps_left : steps;
-    S.d.steps_left -= adv;
-    if (S.d.prec == NLSE_PREC_MIXED && (adv & 1)) S.d.cur ^= 1;
+  long long first = 0;
+  for (int c = 0; c < 2; ++c) {
+    if (which[c].empty() || steps[c] == 0) {
+      first += ntiles[c];
+      continue;
+    }
+    const size_t np = (size_t)steps[c] * 8;
+    BTRY(cudaMemsetAsync(b->d_qctr, 0, sizeof(unsigned) * np, b->stream));
+    BTRY(cudaMemsetAsync(b->d_bar, 0, sizeof(BarrierState), b->stream));
+    int blocks = b->max_blocks[c];
+    if ((long long)blocks > ntiles[c]) blocks = (int)ntiles[c];
+    const BTile* tiles = b->d_tiles + first;
+    int nt_i = (int)ntiles[c], ntd_i = (int)ntiles_d[c], st_i = steps[c];
+    void* args[] = {(void*)&b->d_solves, (void*)&tiles, &nt_i, &ntd_i, &st_i,
+                    (void*)&b->d_qctr, (void*)&b->d_bar, (void*)&b->d_err, &budget};
+    const void* kern = c == 0 ? (const void*)batch_kernel<NLSE_PREC_DOUBLE>
+                              : (const void*)batch_kernel<NLSE_PREC_MIXED>;
+    BTRY(cudaLaunchCooperativeKernel(kern, dim3(blocks), dim3(BT), args, 0, b->stream));
+    ++b->last_launches;
+    first += ntiles[c];
   }
+  // host bookkeeping of the steps each solve advanced in these launches
+  for (int c = 0; c < 2; ++c)
+    for (int id : which[c]) {
+      Slot& S = b->slots[id];
+      long long adv = S.d.steps_left < steps[c] ? S.d.steps_left : steps[c];
+      S.d.steps_left -= adv;
+      if (S.d.prec == NLSE_PREC_MIXED && (adv & 1)) S.d.cur ^= 1;
+    }
   return NLSE_OK;
 }
 

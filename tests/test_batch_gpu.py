@@ -153,3 +153,20 @@ def test_uneven_config4_sample(gpu_lib):
                                  method=i.method, precision=2, flags=oracle.MSD_GUARD)
         assert W.rel_l2(b.download(sl), want) <= MIXED_TOL
     b.close()
+
+
+def test_mixed_batch_equals_single_solver(gpu_lib, cases):
+    # 1D/2D: the batch's two-phase stage (D into scratch, then F) and the
+    # single-solve gather kernel evaluate the same expressions: same bits
+    import nlsemagic_gb300 as ng
+    steps = 17
+    b = ng.Batch(1 << 28)
+    picked = [c for c in cases if c["U"].ndim <= 2]
+    slots = [b.add(c["U"], c["V"], c["s"], c["a"], c["h2"], c["BC"], steps, c["k"], c["method"],
+                   ng.PREC_MIXED) for c in picked]
+    b.run(steps)
+    for c, sl in zip(picked, slots):
+        one = ng.take_steps(c["U"], c["V"], c["s"], c["a"], c["h2"], c["BC"], steps, c["k"],
+                            method=c["method"], precision=ng.PREC_MIXED)
+        assert bits_equal(b.download(sl), one)
+    b.close()
