@@ -493,31 +493,64 @@ def run_batched(args):
             "speedup": v_batch / v_seq}
 
 
+def fifo_latencies(arrivals, service):
+    """Latencies of a single first-come-first-served server with the given
+    arrival times and per-request service times."""
+    clock, lat = 0.0, []
+    for a, d in sorted(zip(arrivals, service)):
+        clock = max(clock, a) + d
+        lat.append(clock - a)
+    return lat
+
+
 def run_serving(args):
     """Continuous-batching request loop on a seeded Poisson stream (dims
     1D:2D:3D = 5:4:1, sizes and step counts log-uniform, FP64 or mixed per
-    request), against serving the same stream one solve at a time."""
+    request) against one solve at a time (each request through its own
+    Solver: create, upload, run, download, release), both saturated (every
+    request queued at t = 0) and at the offered arrival rate."""
     from nlsemagic_gb300 import workloads as W
-    from nlsemagic_gb300.serve import Server, serve_sequential
+    from nlsemagic_gb300.serve import Server, percentile, serve_sequential
     reqs = W.serving_requests(count=args.serve_requests, rate=args.serve_rate,
                               n1=(512, 65536), n2=(64, 1024), n3=(32, args.serve_max3d),
                               steps=(100, args.serve_max_steps))
-    srv = Server(pool_bytes=args.serve_pool_gb << 30, chunk_steps=args.serve_chunk)
-    summary, _ = srv.serve(reqs)
+    pool = args.serve_pool_gb << 30
+
+    def server():
+        return Server(pool_bytes=pool, chunk_steps=args.serve_chunk, solo_bytes=pool)
+
+    srv = server()
+    sat, _ = srv.serve(reqs, time_scale=0.0)  # saturated: all queued at t = 0
     srv.close()
-    log("served: %s" % json.dumps(summary))
-    seq = serve_sequential(reqs)
+    log("served (saturated): %s" % json.dumps(sat))
+    srv = server()
+    live, _ = srv.serve(reqs, time_scale=1.0)  # Poisson arrivals at the offered rate
+    srv.close()
+    log("served (rate %.1f/s): %s" % (args.serve_rate, json.dumps(live)))
+    seq, seq_done = serve_sequential(reqs, time_scale=0.0)
+    service = [c.done - c.admitted for c in seq_done]
+    arrivals = [r.arrival for r in sorted(reqs, key=lambda r: r.arrival)]
+    lat = fifo_latencies(arrivals, service)
+    seq_live = {"p50_latency_s": percentile(lat, 50), "p99_latency_s": percentile(lat, 99)}
     log("sequential: %s" % json.dumps(seq))
     return {"requests": len(reqs), "rate_per_s": args.serve_rate,
             "dims_ratio": "5:4:1", "sizes": {"1d": [512, 65536], "2d": [64, 1024],
                                              "3d": [32, args.serve_max3d]},
-            "steps": [100, args.serve_max_steps], "chunk_steps": args.serve_chunk,
-            "value": summary["gpt_steps_per_s"], "unit": UNIT,
-            "p50_latency_s": summary["p50_latency_s"], "p99_latency_s": summary["p99_latency_s"],
-            "p99_queue_s": summary["p99_queue_s"], "wall_s": summary["wall_s"],
-            "sequential": seq,
-            "throughput_over_sequential": summary["gpt_steps_per_busy_s"] /
-            seq["gpt_steps_per_busy_s"] if seq["gpt_steps_per_busy_s"] else None}
+            "steps": [100, args.serve_max_steps], "precision": "FP64 or mixed, 50/50",
+            "chunk_steps": args.serve_chunk,
+            "value": sat["gpt_steps_per_s"], "unit": UNIT,
+            "requests_per_s": sat["requests_per_s"],
+            "at_rate": {"p50_latency_s": live["p50_latency_s"],
+                        "p99_latency_s": live["p99_latency_s"],
+                        "p99_queue_s": live["p99_queue_s"], "wall_s": live["wall_s"],
+                        "gpt_steps_per_s": live["gpt_steps_per_s"]},
+            "one_at_a_time": {"value": seq["gpt_steps_per_s"], "unit": UNIT,
+                              "requests_per_s": seq["requests_per_s"],
+                              "at_rate": seq_live},
+            "throughput_over_one_at_a_time": sat["gpt_steps_per_s"] / seq["gpt_steps_per_s"]
+            if seq["gpt_steps_per_s"] else None,
+            "requests_per_s_over_one_at_a_time": sat["requests_per_s"] / seq["requests_per_s"]
+            if seq["requests_per_s"] else None}
 
 
 def main():

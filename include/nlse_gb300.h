@@ -175,6 +175,10 @@ int nlse_solver_set_graph_steps(nlse_solver *s, int steps);
 int nlse_solver_launches_per_step(const nlse_solver *s);
 /* Bytes of device memory held by the solver. */
 long long nlse_solver_device_bytes(const nlse_solver *s);
+/* Bytes of device memory a solver for *p holds after a host upload (its
+ * state, scratch and planar staging buffers); -1 for an invalid problem.
+ * For admission by a device-memory budget (no reference counterpart). */
+long long nlse_solver_bytes_for(const nlse_problem *p);
 
 /* ------------------------------------------------------------------------
  * Batched solves: many independent solves of uneven dimension, size,

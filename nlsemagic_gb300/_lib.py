@@ -73,6 +73,7 @@ SIGNATURES = {
     "nlse_solver_set_graph_steps": (_i, [_vp, _i]),
     "nlse_solver_launches_per_step": (_i, [_vp]),
     "nlse_solver_device_bytes": (_ll, [_vp]),
+    "nlse_solver_bytes_for": (_ll, [ctypes.POINTER(Problem)]),
     "nlse_batch_create": (_i, [_ll, _i, ctypes.POINTER(_vp)]),
     "nlse_batch_destroy": (_i, [_vp]),
     "nlse_batch_bytes_for": (_ll, [ctypes.POINTER(Problem)]),

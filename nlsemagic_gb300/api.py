@@ -154,6 +154,13 @@ class Solver:
         check(self._lib.nlse_solver_create(ctypes.byref(self.problem), ctypes.byref(h)))
         self._h = h
 
+    @staticmethod
+    def bytes_for(shape, method=2, precision=PREC_MIXED, BC=1, flags=FLAG_MSD_GUARD):
+        """Device bytes a solver of this shape and class holds after a host upload."""
+        ndim, dims = grid_dims(shape)
+        p = make_problem(ndim, dims, method, precision, BC, 0.0, 1.0, 1.0, 1.0, flags)
+        return int(load().nlse_solver_bytes_for(ctypes.byref(p)))
+
     # -- lifecycle
     def close(self):
         if getattr(self, "_h", None):
@@ -254,9 +261,10 @@ class Batch:
             pass
 
     @staticmethod
-    def bytes_for(shape, precision):
+    def bytes_for(shape, precision, method=2):
+        """Pool bytes one solve takes (2SHOC solves also hold their D scratch)."""
         ndim, dims = grid_dims(shape)
-        p = make_problem(ndim, dims, 1, precision, 1, 0.0, 1.0, 1.0, 1.0)
+        p = make_problem(ndim, dims, method, precision, 1, 0.0, 1.0, 1.0, 1.0)
         return int(load().nlse_batch_bytes_for(ctypes.byref(p)))
 
     def add(self, U, V, s, a, h2, BC, nsteps, k, method=2, precision=PREC_MIXED,

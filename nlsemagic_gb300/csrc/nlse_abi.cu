@@ -567,6 +567,22 @@ extern "C" int nlse_solver_launches_per_step(const nlse_solver* s) {
   return 4 * mixed_stage_launches(s->g, s->prob.method, s->prob.bc, s->kernel_kind);
 }
 
+extern "C" long long nlse_solver_bytes_for(const nlse_problem* p) {
+  if (validate(p)) return -1;
+  const Geom g = make_geom(p);
+  const long long n = g.n;
+  const int kind = (p->flags & NLSE_FLAG_GATHER) ? KERNEL_GATHER : KERNEL_TILED;
+  long long b = 0;
+  if (p->precision == NLSE_PREC_DOUBLE || p->precision == NLSE_PREC_SINGLE) {
+    const long long es = p->precision == NLSE_PREC_DOUBLE ? 8 : 4;
+    b = 4 * 2 * es * n + es * n;
+  } else {
+    b = 7 * 8 * n + 4 * n + 16 * mixed_ghost_entries(g, p->method, p->bc, kind) +
+        8 * mixed_fq_entries(g, p->method, p->bc, kind);
+  }
+  return b + (long long)sizeof(double) + (long long)sizeof(int) + 3 * 8 * n;
+}
+
 extern "C" long long nlse_solver_device_bytes(const nlse_solver* s) {
   return s ? (long long)s->bytes : 0;
 }

@@ -53,3 +53,38 @@ def test_serving_waits_when_pool_is_full(gpu_lib):
     assert summary["requests"] == len(reqs)
     assert summary["rejected"] == 0
     assert summary["p99_queue_s"] > 0
+
+
+def test_serving_solo_and_batched_results_equal_alone(gpu_lib):
+    # 3D requests above solo_points run on their own resident solver (tiled
+    # kernels), the rest in the batched launch; each result equals the same
+    # solve run alone on the same path, bit for bit
+    import nlsemagic_gb300 as ng
+    from nlsemagic_gb300.serve import Server, serve_sequential
+    reqs = W.serving_requests(count=24, rate=500.0, n1=(256, 1024), n2=(32, 64), n3=(18, 30),
+                              steps=(20, 60))
+    srv = Server(pool_bytes=1 << 28, chunk_steps=16, keep_snapshots=True, solo_points=8000)
+    summary, done = srv.serve(reqs)
+    srv.close()
+    assert summary["requests"] == len(reqs)
+    assert any(c.solo for c in done) and any(not c.solo for c in done)
+    by_id = {r.rid: r for r in reqs}
+    for c in done:
+        i = by_id[c.rid].inst
+        if c.solo:
+            want = ng.take_steps(i.U, i.V, i.s, i.a, i.h * i.h, i.BC, i.steps, i.k,
+                                 method=i.method, precision=i.precision)
+        else:
+            b = ng.Batch(1 << 26)
+            sl = b.add(i.U, i.V, i.s, i.a, i.h * i.h, i.BC, i.steps, i.k, i.method, i.precision)
+            b.run(i.steps)
+            want = b.download(sl)
+            b.close()
+        assert bits_equal(c.snapshot, want)
+    # the one-at-a-time baseline computes the same solves (single-solve path)
+    seq, seq_done = serve_sequential(reqs[:6], keep_snapshots=True)
+    for c in seq_done:
+        i = by_id[c.rid].inst
+        want = ng.take_steps(i.U, i.V, i.s, i.a, i.h * i.h, i.BC, i.steps, i.k, method=i.method,
+                             precision=i.precision)
+        assert bits_equal(c.snapshot, want)
