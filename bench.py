@@ -386,8 +386,8 @@ def run_gpu(args, w):
         "frac": achieved / peak,
         "traffic": (traffic_ppt * n / 4.0) if traffic_ppt else None,
         "peak_kind": peak_kind,
-        "kernel": "RK4 step: per stage the deep-point kernel (wide3d) and the shell "
-                  "kernels (shell_d, shell_f); %d launches per RK4 step, timed as one "
+        "kernel": "RK4 step: per stage the face-ghost, interior (wide3d) and face "
+                  "kernels; %d launches per RK4 step, timed as one "
                   "CUDA graph" % solver.launches_per_step,
         "algorithmic_bytes_per_point_step": BYTES_MIXED,
         "algorithmic_bytes_per_stage": BYTES_MIXED / 4.0 * n,

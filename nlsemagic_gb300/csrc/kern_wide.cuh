@@ -16,8 +16,9 @@
 // the D's it replaces with opposite signs.  (Algebraic identity; checked in
 // FP64 against the compact form for BCs 1-3, edges and corners included.)
 // The ghosts are computed per stage by ghost3d into a small face array; a
-// point next to a face takes its +-2 neighbour across that face from there
-// (x, y faces) or its register queue holds it (z faces).
+// point next to an x / y face writes its ghost into its own halo cell of the
+// staged plane, and the register queue entry of plane -1 / L holds the z
+// ghost.
 //
 // One CTA owns a TX x TY column and streams through a chunk of z planes:
 //   - each plane (with a 2-cell x/y halo) is staged into a shared-memory ring
@@ -236,16 +237,27 @@ __global__ void __launch_bounds__(256, NLSE_WIDE_MIN_BLOCKS) wide3d(
       const long long p = (long long)z * MN + pxy;
       float v = 0.f;
       float2 lo = make_float2(0.f, 0.f), kv = lo;
-      float4 gxl, gxh, gyl, gyh;  // ghosts across the x / y faces (2SHOC, next to a face)
       if (inner) {
         v = A.a.V[p];
         if (STAGE >= 2) lo = A.a.lo_in[p];
         if (STAGE == 4) kv = A.a.K[p];
-        if (METHOD == 2 && edge) {
-          if (x == 1) gxl = GH[gl.xlo + y + (long long)N * z];
-          if (x == M - 2) gxh = GH[gl.xhi + y + (long long)N * z];
-          if (y == 1) gyl = GH[gl.ylo + x + (long long)M * z];
-          if (y == N - 2) gyh = GH[gl.yhi + x + (long long)M * z];
+        // 2SHOC next to an x / y face: write the ghost across that face into
+        // this thread's own halo cell of plane z (slot sc, landed two
+        // iterations ago, refilled two iterations on).  Only this thread
+        // reads that cell (it lies outside the grid, two cells from this
+        // point), so program order makes it visible.
+        if (METHOD == 2 && edge && (x == 1 || x == M - 2 || y == 1 || y == N - 2)) {
+          float2* hpc = hplane(sc);
+          float2* epc = eplane(sc);
+          auto put = [&](int i, float4 gv) {
+            hpc[i] = make_float2(gv.x, gv.y);
+            epc[i] = make_float2(gv.z, gv.w);
+          };
+          if (x == M - 2) put(own + 2, GH[gl.xhi + y + (long long)N * z]);
+          if (x == 1) put(own - 2, GH[gl.xlo + y + (long long)N * z]);
+          if (y == N - 2) put(own + 2 * PX, GH[gl.yhi + x + (long long)M * z]);
+          if (y == 1) put(own - 2 * PX, GH[gl.ylo + x + (long long)M * z]);
+          if (TMA) fence_proxy_async();  // before the slot's next TMA refill
         }
       }
       bool ok = true;
@@ -279,12 +291,6 @@ __global__ void __launch_bounds__(256, NLSE_WIDE_MIN_BLOCKS) wide3d(
                        {hp[own - 2 * PX], ep[own - 2 * PX]},
                        {hp[own + 2], ep[own + 2]},
                        {hp[own - 2], ep[own - 2]}};
-          if (edge) {
-            if (y == N - 2) f2n[2] = he_of(gyh);
-            if (y == 1) f2n[3] = he_of(gyl);
-            if (x == M - 2) f2n[4] = he_of(gxh);
-            if (x == 1) f2n[5] = he_of(gxl);
-          }
           T = mixed::f_wide_2shoc<3>(A.c, u0, v, fn, f2n);
           // F next to a face, for the MSD formula of the face points
           if (A.a.fq && (x == 1 || x == M - 2 || y == 1 || y == N - 2 || z == 1 || z == L - 2))
