@@ -15,9 +15,23 @@ static cudaError_t launch_one(const Geom& g, const Consts<R>& c, const ExactStag
   }
   long long blocks = (g.n + 255) / 256;
   if (blocks > 152LL * 32) blocks = 152LL * 32;
+  if (METHOD == 2 && a.dsc) {
+    exact::d_stage<R, DIM, BC><<<(unsigned)blocks, 256, 0, st>>>(g, c, a.Yin, a.V, a.dsc);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    exact::gather_stage_d<R, DIM, BC><<<(unsigned)blocks, 256, 0, st>>>(
+        g, c, a.Yin, a.Psi, a.V, a.K, a.Yout, a.dsc, stage);
+    return cudaGetLastError();
+  }
   exact::gather_stage<R, DIM, METHOD, BC><<<(unsigned)blocks, 256, 0, st>>>(
       g, c, a.Yin, a.Psi, a.V, a.K, a.Yout, stage);
   return cudaGetLastError();
+}
+
+long long exact_dsc_entries(const Geom& g, int method, int BC, int kernel_kind) {
+  if (method != 2) return 0;
+  const bool tiled = kernel_kind == KERNEL_TILED && tiled_supported(g, g.ndim) && BC != 4;
+  return tiled ? 0 : g.n;
 }
 
 template <typename R, int DIM, int METHOD>

@@ -166,6 +166,35 @@ __global__ void __launch_bounds__(256) gather_stage(Geom g, Consts<R> c,
   }
 }
 
+// Two-phase 2SHOC stage: D at every point into scratch, then F from it.
+// Same results as gather_stage, without recomputing D at every neighbour.
+template <typename R, int DIM, int BC>
+__global__ void __launch_bounds__(256) d_stage(Geom g, Consts<R> c, const C2<R>* __restrict__ Yin,
+                                               const R* __restrict__ V, C2<R>* __restrict__ D) {
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < g.n;
+       p += (long long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    decompose(g, p, i, j, k);
+    D[p] = d_at<R, DIM, BC>(g, c, Yin, V, i, j, k);
+  }
+}
+
+template <typename R, int DIM, int BC>
+__global__ void __launch_bounds__(256) gather_stage_d(Geom g, Consts<R> c,
+                                                      const C2<R>* __restrict__ Yin, C2<R>* Psi,
+                                                      const R* __restrict__ V,
+                                                      C2<R>* __restrict__ K,
+                                                      C2<R>* __restrict__ Yout,
+                                                      const C2<R>* __restrict__ D, int stage) {
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < g.n;
+       p += (long long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    decompose(g, p, i, j, k);
+    C2<R> T = f_at_d<R, DIM, BC>(g, c, Yin, V, D, i, j, k);
+    update<R>(c, stage, p, T, Psi, K, Yout);
+  }
+}
+
 }  // namespace exact
 
 // =========================== mixed precision =================================
@@ -414,6 +443,43 @@ __global__ void __launch_bounds__(256) gather_stage(Geom g, Consts<float> c,
     int i, j, k;
     decompose(g, p, i, j, k);
     float2 T = f_at<DIM, METHOD, BC>(g, c, Y, V, i, j, k);
+    update(c, stage, p, T, hi_in, lo_in, d_in, K, d_out, hi_out, lo_out);
+  }
+}
+
+// Two-phase 2SHOC stage (see exact::d_stage / gather_stage_d).
+template <int DIM, int BC>
+__global__ void __launch_bounds__(256) d_stage(Geom g, Consts<float> c,
+                                               const float2* __restrict__ hi_in,
+                                               const float2* __restrict__ e_in,
+                                               const float* __restrict__ V,
+                                               float2* __restrict__ D) {
+  YIn Y{hi_in, e_in};
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < g.n;
+       p += (long long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    decompose(g, p, i, j, k);
+    D[p] = d_at<DIM, BC>(g, c, Y, V, i, j, k);
+  }
+}
+
+template <int DIM, int BC>
+__global__ void __launch_bounds__(256) gather_stage_d(Geom g, Consts<float> c,
+                                                      const float2* __restrict__ hi_in,
+                                                      const float2* __restrict__ lo_in,
+                                                      const float2* __restrict__ d_in,
+                                                      const float* __restrict__ V,
+                                                      float2* __restrict__ K,
+                                                      float2* __restrict__ d_out,
+                                                      float2* __restrict__ hi_out,
+                                                      float2* __restrict__ lo_out,
+                                                      const float2* __restrict__ D, int stage) {
+  YIn Y{hi_in, stage == 1 ? lo_in : d_in};
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < g.n;
+       p += (long long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    decompose(g, p, i, j, k);
+    float2 T = f_at_d<DIM, BC>(g, c, Y, V, D, i, j, k);
     update(c, stage, p, T, hi_in, lo_in, d_in, K, d_out, hi_out, lo_out);
   }
 }

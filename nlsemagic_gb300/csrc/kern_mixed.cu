@@ -18,6 +18,15 @@ static cudaError_t launch_one(const Geom& g, const Consts<float>& c, const Mixed
   }
   long long blocks = (g.n + 255) / 256;
   if (blocks > 152LL * 32) blocks = 152LL * 32;
+  if (METHOD == 2 && a.dsc) {
+    mixed::d_stage<DIM, BC><<<(unsigned)blocks, 256, 0, st>>>(
+        g, c, a.hi_in, stage == 1 ? a.lo_in : a.e_in, a.V, a.dsc);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    mixed::gather_stage_d<DIM, BC><<<(unsigned)blocks, 256, 0, st>>>(
+        g, c, a.hi_in, a.lo_in, a.e_in, a.V, a.K, a.e_out, a.hi_out, a.lo_out, a.dsc, stage);
+    return cudaGetLastError();
+  }
   mixed::gather_stage<DIM, METHOD, BC><<<(unsigned)blocks, 256, 0, st>>>(
       g, c, a.hi_in, a.lo_in, a.e_in, a.V, a.K, a.e_out, a.hi_out, a.lo_out, stage);
   return cudaGetLastError();
@@ -42,8 +51,12 @@ static bool wide_path(const Geom& g, int BC, int kernel_kind) {
 }
 
 int mixed_stage_launches(const Geom& g, int method, int BC, int kernel_kind) {
-  if (!wide_path(g, BC, kernel_kind)) return 1;
+  if (!wide_path(g, BC, kernel_kind)) return method == 2 ? 2 : 1;  // (D,) F
   return method == 2 ? 3 : 2;  // (ghosts,) interior, faces
+}
+
+long long mixed_dsc_entries(const Geom& g, int method, int BC, int kernel_kind) {
+  return method == 2 && !wide_path(g, BC, kernel_kind) ? g.n : 0;
 }
 
 long long mixed_ghost_entries(const Geom& g, int method, int BC, int kernel_kind) {

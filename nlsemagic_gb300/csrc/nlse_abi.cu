@@ -239,6 +239,7 @@ struct nlse_solver {
   int kernel_kind;
   // exact precisions
   void *psi, *K, *ya, *yb, *V;
+  void* dsc;  // 2SHOC on the gather path: D scratch (C2<R> or float2 per point)
   // mixed precision
   float2 *hi[2], *lo[2], *mK, *da, *db, *fq;
   float4* gh;
@@ -287,7 +288,8 @@ extern "C" int nlse_solver_destroy(nlse_solver* s) {
   if (s->stream) cudaStreamSynchronize(s->stream);
   free_graphs(s);
   void* ptrs[] = {s->psi, s->K, s->ya, s->yb, s->V, s->hi[0], s->hi[1], s->lo[0], s->lo[1],
-                  s->mK, s->da, s->db, s->fq, s->gh, s->Vf, s->stage, s->d_mass, s->d_bad};
+                  s->mK, s->da, s->db, s->fq, s->gh, s->Vf, s->stage, s->d_mass, s->d_bad,
+                  s->dsc};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -332,6 +334,8 @@ extern "C" int nlse_solver_create(const nlse_problem* p, nlse_solver** out) {
     if (!r) r = dalloc(s, &s->ya, 2 * es * n);
     if (!r) r = dalloc(s, &s->yb, 2 * es * n);
     if (!r) r = dalloc(s, &s->V, es * n);
+    const long long nd = exact_dsc_entries(s->g, p->method, p->bc, s->kernel_kind);
+    if (!r && nd) r = dalloc(s, &s->dsc, 2 * es * nd);
   } else {
     for (int t = 0; t < 2 && !r; ++t) {
       r = dalloc(s, (void**)&s->hi[t], sizeof(float2) * n);
@@ -345,6 +349,8 @@ extern "C" int nlse_solver_create(const nlse_problem* p, nlse_solver** out) {
     const long long nf = mixed_fq_entries(s->g, p->method, p->bc, s->kernel_kind);
     if (!r && ng) r = dalloc(s, (void**)&s->gh, sizeof(float4) * ng);
     if (!r && nf) r = dalloc(s, (void**)&s->fq, sizeof(float2) * nf);
+    const long long nd = mixed_dsc_entries(s->g, p->method, p->bc, s->kernel_kind);
+    if (!r && nd) r = dalloc(s, &s->dsc, sizeof(float2) * nd);
   }
   if (!r) r = dalloc(s, (void**)&s->d_mass, sizeof(double));
   if (!r) r = dalloc(s, (void**)&s->d_bad, sizeof(int));
@@ -455,8 +461,9 @@ static int enqueue_step(nlse_solver* s) {
     typedef C2<double> T;
     T *psi = (T*)s->psi, *K = (T*)s->K, *ya = (T*)s->ya, *yb = (T*)s->yb;
     const double* V = (const double*)s->V;
-    ExactStageArgs<double> a1{psi, psi, V, K, ya}, a2{ya, psi, V, K, yb}, a3{yb, psi, V, K, ya},
-        a4{ya, psi, V, K, nullptr};
+    T* D = (T*)s->dsc;
+    ExactStageArgs<double> a1{psi, psi, V, K, ya, D}, a2{ya, psi, V, K, yb, D},
+        a3{yb, psi, V, K, ya, D}, a4{ya, psi, V, K, nullptr, D};
     const ExactStageArgs<double>* as[4] = {&a1, &a2, &a3, &a4};
     for (int st = 1; st <= 4 && e == cudaSuccess; ++st)
       e = launch_exact_stage<double>(s->g, p.method, p.bc, s->cd, *as[st - 1], st, s->stream,
@@ -465,8 +472,9 @@ static int enqueue_step(nlse_solver* s) {
     typedef C2<float> T;
     T *psi = (T*)s->psi, *K = (T*)s->K, *ya = (T*)s->ya, *yb = (T*)s->yb;
     const float* V = (const float*)s->V;
-    ExactStageArgs<float> a1{psi, psi, V, K, ya}, a2{ya, psi, V, K, yb}, a3{yb, psi, V, K, ya},
-        a4{ya, psi, V, K, nullptr};
+    T* D = (T*)s->dsc;
+    ExactStageArgs<float> a1{psi, psi, V, K, ya, D}, a2{ya, psi, V, K, yb, D},
+        a3{yb, psi, V, K, ya, D}, a4{ya, psi, V, K, nullptr, D};
     const ExactStageArgs<float>* as[4] = {&a1, &a2, &a3, &a4};
     for (int st = 1; st <= 4 && e == cudaSuccess; ++st)
       e = launch_exact_stage<float>(s->g, p.method, p.bc, s->cf, *as[st - 1], st, s->stream,
@@ -475,11 +483,12 @@ static int enqueue_step(nlse_solver* s) {
     int c = s->cur;
     float4* G = s->gh;
     float2* F = s->fq;
-    MixedStageArgs a1{s->hi[c], s->lo[c], nullptr, s->Vf, s->mK, s->da, nullptr, nullptr, G, F};
-    MixedStageArgs a2{s->hi[c], s->lo[c], s->da, s->Vf, s->mK, s->db, nullptr, nullptr, G, F};
-    MixedStageArgs a3{s->hi[c], s->lo[c], s->db, s->Vf, s->mK, s->da, nullptr, nullptr, G, F};
+    float2* D = (float2*)s->dsc;
+    MixedStageArgs a1{s->hi[c], s->lo[c], nullptr, s->Vf, s->mK, s->da, nullptr, nullptr, G, F, D};
+    MixedStageArgs a2{s->hi[c], s->lo[c], s->da, s->Vf, s->mK, s->db, nullptr, nullptr, G, F, D};
+    MixedStageArgs a3{s->hi[c], s->lo[c], s->db, s->Vf, s->mK, s->da, nullptr, nullptr, G, F, D};
     MixedStageArgs a4{s->hi[c], s->lo[c], s->da, s->Vf, s->mK, nullptr, s->hi[1 - c], s->lo[1 - c],
-                      G, F};
+                      G, F, D};
     const MixedStageArgs* as[4] = {&a1, &a2, &a3, &a4};
     for (int st = 1; st <= 4 && e == cudaSuccess; ++st)
       e = launch_mixed_stage(s->g, p.method, p.bc, s->cf, *as[st - 1], st, s->stream,
@@ -562,7 +571,7 @@ extern "C" int nlse_solver_stream(nlse_solver* s, void** stream) {
 
 extern "C" int nlse_solver_launches_per_step(const nlse_solver* s) {
   if (!s) return 0;
-  if (s->prob.precision != NLSE_PREC_MIXED) return 4;
+  if (s->prob.precision != NLSE_PREC_MIXED) return s->dsc ? 8 : 4;
   // mixed-precision 3D grids on the tiled path: deep-point kernel + shell kernel(s) per stage
   return 4 * mixed_stage_launches(s->g, s->prob.method, s->prob.bc, s->kernel_kind);
 }
@@ -575,10 +584,11 @@ extern "C" long long nlse_solver_bytes_for(const nlse_problem* p) {
   long long b = 0;
   if (p->precision == NLSE_PREC_DOUBLE || p->precision == NLSE_PREC_SINGLE) {
     const long long es = p->precision == NLSE_PREC_DOUBLE ? 8 : 4;
-    b = 4 * 2 * es * n + es * n;
+    b = 4 * 2 * es * n + es * n + 2 * es * exact_dsc_entries(g, p->method, p->bc, kind);
   } else {
     b = 7 * 8 * n + 4 * n + 16 * mixed_ghost_entries(g, p->method, p->bc, kind) +
-        8 * mixed_fq_entries(g, p->method, p->bc, kind);
+        8 * mixed_fq_entries(g, p->method, p->bc, kind) +
+        8 * mixed_dsc_entries(g, p->method, p->bc, kind);
   }
   return b + (long long)sizeof(double) + (long long)sizeof(int) + 3 * 8 * n;
 }

@@ -17,6 +17,7 @@ struct ExactStageArgs {
   const R* V;
   C2<R>* K;
   C2<R>* Yout;       // next stage input (stages 1-3)
+  C2<R>* dsc;        // 2SHOC on the gather path: D scratch (n points), or null
 };
 
 struct MixedStageArgs {
@@ -31,6 +32,7 @@ struct MixedStageArgs {
   // 3D 2SHOC on the tiled path (null otherwise):
   float4* gh;          // ghost values (hi, E) one cell outside each face, mixed_ghost_entries()
   float2* fq;          // F at the points next to a face (n entries, MSD only)
+  float2* dsc;         // 2SHOC on the gather path: D scratch (n points), or null
 };
 
 template <typename R>
@@ -48,6 +50,10 @@ cudaError_t launch_mixed_stage(const Geom& g, int method, int BC, const Consts<f
 int mixed_stage_launches(const Geom& g, int method, int BC, int kernel_kind);
 long long mixed_ghost_entries(const Geom& g, int method, int BC, int kernel_kind);
 long long mixed_fq_entries(const Geom& g, int method, int BC, int kernel_kind);
+// Points of D scratch (ExactStageArgs / MixedStageArgs ::dsc) a 2SHOC stage on
+// the gather path uses (two launches per stage), else 0.
+long long exact_dsc_entries(const Geom& g, int method, int BC, int kernel_kind);
+long long mixed_dsc_entries(const Geom& g, int method, int BC, int kernel_kind);
 
 // Layout conversions and reductions (kern_util.cu).
 cudaError_t planar_to_c2d(const double* re, const double* im, C2<double>* out, long long n,
