@@ -39,6 +39,8 @@
 // or shell3d (CD: gather form).
 #pragma once
 
+#include <type_traits>
+
 #include "kern_gather.cuh"
 #include "kern_tiled.cuh"
 
@@ -208,7 +210,7 @@ __global__ void __launch_bounds__(256, NLSE_WIDE_MIN_BLOCKS) wide3d(
   for (int t = 0; t < 2 * H + P; ++t) issue(pfirst + t, t);
   {
     bool ok = true;
-    if (TMA) {
+    if (TMA && tid == 0) {
 #pragma unroll
       for (int t = 0; t < 2 * H; ++t) ok &= mbar_wait(&bars[t], 0u);
       if (!ok) atomicExch(A.err, NLSE_ERR_TIMEOUT);
@@ -217,98 +219,120 @@ __global__ void __launch_bounds__(256, NLSE_WIDE_MIN_BLOCKS) wide3d(
       drain(pfirst + 2 * H + P - 1);
       return;
     }
+    if (TMA) {
+#pragma unroll
+      for (int t = 0; t < 2 * H; ++t) (void)tiled::mbar_try_wait(&bars[t], 0u);
+    }
 #pragma unroll
     for (int t = 0; t < 2 * H; ++t) q[t] = qload(pfirst + t, t);
     __syncthreads();  // slot 0 is refilled in the first iteration (2SHOC)
   }
 
-  const long long MN = (long long)M * N;
-  const long long pxy = (long long)y * M + x;
-  for (int zb = zs; zb < ze; zb += NU) {
-    const unsigned blk = (unsigned)((zb - zs) / NU) & 1u;
+  // point offsets fit 32 bits (grids have fewer than 2^31 points)
+  const unsigned MN = (unsigned)M * (unsigned)N;
+  const unsigned pxy = (unsigned)y * (unsigned)M + (unsigned)x;
+  // The z loop, instantiated for CTAs whose column touches an x / y face
+  // (EDGE: ghost cells, F next to those faces) and for the others.
+  auto stream = [&](auto edge_tag) {
+    constexpr bool EDGE = decltype(edge_tag)::value;
+    for (int zb = zs; zb < ze; zb += NU) {
+      const unsigned blk = (unsigned)((zb - zs) / NU) & 1u;
 #pragma unroll
-    for (int u = 0; u < NU; ++u) {
-      const int z = zb + u;
-      if (z >= ze) break;
-      const int sc = (u + H) % NU;      // slot of plane z
-      const int sn = (u + 2 * H) % NU;  // slot of plane z+H (queue head)
-      issue(z + H + P, (u + 2 * H + P) % NU);
-      // pointwise operands of the interior point, fetched before the wait
-      const long long p = (long long)z * MN + pxy;
-      float v = 0.f;
-      float2 lo = make_float2(0.f, 0.f), kv = lo;
-      if (inner) {
-        v = A.a.V[p];
-        if (STAGE >= 2) lo = A.a.lo_in[p];
-        if (STAGE == 4) kv = A.a.K[p];
-        // 2SHOC next to an x / y face: write the ghost across that face into
-        // this thread's own halo cell of plane z (slot sc, landed two
-        // iterations ago, refilled two iterations on).  Only this thread
-        // reads that cell (it lies outside the grid, two cells from this
-        // point), so program order makes it visible.
-        if (METHOD == 2 && edge && (x == 1 || x == M - 2 || y == 1 || y == N - 2)) {
-          float2* hpc = hplane(sc);
-          float2* epc = eplane(sc);
-          auto put = [&](int i, float4 gv) {
-            hpc[i] = make_float2(gv.x, gv.y);
-            epc[i] = make_float2(gv.z, gv.w);
-          };
-          if (x == M - 2) put(own + 2, GH[gl.xhi + y + (long long)N * z]);
-          if (x == 1) put(own - 2, GH[gl.xlo + y + (long long)N * z]);
-          if (y == N - 2) put(own + 2 * PX, GH[gl.yhi + x + (long long)M * z]);
-          if (y == 1) put(own - 2 * PX, GH[gl.ylo + x + (long long)M * z]);
-          if (TMA) fence_proxy_async();  // before the slot's next TMA refill
+      for (int u = 0; u < NU; ++u) {
+        const int z = zb + u;
+        if (z >= ze) break;
+        const int sc = (u + H) % NU;      // slot of plane z
+        const int sn = (u + 2 * H) % NU;  // slot of plane z+H (queue head)
+        issue(z + H + P, (u + 2 * H + P) % NU);
+        // pointwise operands of the interior point, fetched before the wait
+        const unsigned p = (unsigned)z * MN + pxy;
+        float v = 0.f;
+        float2 lo = make_float2(0.f, 0.f), kv = lo;
+        if (inner) {
+          v = A.a.V[p];
+          if (STAGE >= 2) lo = A.a.lo_in[p];
+          if (STAGE == 4) kv = A.a.K[p];
+          // 2SHOC next to an x / y face: write the ghost across that face
+          // into this thread's own halo cell of plane z (slot sc, landed two
+          // iterations ago, refilled two iterations on).  Only this thread
+          // reads that cell (it lies outside the grid, two cells from this
+          // point), so program order makes it visible.
+          if (METHOD == 2 && EDGE && (x == 1 || x == M - 2 || y == 1 || y == N - 2)) {
+            float2* hpc = hplane(sc);
+            float2* epc = eplane(sc);
+            auto put = [&](int i, float4 gv) {
+              hpc[i] = make_float2(gv.x, gv.y);
+              epc[i] = make_float2(gv.z, gv.w);
+            };
+            if (x == M - 2) put(own + 2, GH[gl.xhi + y + (long long)N * z]);
+            if (x == 1) put(own - 2, GH[gl.xlo + y + (long long)N * z]);
+            if (y == N - 2) put(own + 2 * PX, GH[gl.yhi + x + (long long)M * z]);
+            if (y == 1) put(own - 2 * PX, GH[gl.ylo + x + (long long)M * z]);
+            if (TMA) fence_proxy_async();  // before the slot's next TMA refill
+          }
         }
-      }
-      bool ok = true;
-      if (TMA) {
-        ok = mbar_wait(&bars[sn], blk ^ (unsigned)((u + 2 * H) / NU));
-        if (!ok) atomicExch(A.err, NLSE_ERR_TIMEOUT);
-      }
-      if (__syncthreads_or(!ok)) {
-        drain(z + H + P);
-        return;
-      }
-      q[sn] = qload(z + H, sn);
+        // one thread waits for the queue-head plane (bounded); the barrier
+        // releases the rest, and each thread then takes the completed phase
+        // with one try_wait (succeeds at once; acquires the TMA writes)
+        const unsigned par = blk ^ (unsigned)((u + 2 * H) / NU);
+        bool ok = true;
+        if (TMA && tid == 0) {
+          ok = mbar_wait(&bars[sn], par);
+          if (!ok) atomicExch(A.err, NLSE_ERR_TIMEOUT);
+        }
+        if (__syncthreads_or(!ok)) {
+          drain(z + H + P);
+          return;
+        }
+        if (TMA) (void)tiled::mbar_try_wait(&bars[sn], par);
+        q[sn] = qload(z + H, sn);
 
-      if (inner) {
-        const float2* hp = hplane(sc);
-        const float2* ep = eplane(sc);
-        const HE& u0 = q[sc];
-        float2 T;
-        if (METHOD == 1) {
-          HE nb[6] = {q[(sc + 1) % NU],           q[(sc + NU - 1) % NU],
-                      {hp[own + PX], ep[own + PX]}, {hp[own - PX], ep[own - PX]},
-                      {hp[own + 1], ep[own + 1]},   {hp[own - 1], ep[own - 1]}};
-          T = mixed::f_interior_cd<3>(A.c, u0, v, nb);
-        } else {
-          HE fn[6] = {q[(sc + 1) % NU],           q[(sc + NU - 1) % NU],
-                      {hp[own + PX], ep[own + PX]}, {hp[own - PX], ep[own - PX]},
-                      {hp[own + 1], ep[own + 1]},   {hp[own - 1], ep[own - 1]}};
-          HE f2n[6] = {q[(sc + 2) % NU],
-                       q[(sc + NU - 2) % NU],
-                       {hp[own + 2 * PX], ep[own + 2 * PX]},
-                       {hp[own - 2 * PX], ep[own - 2 * PX]},
-                       {hp[own + 2], ep[own + 2]},
-                       {hp[own - 2], ep[own - 2]}};
-          T = mixed::f_wide_2shoc<3>(A.c, u0, v, fn, f2n);
-          // F next to a face, for the MSD formula of the face points
-          if (A.a.fq && (x == 1 || x == M - 2 || y == 1 || y == N - 2 || z == 1 || z == L - 2))
-            A.a.fq[p] = T;
-        }
-        if (STAGE == 1) lo = u0.e;
-        float2 eo, ko, ho, lo2;
-        mixed::stage_update(A.c, STAGE, T, u0.h, lo, u0.e, kv, eo, ko, ho, lo2);
-        if (STAGE == 2) A.a.K[p] = ko;
-        if (STAGE < 4) {
-          A.a.e_out[p] = eo;
-        } else {
-          A.a.hi_out[p] = ho;
-          A.a.lo_out[p] = lo2;
+        if (inner) {
+          const float2* hp = hplane(sc);
+          const float2* ep = eplane(sc);
+          const HE& u0 = q[sc];
+          float2 T;
+          if (METHOD == 1) {
+            HE nb[6] = {q[(sc + 1) % NU],           q[(sc + NU - 1) % NU],
+                        {hp[own + PX], ep[own + PX]}, {hp[own - PX], ep[own - PX]},
+                        {hp[own + 1], ep[own + 1]},   {hp[own - 1], ep[own - 1]}};
+            T = mixed::f_interior_cd<3>(A.c, u0, v, nb);
+          } else {
+            HE fn[6] = {q[(sc + 1) % NU],           q[(sc + NU - 1) % NU],
+                        {hp[own + PX], ep[own + PX]}, {hp[own - PX], ep[own - PX]},
+                        {hp[own + 1], ep[own + 1]},   {hp[own - 1], ep[own - 1]}};
+            HE f2n[6] = {q[(sc + 2) % NU],
+                         q[(sc + NU - 2) % NU],
+                         {hp[own + 2 * PX], ep[own + 2 * PX]},
+                         {hp[own - 2 * PX], ep[own - 2 * PX]},
+                         {hp[own + 2], ep[own + 2]},
+                         {hp[own - 2], ep[own - 2]}};
+            T = mixed::f_wide_2shoc<3>(A.c, u0, v, fn, f2n);
+            // F next to a face, for the MSD formula of the face points
+            if (A.a.fq) {
+              const bool nz = z == 1 || z == L - 2;
+              if (EDGE ? (nz || x == 1 || x == M - 2 || y == 1 || y == N - 2) : nz)
+                A.a.fq[p] = T;
+            }
+          }
+          if (STAGE == 1) lo = u0.e;
+          float2 eo, ko, ho, lo2;
+          mixed::stage_update(A.c, STAGE, T, u0.h, lo, u0.e, kv, eo, ko, ho, lo2);
+          if (STAGE == 2) A.a.K[p] = ko;
+          if (STAGE < 4) {
+            A.a.e_out[p] = eo;
+          } else {
+            A.a.hi_out[p] = ho;
+            A.a.lo_out[p] = lo2;
+          }
         }
       }
     }
-  }
+  };
+  if (edge)
+    stream(std::integral_constant<bool, true>());
+  else
+    stream(std::integral_constant<bool, false>());
 }
 
 // ---- shell enumeration ------------------------------------------------------
@@ -504,30 +528,20 @@ inline int sm_count() {
   return n;
 }
 
-// z chunk length.  CTAs of a stage all cost about (chunk + 2H) plane steps
-// (the chunk plus the queue fill), and the block scheduler hands them to SMs
-// as slots free up, so the stage takes about
-//   ceil(CTAs / SMs) * (ceil(L / chunks) + 2H)
-// plane steps; chunks are chosen to minimise that while giving every SM at
-// least `occ` resident CTAs.
+// z chunk length: short enough that a stage runs at least 8 waves of
+// resident CTAs (measured at 320^3 with 4 CTAs per SM: chunks of 16-32
+// planes ran 12-14% faster than the 2-3 waves a load-balance model
+// prefers), and at least 16 planes so the 2H-plane queue fill stays small.
 inline int default_zc(const Geom& g, int H, int occ) {
+  (void)H;
   const long long cols = (long long)((g.M + 31) / 32) * ((g.N + 7) / 8);
-  const long long nsm = sm_count();
-  long long best_cost = -1;
-  int best = g.L;
-  for (int nbz = 1; nbz <= g.L; ++nbz) {
-    const int zc = (g.L + nbz - 1) / nbz;
-    if (nbz > 1 && zc == (g.L + nbz - 2) / (nbz - 1)) continue;  // same chunk length
-    if (zc < 4) break;
-    const long long ctas = cols * ((g.L + zc - 1) / zc);
-    long long cost = (ctas + nsm - 1) / nsm * (zc + 2 * H);
-    if (ctas < nsm * occ) cost = cost * 4;  // too few CTAs to hide latency
-    if (best_cost < 0 || cost < best_cost) {
-      best_cost = cost;
-      best = zc;
-    }
-  }
-  return best;
+  const long long want = 8LL * sm_count() * (occ > 0 ? occ : 1);
+  long long nbz = (want + cols - 1) / cols;
+  if (nbz < 1) nbz = 1;
+  int zc = (int)((g.L + nbz - 1) / nbz);
+  if (zc < 16) zc = 16;
+  if (zc > g.L) zc = g.L;
+  return zc;
 }
 
 template <int METHOD, int STAGE, bool TMA>
