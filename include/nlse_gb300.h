@@ -262,6 +262,25 @@ int nlse_tune_get(const char *key, long long *value);
  * (src/NLSEmagic3D/NLSEmagic3D.m:154-163). */
 double nlse_linear_stability_k(int ndim, int method, double h, double a);
 
+/* ------------------------------------------------------------------------
+ * 3D vorticity of a wavefunction (post-chunk analysis).  Replaces the MEX
+ * function [w_x,w_y,w_z,W] = rmc_vorticity3D(U, 1/(h*2), veps)
+ * (src/NLSEmagic3D/rmc_vorticity3D.c:1-19, 24-354): v = Im(conj(U) grad U) /
+ * (2|U|^2 + veps), w = curl v, W = |w|, FP64, the reference's difference
+ * rules (one-sided on the faces).  Edge and corner points, where the
+ * reference computes no gradient, give 0.
+ * ------------------------------------------------------------------------ */
+/* Host arrays, MATLAB layout: dims = {M, N, L} (first index fastest); Ui may be
+ * NULL (real U); lh2 = 1/(2h). */
+int nlse_vorticity3d(const double *Ur, const double *Ui, const long long *dims, double lh2,
+                     double veps, double *wx, double *wy, double *wz, double *W);
+/* From a resident 3D solve's current state (any precision class, taken as
+ * FP64), into device buffers of n doubles each, on the solver's stream;
+ * lh2 = 1/(2 sqrt(h2)).  No reference counterpart (the reference copies U
+ * back to MATLAB first). */
+int nlse_solver_vorticity(nlse_solver *s, double veps, double *d_wx, double *d_wy, double *d_wz,
+                          double *d_W);
+
 #ifdef __cplusplus
 }
 #endif

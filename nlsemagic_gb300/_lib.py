@@ -74,6 +74,9 @@ SIGNATURES = {
     "nlse_solver_launches_per_step": (_i, [_vp]),
     "nlse_solver_device_bytes": (_ll, [_vp]),
     "nlse_solver_bytes_for": (_ll, [ctypes.POINTER(Problem)]),
+    "nlse_vorticity3d": (_i, [_dp, _dp, ctypes.POINTER(_ll), ctypes.c_double, ctypes.c_double,
+                              _dp, _dp, _dp, _dp]),
+    "nlse_solver_vorticity": (_i, [_vp, ctypes.c_double, _vp, _vp, _vp, _vp]),
     "nlse_batch_create": (_i, [_ll, _i, ctypes.POINTER(_vp)]),
     "nlse_batch_destroy": (_i, [_vp]),
     "nlse_batch_bytes_for": (_ll, [ctypes.POINTER(Problem)]),

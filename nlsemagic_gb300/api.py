@@ -154,6 +154,20 @@ class Solver:
         check(self._lib.nlse_solver_create(ctypes.byref(self.problem), ctypes.byref(h)))
         self._h = h
 
+    def vorticity(self, veps=1e-10):
+        """Vorticity (wx, wy, wz, W) of the current 3D state, computed on the
+        device from the resident state; returned as numpy arrays of the grid
+        shape (the device buffers come from torch, used only as an
+        allocator)."""
+        import torch
+        if self.ndim != 3:
+            raise ValueError("vorticity needs a 3D solve")
+        bufs = [torch.empty(self.n, dtype=torch.float64, device="cuda") for _ in range(4)]
+        check(self._lib.nlse_solver_vorticity(self._h, float(veps),
+                                              *(ctypes.c_void_p(b.data_ptr()) for b in bufs)))
+        self.sync()
+        return tuple(b.cpu().numpy().reshape(self.shape, order="F") for b in bufs)
+
     @staticmethod
     def bytes_for(shape, method=2, precision=PREC_MIXED, BC=1, flags=FLAG_MSD_GUARD):
         """Device bytes a solver of this shape and class holds after a host upload."""
@@ -320,3 +334,28 @@ class Batch:
     @property
     def last_launches(self):
         return int(self._lib.nlse_batch_last_launches(self._h))
+
+
+# ---------------------------------------------------------------------------
+# 3D vorticity (post-chunk analysis)
+# ---------------------------------------------------------------------------
+def rmc_vorticity3D(U, lh2, veps):
+    """[w_x, w_y, w_z, W] = rmc_vorticity3D(U, 1/(h*2), veps) on the GPU
+    (src/NLSEmagic3D/rmc_vorticity3D.c:12-16): U MATLAB-shaped (M, N, L),
+    complex or real.  Returns four real arrays of U's shape."""
+    U = np.asarray(U)
+    if U.ndim != 3:
+        raise ValueError("rmc_vorticity3D needs a 3D array")
+    re = np.ascontiguousarray(np.real(U).ravel(order="F"), dtype=np.float64)
+    im = (np.ascontiguousarray(np.imag(U).ravel(order="F"), dtype=np.float64)
+          if np.iscomplexobj(U) else None)
+    dims = (ctypes.c_longlong * 3)(*(int(d) for d in U.shape))
+    outs = [np.empty(U.size) for _ in range(4)]
+    check(load().nlse_vorticity3d(_ptr(re), _ptr(im) if im is not None else None, dims,
+                                  float(lh2), float(veps), *(_ptr(o) for o in outs)))
+    return tuple(o.reshape(U.shape, order="F") for o in outs)
+
+
+def vorticity3d(U, h, veps=1e-10):
+    """Vorticity of U on a grid of spacing h: rmc_vorticity3D(U, 1/(2h), veps)."""
+    return rmc_vorticity3D(U, 1.0 / (2.0 * h), veps)

@@ -33,6 +33,7 @@ UNITS = {
     "nlse_abi.cu": [],
     "nlse_batch.cu": ["-fmad=false"],
     "nlse_noalloc.cu": [],
+    "kern_vort.cu": ["-fmad=false"],
 }
 
 

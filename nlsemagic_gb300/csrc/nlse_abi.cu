@@ -247,6 +247,7 @@ struct nlse_solver {
   int cur;
   // device staging for planar transfers: re, im, V (n doubles each)
   double* stage;
+  double* vort;  // vorticity scratch (3 n doubles), allocated on first use
   double* d_mass;
   int* d_bad;
   // graphs
@@ -289,7 +290,7 @@ extern "C" int nlse_solver_destroy(nlse_solver* s) {
   free_graphs(s);
   void* ptrs[] = {s->psi, s->K, s->ya, s->yb, s->V, s->hi[0], s->hi[1], s->lo[0], s->lo[1],
                   s->mK, s->da, s->db, s->fq, s->gh, s->Vf, s->stage, s->d_mass, s->d_bad,
-                  s->dsc};
+                  s->dsc, s->vort};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -785,4 +786,97 @@ extern "C" int NLSE3D_TAKE_STEPS_CUDA_MIXED(const double* Uoldr, const double* U
                                             double k, int L, int N, int M, int method) {
   nlse_problem p = mkprob(3, M, N, L, method, NLSE_PREC_MIXED, BC, s, a, h2, k);
   return nlse_take_steps(&p, Uoldr, Uoldi, V, Unewr, Unewi, chunk_size);
+}
+
+// ---------------------------------------------------------------------------
+// 3D vorticity (post-chunk analysis; src/NLSEmagic3D/rmc_vorticity3D.c)
+// ---------------------------------------------------------------------------
+static int vort_dims(const long long* dims, int* M, int* N, int* L) {
+  if (!dims) return fail(NLSE_ERR_ARG, "dims is NULL");
+  long long n = 1;
+  for (int d = 0; d < 3; ++d) {
+    if (dims[d] < 3) return fail(NLSE_ERR_ARG, "dimension %d is %lld; at least 3 points are needed", d, dims[d]);
+    n *= dims[d];
+    if (n > (1LL << 31) - 1) return fail(NLSE_ERR_CAPACITY, "grid has more than 2^31-1 points");
+  }
+  *M = (int)dims[0];
+  *N = (int)dims[1];
+  *L = (int)dims[2];
+  return NLSE_OK;
+}
+
+namespace {
+struct VortCache {
+  int device = -1;
+  long long cap = 0;  // points
+  double* buf = nullptr;  // Ur, Ui, v (3), outputs (4): 9 n doubles
+  cudaStream_t stream = nullptr;
+  ~VortCache() {
+    if (buf) cudaFree(buf);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+thread_local VortCache t_vort;
+}  // namespace
+
+extern "C" int nlse_vorticity3d(const double* Ur, const double* Ui, const long long* dims,
+                                double lh2, double veps, double* wx, double* wy, double* wz,
+                                double* W) {
+  int M, N, L;
+  int rc = vort_dims(dims, &M, &N, &L);
+  if (rc) return rc;
+  if (!Ur || !wx || !wy || !wz || !W) return fail(NLSE_ERR_ARG, "NULL array argument");
+  if (!isfinite(lh2) || !isfinite(veps)) return fail(NLSE_ERR_ARG, "lh2 and veps must be finite");
+  const long long n = (long long)M * N * L;
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  VortCache& c = t_vort;
+  if (c.device != dev || c.cap < n) {
+    if (c.buf) cudaFree(c.buf);
+    c.buf = nullptr;
+    c.cap = 0;
+    if (c.stream && c.device != dev) {
+      cudaStreamDestroy(c.stream);
+      c.stream = nullptr;
+    }
+    c.device = dev;
+    CUDA_TRY(cudaMalloc(&c.buf, sizeof(double) * 9 * n));
+    c.cap = n;
+    if (!c.stream) CUDA_TRY(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+  }
+  double *dr = c.buf, *di = c.buf + n, *dv = c.buf + 2 * n, *dw = c.buf + 5 * n;
+  const size_t b = sizeof(double) * n;
+  CUDA_TRY(cudaMemcpyAsync(dr, Ur, b, cudaMemcpyHostToDevice, c.stream));
+  if (Ui)
+    CUDA_TRY(cudaMemcpyAsync(di, Ui, b, cudaMemcpyHostToDevice, c.stream));
+  else
+    CUDA_TRY(cudaMemsetAsync(di, 0, b, c.stream));
+  CUDA_TRY(launch_vorticity(M, N, L, dr, di, lh2, veps, dv, dw, dw + n, dw + 2 * n, dw + 3 * n,
+                            c.stream));
+  double* outs[4] = {wx, wy, wz, W};
+  for (int t = 0; t < 4; ++t)
+    CUDA_TRY(cudaMemcpyAsync(outs[t], dw + t * n, b, cudaMemcpyDeviceToHost, c.stream));
+  CUDA_TRY(cudaStreamSynchronize(c.stream));
+  return NLSE_OK;
+}
+
+extern "C" int nlse_solver_vorticity(nlse_solver* s, double veps, double* d_wx, double* d_wy,
+                                     double* d_wz, double* d_W) {
+  if (!s || !d_wx || !d_wy || !d_wz || !d_W) return fail(NLSE_ERR_ARG, "NULL argument");
+  if (s->g.ndim != 3) return fail(NLSE_ERR_ARG, "vorticity needs a 3D solve");
+  if (!isfinite(veps)) return fail(NLSE_ERR_ARG, "veps must be finite");
+  CUDA_TRY(cudaSetDevice(s->device));
+  int r = ensure_stage(s);
+  if (r) return r;
+  const long long n = s->g.n;
+  if (!s->vort) {
+    r = dalloc(s, (void**)&s->vort, sizeof(double) * 3 * n);
+    if (r) return r;
+  }
+  r = emit(s, s->stage, s->stage + n);  // the state as planar doubles
+  if (r) return r;
+  const double lh2 = 1.0 / (2.0 * sqrt(s->prob.h2));
+  CUDA_TRY(launch_vorticity(s->g.M, s->g.N, s->g.L, s->stage, s->stage + n, lh2, veps, s->vort,
+                            d_wx, d_wy, d_wz, d_W, s->stream));
+  return NLSE_OK;
 }

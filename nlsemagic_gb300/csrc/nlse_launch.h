@@ -80,6 +80,12 @@ cudaError_t mass_hilo(const float2* hi, const float2* lo, long long n, double* o
 
 bool tiled_supported(const Geom& g, int dim);
 
+// 3D vorticity (kern_vort.cu): planar FP64 U of M x N x L points -> wx, wy,
+// wz, W; vscratch holds 3 n doubles.
+cudaError_t launch_vorticity(int M, int N, int L, const double* Ur, const double* Ui, double lh2,
+                             double veps, double* vscratch, double* wx, double* wy, double* wz,
+                             double* W, cudaStream_t st);
+
 // Device error word of the tiled kernels (bounded-wait timeouts, self-check
 // failures): take_device_error() returns and clears it.
 namespace tiled {

@@ -117,3 +117,45 @@ def ref_take_steps(U, V, s, a, h2, BC, chunk, k, method=1, precision=2):
     if rc != 0:
         raise RuntimeError("reference call failed (code %d)" % rc)
     return (outr + 1j * outi).reshape(U.shape, order="F")
+
+
+def vorticity3d(U, lh2, veps):
+    """C restatement of the 3D vorticity routine: U MATLAB-shaped (M, N, L),
+    lh2 = 1/(2h).  Returns (wx, wy, wz, W), each real of U's shape."""
+    U = np.asarray(U)
+    if U.ndim != 3:
+        raise ValueError("vorticity3d needs a 3D array")
+    M, N, L = (int(d) for d in U.shape)
+    Ur, Ui, _ = _planes(U, np.zeros(U.shape))
+    lib = _load_port()
+    f = lib.nlse_oracle_vorticity3d
+    f.restype = None
+    f.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp, ctypes.c_double,
+                  ctypes.c_double, _dp, _dp, _dp, _dp]
+    outs = [np.empty(U.size) for _ in range(4)]
+    f(M, N, L, _ptr(Ur), _ptr(Ui), float(lh2), float(veps), *(_ptr(o) for o in outs))
+    return tuple(o.reshape(U.shape, order="F") for o in outs)
+
+
+def ref_vorticity3d(U, lh2, veps):
+    """The reference's own rmc_vorticity3D MEX function (via the shim)."""
+    U = np.asarray(U)
+    if "rmc_vorticity3D" not in _refs:
+        libs = _build.build_ref()
+        if "rmc_vorticity3D" not in libs:
+            raise RuntimeError("reference vorticity routine is not available here")
+        lib = ctypes.CDLL(libs["rmc_vorticity3D"], mode=ctypes.RTLD_LOCAL)
+        f = lib.mex_call_vorticity
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.POINTER(ctypes.c_longlong), _dp, _dp, ctypes.c_double,
+                      ctypes.c_double, _dp, _dp, _dp, _dp]
+        _refs["rmc_vorticity3D"] = lib
+    lib = _refs["rmc_vorticity3D"]
+    Ur, Ui, _ = _planes(U, np.zeros(U.shape))
+    cd = (ctypes.c_longlong * 3)(*(int(d) for d in U.shape))
+    outs = [np.empty(U.size) for _ in range(4)]
+    rc = lib.mex_call_vorticity(cd, _ptr(Ur), _ptr(Ui) if np.iscomplexobj(U) else None,
+                                float(lh2), float(veps), *(_ptr(o) for o in outs))
+    if rc != 0:
+        raise RuntimeError("reference vorticity call failed (code %d)" % rc)
+    return tuple(o.reshape(U.shape, order="F") for o in outs)

@@ -165,3 +165,43 @@ int ref_take_steps(int ndims, const long long *dims, const double *Ur, const dou
     return mex_call_take_steps(ndims, dims, Ur, Ui, V, s, a, h2, BC, chunk, k, 0, 0, 8, out_r,
                                out_i);
 }
+
+/*
+ * [wx, wy, wz, W] = rmc_vorticity3D(U, lh2, veps) through the mexFunction
+ * linked into this shared object.  dims = {M, N, L} (first index fastest).
+ * Returns 0 on success, -2 if an output is missing, -3 on a MATLAB error.
+ */
+int mex_call_vorticity(const long long *dims, const double *Ur, const double *Ui, double lh2,
+                       double veps, double *wx, double *wy, double *wz, double *W) {
+    mwSize d[3];
+    mwSize n, i;
+    mxArray *prhs[3];
+    mxArray *plhs[4];
+    double *outs[4];
+    for (i = 0; i < 3; ++i) d[i] = (mwSize)dims[i];
+    prhs[0] = make_array(3, d, Ui ? mxCOMPLEX : mxREAL);
+    n = numel(prhs[0]);
+    memcpy(prhs[0]->pr, Ur, n * sizeof(double));
+    if (Ui) memcpy(prhs[0]->pi, Ui, n * sizeof(double));
+    prhs[1] = make_scalar(lh2);
+    prhs[2] = make_scalar(veps);
+    for (i = 0; i < 4; ++i) plhs[i] = NULL;
+    g_mex_error = 0;
+    mexFunction(4, plhs, 3, (const mxArray **)prhs);
+    outs[0] = wx;
+    outs[1] = wy;
+    outs[2] = wz;
+    outs[3] = W;
+    for (i = 0; i < 4; ++i) {
+        if (!plhs[i]) {
+            for (i = 0; i < 3; ++i) free_array(prhs[i]);
+            return -2;
+        }
+    }
+    for (i = 0; i < 4; ++i) {
+        memcpy(outs[i], plhs[i]->pr, n * sizeof(double));
+        free_array(plhs[i]);
+    }
+    for (i = 0; i < 3; ++i) free_array(prhs[i]);
+    return g_mex_error ? -3 : 0;
+}

@@ -157,3 +157,100 @@ int nlse_oracle_1d(const double *Ur, const double *Ui, const double *V, double *
     return nlse_oracle_take_steps(1, method, precision, dims, Ur, Ui, V, s, a, h2, BC, chunk, k,
                                   out_r, out_i, flags);
 }
+
+/* ------------------------------------------------------------------------
+ * 3D vorticity of a wavefunction (post-chunk analysis), FP64:
+ *   v = Im(conj(U) grad U) / (2|U|^2 + veps),  w = curl v,  W = |w|,
+ * restating src/NLSEmagic3D/rmc_vorticity3D.c:24-354.  lh2 = 1/(2h).
+ * Axes follow that file: "x" is the slowest index i (0..L-1), "y" the middle
+ * index j (0..N-1), "z" the fastest index k (0..M-1); p = (i*N + j)*M + k.
+ * Derivatives (of U, then of v), per point class:
+ *   interior (i, j, k all inner): central  lh2*(f(+1) - f(-1)) on all axes;
+ *   x face (i = 0 / L-1, j, k inner): x one-sided (2 lh2)*(f(1)-f(0)) or
+ *       (2 lh2)*(f(L-1)-f(L-2)), y and z central;
+ *   y face (j = 0 / N-1, i, k inner): y one-sided; x one-sided FORWARD in i
+ *       (as the reference does on the y and z faces); z central;
+ *   z face (k = 0 / M-1, i, j inner): z one-sided; x forward; y central.
+ * Edge and corner points get no gradient in the reference (its arrays there
+ * are left uninitialised); here they are 0, which makes v there 0, and the
+ * outputs w, W there are 0 as in the reference.
+ * ------------------------------------------------------------------------ */
+enum { VC_INT = 0, VC_FX = 1, VC_FY = 2, VC_FZ = 3, VC_EDGE = 4 };
+
+static int vclass(int M, int N, int L, int i, int j, int k) {
+    int bx = (i == 0 || i == L - 1), by = (j == 0 || j == N - 1), bz = (k == 0 || k == M - 1);
+    if (bx + by + bz == 0) return VC_INT;
+    if (bx + by + bz > 1) return VC_EDGE;
+    return bx ? VC_FX : (by ? VC_FY : VC_FZ);
+}
+
+/* derivative of f along one axis at p; stride st, coordinate c of extent n;
+ * mode 0 central, 1 one-sided (forward at c = 0, backward at c = n-1),
+ * 2 forward one-sided */
+static double vderiv(const double *f, long long p, long long st, int c, int n, double lh2,
+                     int mode) {
+    if (mode == 0) return lh2 * (f[p + st] - f[p - st]);
+    if (mode == 2 || c == 0) return (lh2 * 2) * (f[p + st] - f[p]);
+    (void)n;
+    return (lh2 * 2) * (f[p] - f[p - st]);
+}
+
+void nlse_oracle_vorticity3d(int M, int N, int L, const double *Ur, const double *Ui, double lh2,
+                             double veps, double *wx, double *wy, double *wz, double *W) {
+    const long long n = (long long)M * N * L, sx = (long long)M * N, sy = M, sz = 1;
+    double *v = (double *)calloc((size_t)(3 * n), sizeof(double));
+    double *vx = v, *vy = v + n, *vz = v + 2 * n;
+    int i, j, k;
+    for (i = 0; i < L; ++i)
+        for (j = 0; j < N; ++j)
+            for (k = 0; k < M; ++k) {
+                const long long p = ((long long)i * N + j) * M + k;
+                const int cls = vclass(M, N, L, i, j, k);
+                double gxr = 0, gxi = 0, gyr = 0, gyi = 0, gzr = 0, gzi = 0, l;
+                if (cls != VC_EDGE) {
+                    const int mx = cls == VC_INT ? 0 : (cls == VC_FX ? 1 : 2);
+                    const int my = cls == VC_FY ? 1 : 0;
+                    const int mz = cls == VC_FZ ? 1 : 0;
+                    gxr = vderiv(Ur, p, sx, i, L, lh2, mx);
+                    gxi = vderiv(Ui, p, sx, i, L, lh2, mx);
+                    gyr = vderiv(Ur, p, sy, j, N, lh2, my);
+                    gyi = vderiv(Ui, p, sy, j, N, lh2, my);
+                    gzr = vderiv(Ur, p, sz, k, M, lh2, mz);
+                    gzi = vderiv(Ui, p, sz, k, M, lh2, mz);
+                }
+                l = 1 / (2 * Ur[p] * Ur[p] + 2 * Ui[p] * Ui[p] + veps);
+                vx[p] = (Ur[p] * gxi - Ui[p] * gxr) * l;
+                vy[p] = (Ur[p] * gyi - Ui[p] * gyr) * l;
+                vz[p] = (Ur[p] * gzi - Ui[p] * gzr) * l;
+            }
+    for (i = 0; i < L; ++i)
+        for (j = 0; j < N; ++j)
+            for (k = 0; k < M; ++k) {
+                const long long p = ((long long)i * N + j) * M + k;
+                const int cls = vclass(M, N, L, i, j, k);
+                double vzx, vyx, vzy, vxy, vyz, vxz, a, b, c;
+                if (cls == VC_EDGE) {
+                    wx[p] = wy[p] = wz[p] = W[p] = 0;
+                    continue;
+                }
+                {
+                    const int mx = cls == VC_INT ? 0 : (cls == VC_FX ? 1 : 2);
+                    const int my = cls == VC_FY ? 1 : 0;
+                    const int mz = cls == VC_FZ ? 1 : 0;
+                    vzx = vderiv(vz, p, sx, i, L, lh2, mx);
+                    vyx = vderiv(vy, p, sx, i, L, lh2, mx);
+                    vzy = vderiv(vz, p, sy, j, N, lh2, my);
+                    vxy = vderiv(vx, p, sy, j, N, lh2, my);
+                    vyz = vderiv(vy, p, sz, k, M, lh2, mz);
+                    vxz = vderiv(vx, p, sz, k, M, lh2, mz);
+                }
+                a = vzy - vyz;
+                b = vxz - vzx;
+                c = vyx - vxy;
+                wx[p] = a;
+                wy[p] = b;
+                wz[p] = c;
+                W[p] = sqrt(a * a + b * b + c * c);
+            }
+    free(v);
+}

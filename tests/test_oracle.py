@@ -143,3 +143,59 @@ def test_mass_conserved_and_grey_soliton_tracks_closed_form():
     inner = slice(200, 824)
     err = np.max(np.abs(out[inner] - exact[inner]))
     assert err < 5e-3, err
+
+
+# ---- 3D vorticity (src/NLSEmagic3D/rmc_vorticity3D.c) --------------------------
+VORT_SHAPES = [(5, 6, 7), (9, 8, 10), (3, 3, 3), (12, 5, 4), (40, 33, 21)]
+
+
+@pytest.mark.parametrize("shape", VORT_SHAPES)
+def test_vorticity_oracle_matches_reference(shape):
+    if not oracle.ref_available():
+        pytest.skip("reference checkout not present")
+    rng = np.random.default_rng(sum(shape))
+    U = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    U[1, 1, 1] = 0.0  # veps keeps |U| = 0 finite
+    lh2, veps = 1.0 / (2 * 0.3), 1e-6
+    got = oracle.vorticity3d(U, lh2, veps)
+    want = oracle.ref_vorticity3d(U, lh2, veps)
+    M, N, L = shape
+    interior = np.zeros(shape, bool)
+    interior[1:M - 1, 1:N - 1, 1:L - 1] = True
+    for g, w in zip(got, want):
+        # interior points never read the reference's uninitialised edge
+        # gradients: bit-identical
+        assert np.array_equal(g[interior], w[interior])
+        # the edges and corners are 0 in both
+        edge = np.zeros(shape, bool)
+        for a in range(3):
+            for b in range(a + 1, 3):
+                sl = [slice(None)] * 3
+                for ia in (0, shape[a] - 1):
+                    for ib in (0, shape[b] - 1):
+                        sl[a], sl[b] = ia, ib
+                        edge[tuple(sl)] = True
+        assert np.all(g[edge] == 0) and np.all(w[edge] == 0)
+    if U.size >= 16384:
+        # large enough that the reference's scratch comes from freshly mapped
+        # (zeroed) memory: its edge gradients are 0 as here, every point agrees
+        for g, w in zip(got, want):
+            assert np.array_equal(g, w)
+
+
+def test_vorticity_of_a_straight_vortex_line():
+    # U = (x + i y)/r-like charge-1 line along the slowest axis: the vorticity
+    # points along that axis and its magnitude integrates to ~2 pi / |v| scale
+    h = 0.25
+    n = 24
+    ax = (np.arange(n) - (n - 1) / 2) * h
+    Z, Y, X = np.meshgrid(ax, ax, ax, indexing="ij")  # fastest first: (k, j, i)
+    # in the routine's axes: x = slowest (i), y = middle (j), z = fastest (k);
+    # a line along x winds in the (y, z) plane
+    U = np.tanh(np.hypot(Y, Z)) * np.exp(1j * np.arctan2(Y, Z))
+    wx, wy, wz, W = oracle.vorticity3d(U, 1 / (2 * h), 1e-12)
+    core = W[n // 2 - 2:n // 2 + 2, n // 2 - 2:n // 2 + 2, n // 2]
+    far = W[2, 2, n // 2]
+    assert core.max() > 10 * far
+    mid = (slice(3, n - 3),) * 3
+    assert np.abs(wx[mid]).max() > 5 * max(np.abs(wy[mid]).max(), np.abs(wz[mid]).max())
