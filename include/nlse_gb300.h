@@ -281,6 +281,52 @@ int nlse_vorticity3d(const double *Ur, const double *Ui, const long long *dims, 
 int nlse_solver_vorticity(nlse_solver *s, double veps, double *d_wx, double *d_wy, double *d_wz,
                           double *d_W);
 
+/* ------------------------------------------------------------------------
+ * Initial conditions generated on the device, and per-chunk diagnostics
+ * (the initial data and the analysis the MATLAB drivers compute on the host
+ * every frame: src/NLSEmagic1D/NLSEmagic1D_FRS.m:211-225 and :521-595).
+ * No reference C counterpart.
+ * ------------------------------------------------------------------------ */
+#define NLSE_IC_SECH 1     /* 1D bright: sqrt(2om/s) sech(sqrt(om/a)(x-x0)) e^{i c x/(2a)} */
+#define NLSE_IC_TANH 2     /* 1D dark: sqrt(om/s) tanh(sqrt(|om/(2a)|)(x-x0)) e^{i c x/(2a)} */
+#define NLSE_IC_GAUSS 3    /* 1D linear: exp(-x^2/(2a)), V = x^2/a */
+#define NLSE_IC_GREY 4     /* 1D co-moving grey soliton (om < 0) */
+#define NLSE_IC_VORTICES 5 /* 2D: prod_j tanh(r_j) e^{i q_j theta_j} */
+#define NLSE_IC_RINGS 6    /* 3D: sqrt(max(0,1-V)) prod_j tanh(d_j) e^{i phi_j}, V = omega^2 r^2/2 */
+#define NLSE_NOISE_NONE 0
+#define NLSE_NOISE_ADD 1   /* psi += noise (g1 + i g2) */
+#define NLSE_NOISE_PHASE 2 /* psi *= exp(i noise g1) */
+
+typedef struct nlse_ic {
+  int kind;             /* NLSE_IC_* (its dimension must be the solver's) */
+  int count;            /* vortices / rings in items */
+  const double *items;  /* host array: vortices (x, y, charge) x count;
+                           rings (cx, cy, cz, nx, ny, nz, radius) x count, n unit */
+  double om, c, x0;     /* 1D solitons: frequency, speed, centre */
+  double omega;         /* rings: trap frequency */
+  int noise_kind;       /* NLSE_NOISE_* */
+  double noise;         /* noise amplitude */
+  unsigned long long seed; /* noise seed (counter-based: same values on every device) */
+} nlse_ic;
+
+/* Fill the solver's state and potential with an initial condition on the
+ * grid x_i = -n h/2 + i h (every axis, h = sqrt(h2)). */
+int nlse_solver_init_ic(nlse_solver *s, const nlse_ic *ic);
+
+typedef struct nlse_diag {
+  double mass;          /* sum |psi|^2 h^d over the finite points */
+  double max_abs2;      /* max |psi|^2 */
+  double max_re;        /* max Re psi (the drivers' blow-up test) */
+  long long nonfinite;  /* points with a NaN or Inf component */
+} nlse_diag;
+
+/* Diagnostics of the current state, reduced on the device (FP64). */
+int nlse_solver_diagnostics(nlse_solver *s, nlse_diag *out);
+/* 1D solitons (NLSE_IC_SECH..NLSE_IC_GREY): maximum errors of Re psi, Im psi
+ * and |psi|^2 against the closed-form solution at time t
+ * (NLSEmagic1D_FRS.m:535-542, 589-591). */
+int nlse_solver_error_1d(nlse_solver *s, const nlse_ic *ic, double t, double err[3]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -8,7 +8,8 @@ CPU fallback: without the built library every call raises
 :class:`NativeLibraryMissing`.
 """
 from ._lib import (FLAG_GATHER, FLAG_MSD_GUARD, PREC_DOUBLE, PREC_MIXED, PREC_SINGLE,  # noqa: F401
-                   NativeLibraryMissing, NLSEError, load)
+                   IC_GAUSS, IC_GREY, IC_RINGS, IC_SECH, IC_TANH, IC_VORTICES, NOISE_ADD,
+                   NOISE_NONE, NOISE_PHASE, NativeLibraryMissing, NLSEError, load)
 from .api import *  # noqa: F401,F403
 from .api import Batch, Solver, linear_stability_k, take_steps  # noqa: F401
 

@@ -47,6 +47,25 @@ class Problem(ctypes.Structure):
                 ("flags", ctypes.c_int)]
 
 
+IC_SECH, IC_TANH, IC_GAUSS, IC_GREY, IC_VORTICES, IC_RINGS = 1, 2, 3, 4, 5, 6
+NOISE_NONE, NOISE_ADD, NOISE_PHASE = 0, 1, 2
+
+
+class InitialCondition(ctypes.Structure):
+    """nlse_ic of include/nlse_gb300.h."""
+    _fields_ = [("kind", ctypes.c_int), ("count", ctypes.c_int),
+                ("items", ctypes.POINTER(ctypes.c_double)), ("om", ctypes.c_double),
+                ("c", ctypes.c_double), ("x0", ctypes.c_double), ("omega", ctypes.c_double),
+                ("noise_kind", ctypes.c_int), ("noise", ctypes.c_double),
+                ("seed", ctypes.c_ulonglong)]
+
+
+class Diagnostics(ctypes.Structure):
+    """nlse_diag of include/nlse_gb300.h."""
+    _fields_ = [("mass", ctypes.c_double), ("max_abs2", ctypes.c_double),
+                ("max_re", ctypes.c_double), ("nonfinite", ctypes.c_longlong)]
+
+
 _lib = None
 _lock = threading.Lock()
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -77,6 +96,9 @@ SIGNATURES = {
     "nlse_vorticity3d": (_i, [_dp, _dp, ctypes.POINTER(_ll), ctypes.c_double, ctypes.c_double,
                               _dp, _dp, _dp, _dp]),
     "nlse_solver_vorticity": (_i, [_vp, ctypes.c_double, _vp, _vp, _vp, _vp]),
+    "nlse_solver_init_ic": (_i, [_vp, ctypes.POINTER(InitialCondition)]),
+    "nlse_solver_diagnostics": (_i, [_vp, ctypes.POINTER(Diagnostics)]),
+    "nlse_solver_error_1d": (_i, [_vp, ctypes.POINTER(InitialCondition), ctypes.c_double, _dp]),
     "nlse_batch_create": (_i, [_ll, _i, ctypes.POINTER(_vp)]),
     "nlse_batch_destroy": (_i, [_vp]),
     "nlse_batch_bytes_for": (_ll, [ctypes.POINTER(Problem)]),

@@ -154,6 +154,46 @@ class Solver:
         check(self._lib.nlse_solver_create(ctypes.byref(self.problem), ctypes.byref(h)))
         self._h = h
 
+    # -- initial conditions and diagnostics on the device
+    @staticmethod
+    def _ic(kind, items=None, om=0.0, c=0.0, x0=0.0, omega=0.0, noise_kind=_lib.NOISE_NONE,
+            noise=0.0, seed=0):
+        ic = _lib.InitialCondition()
+        ic.kind = int(kind)
+        arr = None
+        if items is not None:
+            arr = np.ascontiguousarray(np.asarray(items, dtype=np.float64).ravel())
+            ic.items = arr.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+            ic.count = int(arr.size // (3 if kind == _lib.IC_VORTICES else 7))
+        ic.om, ic.c, ic.x0, ic.omega = float(om), float(c), float(x0), float(omega)
+        ic.noise_kind, ic.noise, ic.seed = int(noise_kind), float(noise), int(seed)
+        return ic, arr
+
+    def init_ic(self, kind, items=None, **kw):
+        """Generate the initial state and potential on the device.  kind:
+        IC_SECH, IC_TANH, IC_GAUSS, IC_GREY (1D; om, c, x0), IC_VORTICES (2D;
+        items = [(x, y, charge), ...]), IC_RINGS (3D; items = [(cx, cy, cz, nx,
+        ny, nz, radius), ...], omega = trap frequency); optional noise_kind
+        (NOISE_ADD / NOISE_PHASE), noise, seed."""
+        ic, keep = self._ic(kind, items, **kw)
+        check(self._lib.nlse_solver_init_ic(self._h, ctypes.byref(ic)))
+        del keep
+
+    def diagnostics(self):
+        """dict(mass = sum |psi|^2 h^d, max_abs2, max_re, nonfinite), reduced on the device."""
+        d = _lib.Diagnostics()
+        check(self._lib.nlse_solver_diagnostics(self._h, ctypes.byref(d)))
+        return {"mass": d.mass, "max_abs2": d.max_abs2, "max_re": d.max_re,
+                "nonfinite": int(d.nonfinite)}
+
+    def error_1d(self, kind, t, **kw):
+        """Maximum errors (Re, Im, |psi|^2) against the closed-form 1D soliton at time t."""
+        ic, keep = self._ic(kind, **kw)
+        err = (ctypes.c_double * 3)()
+        check(self._lib.nlse_solver_error_1d(self._h, ctypes.byref(ic), float(t), err))
+        del keep
+        return tuple(err)
+
     def vorticity(self, veps=1e-10):
         """Vorticity (wx, wy, wz, W) of the current 3D state, computed on the
         device from the resident state; returned as numpy arrays of the grid

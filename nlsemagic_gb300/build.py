@@ -34,6 +34,7 @@ UNITS = {
     "nlse_batch.cu": ["-fmad=false"],
     "nlse_noalloc.cu": [],
     "kern_vort.cu": ["-fmad=false"],
+    "kern_init.cu": [],
 }
 
 

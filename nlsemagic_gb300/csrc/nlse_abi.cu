@@ -248,6 +248,7 @@ struct nlse_solver {
   // device staging for planar transfers: re, im, V (n doubles each)
   double* stage;
   double* vort;  // vorticity scratch (3 n doubles), allocated on first use
+  void* d_diag;  // diagnostics accumulators (64 bytes), allocated on first use
   double* d_mass;
   int* d_bad;
   // graphs
@@ -290,7 +291,7 @@ extern "C" int nlse_solver_destroy(nlse_solver* s) {
   free_graphs(s);
   void* ptrs[] = {s->psi, s->K, s->ya, s->yb, s->V, s->hi[0], s->hi[1], s->lo[0], s->lo[1],
                   s->mK, s->da, s->db, s->fq, s->gh, s->Vf, s->stage, s->d_mass, s->d_bad,
-                  s->dsc, s->vort};
+                  s->dsc, s->vort, s->d_diag};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -878,5 +879,91 @@ extern "C" int nlse_solver_vorticity(nlse_solver* s, double veps, double* d_wx, 
   const double lh2 = 1.0 / (2.0 * sqrt(s->prob.h2));
   CUDA_TRY(launch_vorticity(s->g.M, s->g.N, s->g.L, s->stage, s->stage + n, lh2, veps, s->vort,
                             d_wx, d_wy, d_wz, d_W, s->stream));
+  return NLSE_OK;
+}
+
+// ---------------------------------------------------------------------------
+// initial conditions and diagnostics on the device
+// ---------------------------------------------------------------------------
+extern "C" int nlse_solver_init_ic(nlse_solver* s, const nlse_ic* ic) {
+  if (!s || !ic) return fail(NLSE_ERR_ARG, "NULL argument");
+  const int nd = s->g.ndim;
+  const int want = ic->kind <= NLSE_IC_GREY ? 1 : (ic->kind == NLSE_IC_VORTICES ? 2 : 3);
+  if (ic->kind < NLSE_IC_SECH || ic->kind > NLSE_IC_RINGS)
+    return fail(NLSE_ERR_ARG, "unknown initial condition %d", ic->kind);
+  if (want != nd)
+    return fail(NLSE_ERR_ARG, "initial condition %d is %dD, the solve is %dD", ic->kind, want, nd);
+  const int per = ic->kind == NLSE_IC_VORTICES ? 3 : (ic->kind == NLSE_IC_RINGS ? 7 : 0);
+  if (per && (ic->count < 0 || ic->count > 4096 || (ic->count > 0 && !ic->items)))
+    return fail(NLSE_ERR_ARG, "bad vortex / ring list");
+  if (ic->noise_kind < NLSE_NOISE_NONE || ic->noise_kind > NLSE_NOISE_PHASE)
+    return fail(NLSE_ERR_ARG, "unknown noise kind %d", ic->noise_kind);
+  CUDA_TRY(cudaSetDevice(s->device));
+  int r = ensure_stage(s);
+  if (r) return r;
+  double* d_items = nullptr;
+  const size_t ib = sizeof(double) * (size_t)(per ? per * ic->count : 0);
+  if (ib) {
+    CUDA_TRY(cudaMalloc(&d_items, ib));
+    cudaError_t e = cudaMemcpyAsync(d_items, ic->items, ib, cudaMemcpyHostToDevice, s->stream);
+    if (e != cudaSuccess) {
+      cudaFree(d_items);
+      return fail(NLSE_ERR_CUDA, "copy of the vortex / ring list failed: %s", cudaGetErrorString(e));
+    }
+  }
+  const long long n = s->g.n;
+  double *re = s->stage, *im = s->stage + n, *vv = s->stage + 2 * n;
+  cudaError_t e = launch_ic(nd, s->g.M, s->g.N, s->g.L, sqrt(s->prob.h2), *ic, d_items,
+                            s->prob.s, s->prob.a, re, im, vv, s->stream);
+  if (e == cudaSuccess) r = ingest(s, re, im, vv);
+  cudaError_t e2 = cudaStreamSynchronize(s->stream);
+  if (d_items) cudaFree(d_items);
+  if (e != cudaSuccess) return fail(NLSE_ERR_CUDA, "initial-condition kernel: %s", cudaGetErrorString(e));
+  if (r) return r;
+  if (e2 != cudaSuccess) return fail(NLSE_ERR_CUDA, "initial condition: %s", cudaGetErrorString(e2));
+  return NLSE_OK;
+}
+
+static int run_diag(nlse_solver* s, const nlse_ic* ic, double t, double out[7]) {
+  CUDA_TRY(cudaSetDevice(s->device));
+  if (!s->d_diag) {
+    int r = dalloc(s, &s->d_diag, 64);
+    if (r) return r;
+  }
+  const void *a, *b = nullptr;
+  if (s->prob.precision == NLSE_PREC_MIXED) {
+    a = s->hi[s->cur];
+    b = s->lo[s->cur];
+  } else {
+    a = s->psi;
+  }
+  CUDA_TRY(launch_diag(s->prob.precision, s->g.ndim, s->g.M, s->g.N, s->g.L, sqrt(s->prob.h2), a,
+                       b, ic, s->prob.s, s->prob.a, t, s->d_diag, out, s->stream));
+  return device_error_check();
+}
+
+extern "C" int nlse_solver_diagnostics(nlse_solver* s, nlse_diag* out) {
+  if (!s || !out) return fail(NLSE_ERR_ARG, "NULL argument");
+  double v[7];
+  int r = run_diag(s, nullptr, 0.0, v);
+  if (r) return r;
+  const double h = sqrt(s->prob.h2);
+  out->mass = v[0] * (s->g.ndim == 1 ? h : (s->g.ndim == 2 ? h * h : h * h * h));
+  out->max_abs2 = v[1];
+  out->max_re = v[2];
+  out->nonfinite = (long long)v[6];
+  return NLSE_OK;
+}
+
+extern "C" int nlse_solver_error_1d(nlse_solver* s, const nlse_ic* ic, double t, double err[3]) {
+  if (!s || !ic || !err) return fail(NLSE_ERR_ARG, "NULL argument");
+  if (s->g.ndim != 1 || ic->kind < NLSE_IC_SECH || ic->kind > NLSE_IC_GREY)
+    return fail(NLSE_ERR_ARG, "closed-form errors exist for the 1D solitons only");
+  double v[7];
+  int r = run_diag(s, ic, t, v);
+  if (r) return r;
+  err[0] = v[3];
+  err[1] = v[4];
+  err[2] = v[5];
   return NLSE_OK;
 }

@@ -6,6 +6,8 @@
 
 #include "nlse_common.cuh"
 
+struct nlse_ic;  // include/nlse_gb300.h
+
 namespace nlse {
 
 enum KernelKind { KERNEL_GATHER = 0, KERNEL_TILED = 1 };
@@ -79,6 +81,15 @@ cudaError_t mass_hilo(const float2* hi, const float2* lo, long long n, double* o
                       cudaStream_t st);
 
 bool tiled_supported(const Geom& g, int dim);
+
+// Initial conditions and diagnostics (kern_init.cu); ::nlse_ic is declared
+// in include/nlse_gb300.h.
+cudaError_t launch_ic(int ndim, int M, int N, int L, double h, const ::nlse_ic& ic,
+                      const double* d_items, double s, double a, double* re, double* im, double* V,
+                      cudaStream_t st);
+cudaError_t launch_diag(int cls, int ndim, int M, int N, int L, double h, const void* a,
+                        const void* b, const ::nlse_ic* ic, double s, double aa, double t,
+                        void* scratch, double out[7], cudaStream_t st);
 
 // 3D vorticity (kern_vort.cu): planar FP64 U of M x N x L points -> wx, wy,
 // wz, W; vscratch holds 3 n doubles.

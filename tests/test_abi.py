@@ -108,3 +108,28 @@ def test_missing_library_fails_loudly(tmp_path):
             _lib.load(str(tmp_path / "absent.so"))
         finally:
             _lib._lib = saved
+
+
+def test_ctypes_structs_match_the_c_header(tmp_path):
+    # sizes and field offsets of the structures passed by pointer
+    src = tmp_path / "layout.c"
+    src.write_text(
+        '#include <stdio.h>\n#include <stddef.h>\n#include "nlse_gb300.h"\n'
+        'int main(void){\n'
+        ' printf("%zu %zu %zu %zu %zu %zu %zu\\n", sizeof(nlse_problem), offsetof(nlse_problem,dims),'
+        ' offsetof(nlse_problem,s), offsetof(nlse_problem,flags), sizeof(nlse_ic), offsetof(nlse_ic,items),'
+        ' offsetof(nlse_ic,seed));\n'
+        ' printf("%zu %zu %zu\\n", sizeof(nlse_diag), offsetof(nlse_diag,max_re), offsetof(nlse_diag,nonfinite));\n'
+        ' return 0;}\n')
+    exe = tmp_path / "layout"
+    import subprocess
+    r = subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()
+    want = [ctypes.sizeof(_lib.Problem), _lib.Problem.dims.offset, _lib.Problem.s.offset,
+            _lib.Problem.flags.offset, ctypes.sizeof(_lib.InitialCondition),
+            _lib.InitialCondition.items.offset, _lib.InitialCondition.seed.offset,
+            ctypes.sizeof(_lib.Diagnostics), _lib.Diagnostics.max_re.offset,
+            _lib.Diagnostics.nonfinite.offset]
+    assert [int(v) for v in out] == want
