@@ -327,6 +327,17 @@ int nlse_solver_diagnostics(nlse_solver *s, nlse_diag *out);
  * (NLSEmagic1D_FRS.m:535-542, 589-591). */
 int nlse_solver_error_1d(nlse_solver *s, const nlse_ic *ic, double t, double err[3]);
 
+/* ------------------------------------------------------------------------
+ * 2D cubic-quintic NLSE, 2SHOC, FP64:
+ *   i U_t + a (U_xx + U_yy) - V U + (s1 |U|^2 + s2 |U|^4) U = 0.
+ * Replaces U = CQNLSE2D_TAKE_STEPS_2SHOC(U, V, s1, s2, a, h2, BC, chunk_size, k)
+ * (src_old/NLSE2D_v1/CQNLSE2D_TAKE_STEPS_2SHOC.c:357-437) with that file's
+ * own boundary formulas.  p->s is s1; p must be 2D, 2SHOC, FP64, BC 1-3;
+ * NLSE_FLAG_MSD_GUARD makes its MSD zero-neighbour divisions 0.
+ * ------------------------------------------------------------------------ */
+int nlse_cq2d_take_steps(const nlse_problem *p, double s2, const double *Ur, const double *Ui,
+                         const double *V, double *out_r, double *out_i, int chunk_size);
+
 #ifdef __cplusplus
 }
 #endif

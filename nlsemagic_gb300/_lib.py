@@ -97,6 +97,8 @@ SIGNATURES = {
                               _dp, _dp, _dp, _dp]),
     "nlse_solver_vorticity": (_i, [_vp, ctypes.c_double, _vp, _vp, _vp, _vp]),
     "nlse_solver_init_ic": (_i, [_vp, ctypes.POINTER(InitialCondition)]),
+    "nlse_cq2d_take_steps": (_i, [ctypes.POINTER(Problem), ctypes.c_double, _dp, _dp, _dp, _dp,
+                                  _dp, _i]),
     "nlse_solver_diagnostics": (_i, [_vp, ctypes.POINTER(Diagnostics)]),
     "nlse_solver_error_1d": (_i, [_vp, ctypes.POINTER(InitialCondition), ctypes.c_double, _dp]),
     "nlse_batch_create": (_i, [_ll, _i, ctypes.POINTER(_vp)]),

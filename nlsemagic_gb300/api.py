@@ -399,3 +399,23 @@ def rmc_vorticity3D(U, lh2, veps):
 def vorticity3d(U, h, veps=1e-10):
     """Vorticity of U on a grid of spacing h: rmc_vorticity3D(U, 1/(2h), veps)."""
     return rmc_vorticity3D(U, 1.0 / (2.0 * h), veps)
+
+
+# ---------------------------------------------------------------------------
+# 2D cubic-quintic NLSE (2SHOC, FP64)
+# ---------------------------------------------------------------------------
+def CQNLSE2D_TAKE_STEPS_2SHOC(U, V, s1, s2, a, h2, BC, chunk_size, k, flags=FLAG_MSD_GUARD):
+    """U = CQNLSE2D_TAKE_STEPS_2SHOC(U, V, s1, s2, a, h2, BC, chunk_size, k) on
+    the GPU (src_old/NLSE2D_v1/CQNLSE2D_TAKE_STEPS_2SHOC.c:357-437); U
+    MATLAB-shaped (M, N)."""
+    U = np.asarray(U)
+    if U.ndim != 2:
+        raise ValueError("the cubic-quintic integrator is 2D")
+    ndim, dims = grid_dims(U.shape)
+    prob = make_problem(2, dims, 2, PREC_DOUBLE, BC, s1, a, h2, k, flags)
+    re, im = planar(U)
+    vv = np.ascontiguousarray(np.asarray(V, dtype=np.float64).ravel(order="F"))
+    outr, outi = np.empty_like(re), np.empty_like(im)
+    check(load().nlse_cq2d_take_steps(ctypes.byref(prob), float(s2), _ptr(re), _ptr(im),
+                                      _ptr(vv), _ptr(outr), _ptr(outi), int(chunk_size)))
+    return (outr + 1j * outi).reshape(U.shape, order="F")

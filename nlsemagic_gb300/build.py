@@ -35,6 +35,7 @@ UNITS = {
     "nlse_noalloc.cu": [],
     "kern_vort.cu": ["-fmad=false"],
     "kern_init.cu": [],
+    "kern_cq.cu": ["-fmad=false"],
 }
 
 

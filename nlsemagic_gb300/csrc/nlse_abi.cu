@@ -967,3 +967,84 @@ extern "C" int nlse_solver_error_1d(nlse_solver* s, const nlse_ic* ic, double t,
   err[2] = v[5];
   return NLSE_OK;
 }
+
+// ---------------------------------------------------------------------------
+// 2D cubic-quintic 2SHOC, FP64 (src_old/NLSE2D_v1/CQNLSE2D_TAKE_STEPS_2SHOC.c)
+// ---------------------------------------------------------------------------
+namespace {
+struct CqCache {
+  int device = -1;
+  long long cap = 0;
+  double* buf = nullptr;  // psi, K, ya, yb, D (2 doubles each per point), V, staging (3)
+  cudaStream_t stream = nullptr;
+  ~CqCache() {
+    if (buf) cudaFree(buf);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+thread_local CqCache t_cq;
+}  // namespace
+
+extern "C" int nlse_cq2d_take_steps(const nlse_problem* p, double s2, const double* Ur,
+                                    const double* Ui, const double* V, double* out_r,
+                                    double* out_i, int chunk_size) {
+  int rc = validate(p);
+  if (rc) return rc;
+  if (p->ndim != 2 || p->method != 2 || p->precision != NLSE_PREC_DOUBLE)
+    return fail(NLSE_ERR_ARG, "the cubic-quintic integrator is 2D, 2SHOC, FP64");
+  if (p->bc > 3) return fail(NLSE_ERR_ARG, "BC must be 1, 2 or 3");
+  if (!isfinite(s2)) return fail(NLSE_ERR_ARG, "s2 must be finite");
+  if (!Ur || !V || !out_r || !out_i) return fail(NLSE_ERR_ARG, "NULL array argument");
+  if (chunk_size < 0) return fail(NLSE_ERR_ARG, "chunk_size must be >= 0");
+  const Geom g = make_geom(p);
+  const long long n = g.n;
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  CqCache& c = t_cq;
+  if (c.device != dev || c.cap < n) {
+    if (c.buf) cudaFree(c.buf);
+    c.buf = nullptr;
+    c.cap = 0;
+    if (c.stream && c.device != dev) {
+      cudaStreamDestroy(c.stream);
+      c.stream = nullptr;
+    }
+    c.device = dev;
+    CUDA_TRY(cudaMalloc(&c.buf, sizeof(double) * 14 * n));
+    c.cap = n;
+    if (!c.stream) CUDA_TRY(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+  }
+  typedef C2<double> T;
+  T *psi = (T*)c.buf, *K = psi + n, *ya = K + n, *yb = ya + n, *D = yb + n;
+  double* vv = (double*)(D + n);
+  double *re = vv + n, *im = re + n, *vst = im + n;
+  const size_t b = sizeof(double) * n;
+  CUDA_TRY(cudaMemcpyAsync(re, Ur, b, cudaMemcpyHostToDevice, c.stream));
+  if (Ui) CUDA_TRY(cudaMemcpyAsync(im, Ui, b, cudaMemcpyHostToDevice, c.stream));
+  CUDA_TRY(cudaMemcpyAsync(vst, V, b, cudaMemcpyHostToDevice, c.stream));
+  CUDA_TRY(planar_to_c2d(re, Ui ? im : nullptr, psi, n, c.stream));
+  CUDA_TRY(cudaMemcpyAsync(vv, vst, b, cudaMemcpyDeviceToDevice, c.stream));
+  const Consts<double> k = consts_double(p);
+  CqParams q;
+  q.M = g.M;
+  q.N = g.N;
+  q.BC = p->bc;
+  q.guard = (p->flags & NLSE_FLAG_MSD_GUARD) ? 1 : 0;
+  q.s1 = p->s;
+  q.s2 = s2;
+  q.a = p->a;
+  q.lh2 = 1.0 / p->h2;
+  q.l_a = 1.0 / p->a;
+  q.a1_6h2 = p->a * (1.0 / (6.0 * p->h2));
+  q.a1_12 = p->a * (1.0 / 12.0);
+  const T* yin[4] = {psi, ya, yb, ya};
+  T* yout[4] = {ya, yb, ya, nullptr};
+  for (int step = 0; step < chunk_size; ++step)
+    for (int st = 1; st <= 4; ++st)
+      CUDA_TRY(launch_cq_stage(q, k, yin[st - 1], psi, vv, K, yout[st - 1], D, st, c.stream));
+  CUDA_TRY(c2d_to_planar(psi, re, im, n, c.stream));
+  CUDA_TRY(cudaMemcpyAsync(out_r, re, b, cudaMemcpyDeviceToHost, c.stream));
+  CUDA_TRY(cudaMemcpyAsync(out_i, im, b, cudaMemcpyDeviceToHost, c.stream));
+  CUDA_TRY(cudaStreamSynchronize(c.stream));
+  return NLSE_OK;
+}

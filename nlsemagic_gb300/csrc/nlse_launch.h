@@ -91,6 +91,16 @@ cudaError_t launch_diag(int cls, int ndim, int M, int N, int L, double h, const 
                         const void* b, const ::nlse_ic* ic, double s, double aa, double t,
                         void* scratch, double out[7], cudaStream_t st);
 
+// 2D cubic-quintic 2SHOC stage (kern_cq.cu): D into Dscratch, then F and the
+// RK4 update, FP64.
+struct CqParams {
+  int M, N, BC, guard;
+  double s1, s2, a, lh2, l_a, a1_6h2, a1_12;
+};
+cudaError_t launch_cq_stage(const CqParams& c, const Consts<double>& k, const C2<double>* Yin,
+                            C2<double>* Psi, const double* V, C2<double>* K, C2<double>* Yout,
+                            C2<double>* Dscratch, int stage, cudaStream_t st);
+
 // 3D vorticity (kern_vort.cu): planar FP64 U of M x N x L points -> wx, wy,
 // wz, W; vscratch holds 3 n doubles.
 cudaError_t launch_vorticity(int M, int N, int L, const double* Ur, const double* Ui, double lh2,

@@ -159,3 +159,47 @@ def ref_vorticity3d(U, lh2, veps):
     if rc != 0:
         raise RuntimeError("reference vorticity call failed (code %d)" % rc)
     return tuple(o.reshape(U.shape, order="F") for o in outs)
+
+
+def cq2d(U, V, s1, s2, a, h2, BC, chunk, k, flags=MSD_GUARD):
+    """C restatement of the 2D cubic-quintic 2SHOC integrator (FP64).  U
+    MATLAB-shaped (M, N)."""
+    U = np.asarray(U)
+    M, N = (int(d) for d in U.shape)
+    Ur, Ui, Vv = _planes(U, V)
+    lib = _load_port()
+    f = lib.nlse_oracle_cq2d
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp] + [ctypes.c_double] * 4 + \
+        [ctypes.c_int, ctypes.c_int, ctypes.c_double, _dp, _dp, ctypes.c_int]
+    outr, outi = np.empty_like(Ur), np.empty_like(Ui)
+    rc = f(M, N, _ptr(Ur), _ptr(Ui), _ptr(Vv), float(s1), float(s2), float(a), float(h2), int(BC),
+           int(chunk), float(k), _ptr(outr), _ptr(outi), int(flags))
+    if rc != 0:
+        raise ValueError("oracle rejected arguments (code %d)" % rc)
+    return (outr + 1j * outi).reshape(U.shape, order="F")
+
+
+def ref_cq2d(U, V, s1, s2, a, h2, BC, chunk, k):
+    """The reference's own CQNLSE2D_TAKE_STEPS_2SHOC MEX function (via the shim)."""
+    U = np.asarray(U)
+    name = "CQNLSE2D_TAKE_STEPS_2SHOC"
+    if name not in _refs:
+        libs = _build.build_ref()
+        if name not in libs:
+            raise RuntimeError("reference cubic-quintic integrator is not available here")
+        lib = ctypes.CDLL(libs[name], mode=ctypes.RTLD_LOCAL)
+        f = lib.mex_call_cq2d
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.POINTER(ctypes.c_longlong), _dp, _dp, _dp] + \
+            [ctypes.c_double] * 4 + [ctypes.c_int, ctypes.c_int, ctypes.c_double, _dp, _dp]
+        _refs[name] = lib
+    Ur, Ui, Vv = _planes(U, V)
+    cd = (ctypes.c_longlong * 2)(*(int(d) for d in U.shape))
+    outr, outi = np.empty_like(Ur), np.empty_like(Ui)
+    rc = _refs[name].mex_call_cq2d(cd, _ptr(Ur), _ptr(Ui), _ptr(Vv), float(s1), float(s2),
+                                   float(a), float(h2), int(BC), int(chunk), float(k), _ptr(outr),
+                                   _ptr(outi))
+    if rc != 0:
+        raise RuntimeError("reference call failed (code %d)" % rc)
+    return (outr + 1j * outi).reshape(U.shape, order="F")

@@ -43,6 +43,7 @@ REF_FILES = {
     "NLSE3D_TAKE_STEPS_2SHOC": "src/NLSEmagic3D/NLSE3D_TAKE_STEPS_2SHOC.c",
     "NLSE3D_TAKE_STEPS_2SHOC_F": "src/NLSEmagic3D/NLSE3D_TAKE_STEPS_2SHOC_F.c",
     "rmc_vorticity3D": "src/NLSEmagic3D/rmc_vorticity3D.c",
+    "CQNLSE2D_TAKE_STEPS_2SHOC": "src_old/NLSE2D_v1/CQNLSE2D_TAKE_STEPS_2SHOC.c",
 }
 
 REF_CFLAGS = ["-std=gnu89", "-O3", "-funroll-loops", "-ffp-contract=off",

@@ -205,3 +205,44 @@ int mex_call_vorticity(const long long *dims, const double *Ur, const double *Ui
     for (i = 0; i < 3; ++i) free_array(prhs[i]);
     return g_mex_error ? -3 : 0;
 }
+
+/* U = CQNLSE2D_TAKE_STEPS_2SHOC(U, V, s1, s2, a, h2, BC, chunk_size, k) through
+ * the mexFunction linked into this shared object; dims = {M, N}. */
+int mex_call_cq2d(const long long *dims, const double *Ur, const double *Ui, const double *V,
+                  double s1, double s2, double a, double h2, int BC, int chunk, double k,
+                  double *out_r, double *out_i) {
+    mwSize d[2];
+    mwSize n, i;
+    mxArray *prhs[9];
+    mxArray *plhs[1];
+    d[0] = (mwSize)dims[0];
+    d[1] = (mwSize)dims[1];
+    prhs[0] = make_array(2, d, Ui ? mxCOMPLEX : mxREAL);
+    prhs[1] = make_array(2, d, mxREAL);
+    n = numel(prhs[0]);
+    memcpy(prhs[0]->pr, Ur, n * sizeof(double));
+    if (Ui) memcpy(prhs[0]->pi, Ui, n * sizeof(double));
+    memcpy(prhs[1]->pr, V, n * sizeof(double));
+    prhs[2] = make_scalar(s1);
+    prhs[3] = make_scalar(s2);
+    prhs[4] = make_scalar(a);
+    prhs[5] = make_scalar(h2);
+    prhs[6] = make_scalar((double)BC);
+    prhs[7] = make_scalar((double)chunk);
+    prhs[8] = make_scalar(k);
+    plhs[0] = NULL;
+    g_mex_error = 0;
+    mexFunction(1, plhs, 9, (const mxArray **)prhs);
+    if (!plhs[0]) {
+        for (i = 0; i < 9; ++i) free_array(prhs[i]);
+        return -2;
+    }
+    memcpy(out_r, plhs[0]->pr, n * sizeof(double));
+    if (plhs[0]->pi)
+        memcpy(out_i, plhs[0]->pi, n * sizeof(double));
+    else
+        memset(out_i, 0, n * sizeof(double));
+    free_array(plhs[0]);
+    for (i = 0; i < 9; ++i) free_array(prhs[i]);
+    return g_mex_error ? -3 : 0;
+}

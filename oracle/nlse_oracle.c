@@ -254,3 +254,177 @@ void nlse_oracle_vorticity3d(int M, int N, int L, const double *Ur, const double
             }
     free(v);
 }
+
+/* ------------------------------------------------------------------------
+ * 2D cubic-quintic NLSE, 2SHOC, FP64:
+ *   i U_t + a (U_xx + U_yy) - V U + (s1 |U|^2 + s2 |U|^4) U = 0,
+ * restating src_old/NLSE2D_v1/CQNLSE2D_TAKE_STEPS_2SHOC.c (the only cubic-
+ * quintic integrator of the reference).  Rows i = 0..N-1 (second MATLAB
+ * index), columns j = 0..M-1 (first, fastest); p = i*M + j.  That file's own
+ * boundary formulas are kept:
+ *   MSD D at a boundary point b with inward neighbour q (edges: the normal
+ *   neighbour, corners: the diagonal one, CQNLSE2D_TAKE_STEPS_2SHOC.c:52-57):
+ *     A = (Ui_q Ur_b - Ur_q Ui_b)/|U_q|^2, B = (Ui_q Ui_b + Ur_q Ur_b)/|U_q|^2,
+ *     NL = ((V_b - V_q) + s1|U_q|^2 + s2|U_q|^4 - (s1|U_b|^2 + s2|U_b|^4))/a,
+ *     D_b = (A Di_q + B Dr_q + NL Ur_b,  B Di_q - A Dr_q + NL Ui_b)
+ *   and on the j = M-1 edge its s1 term reads |U(i, 1)|^2 for |U_q|^2
+ *   (:126-127; kept: the file's results are the contract);
+ *   MSD F: OM = (Fi_q Ur_q - Fr_q Ui_q)/|U_q|^2, F_b = (-OM Ui_b, OM Ur_b);
+ *   Dirichlet D = -(1/a)(s1|U|^2 + s2|U|^4 - V) U, F = 0;
+ *   BC 3: D = 0, F = i(s1|U|^2 + s2|U|^4 - V) U.
+ * flags & 1 (the zero-neighbour guard): A = B = OM = 0 where |U_q|^2 = 0
+ * (the file itself divides 0/0).
+ * ------------------------------------------------------------------------ */
+typedef struct {
+    int M, N, BC, guard;
+    double s1, s2, a, lh2, l_a, a1_6h2, a1_12;
+} cq_t;
+
+static double cq_m(const double *r, const double *i, long long p) { return r[p] * r[p] + i[p] * i[p]; }
+
+static void cq_F(const cq_t *c, const double *Ur, const double *Ui, const double *V, double *Dr,
+                 double *Di, double *Fr, double *Fi) {
+    const int M = c->M, N = c->N;
+    int i, j, t;
+    long long p;
+    /* interior D */
+    for (i = 1; i < N - 1; ++i)
+        for (j = 1; j < M - 1; ++j) {
+            p = (long long)i * M + j;
+            Di[p] = (Ui[p + M] + Ui[p - M] - 4 * Ui[p] + Ui[p + 1] + Ui[p - 1]) * c->lh2;
+            Dr[p] = (Ur[p + M] + Ur[p - M] - 4 * Ur[p] + Ur[p + 1] + Ur[p - 1]) * c->lh2;
+        }
+    /* boundary D */
+    for (i = 0; i < N; ++i)
+        for (j = 0; j < M; ++j) {
+            double m, A, B, NL, mq;
+            long long q;
+            int qi, qj;
+            if (i > 0 && i < N - 1 && j > 0 && j < M - 1) continue;
+            p = (long long)i * M + j;
+            if (c->BC == 1) {
+                m = cq_m(Ur, Ui, p);
+                Dr[p] = -c->l_a * (c->s1 * m + c->s2 * m * m - V[p]) * Ur[p];
+                Di[p] = -c->l_a * (c->s1 * m + c->s2 * m * m - V[p]) * Ui[p];
+            } else if (c->BC == 2) {
+                qi = i == 0 ? 1 : (i == N - 1 ? N - 2 : i);
+                qj = j == 0 ? 1 : (j == M - 1 ? M - 2 : j);
+                q = (long long)qi * M + qj;
+                mq = cq_m(Ur, Ui, q);
+                m = cq_m(Ur, Ui, p);
+                if (c->guard && mq == 0) {
+                    A = 0;
+                    B = 0;
+                } else {
+                    A = (Ui[q] * Ur[p] - Ur[q] * Ui[p]) / (Ur[q] * Ur[q] + Ui[q] * Ui[q]);
+                    B = (Ui[q] * Ui[p] + Ur[q] * Ur[p]) / (Ur[q] * Ur[q] + Ui[q] * Ui[q]);
+                }
+                {
+                    /* the s1 term of the j = M-1 edge (not a corner) reads U(i, 1) */
+                    const long long q1 = (j == M - 1 && i > 0 && i < N - 1) ? (long long)i * M + 1 : q;
+                    const double m1 = cq_m(Ur, Ui, q1);
+                    NL = ((V[p] - V[q]) + c->s1 * m1 + c->s2 * mq * mq - (c->s1 * m + c->s2 * m * m)) / c->a;
+                }
+                Dr[p] = A * Di[q] + B * Dr[q] + NL * Ur[p];
+                Di[p] = B * Di[q] - A * Dr[q] + NL * Ui[p];
+            } else {
+                Dr[p] = 0.0;
+                Di[p] = 0.0;
+            }
+        }
+    /* interior F */
+    for (i = 1; i < N - 1; ++i)
+        for (j = 1; j < M - 1; ++j) {
+            double m;
+            p = (long long)i * M + j;
+            m = cq_m(Ur, Ui, p);
+            Fr[p] = -c->a * Di[p] + c->a1_12 * (Di[p + M] + Di[p - M] + Di[p + 1] + Di[p - 1]) -
+                    c->a1_6h2 * (Ui[p + M + 1] + Ui[p + M - 1] - 4 * Ui[p] + Ui[p - M + 1] + Ui[p - M - 1]) -
+                    (c->s1 * m + c->s2 * m * m - V[p]) * Ui[p];
+            Fi[p] = c->a * Dr[p] - c->a1_12 * (Dr[p + M] + Dr[p - M] + Dr[p + 1] + Dr[p - 1]) +
+                    c->a1_6h2 * (Ur[p + M + 1] + Ur[p + M - 1] - 4 * Ur[p] + Ur[p - M + 1] + Ur[p - M - 1]) +
+                    (c->s1 * m + c->s2 * m * m - V[p]) * Ur[p];
+        }
+    /* boundary F */
+    for (i = 0; i < N; ++i)
+        for (j = 0; j < M; ++j) {
+            double m, OM;
+            long long q;
+            int qi, qj;
+            if (i > 0 && i < N - 1 && j > 0 && j < M - 1) continue;
+            p = (long long)i * M + j;
+            if (c->BC == 2) {
+                qi = i == 0 ? 1 : (i == N - 1 ? N - 2 : i);
+                qj = j == 0 ? 1 : (j == M - 1 ? M - 2 : j);
+                q = (long long)qi * M + qj;
+                if (c->guard && cq_m(Ur, Ui, q) == 0)
+                    OM = 0;
+                else
+                    OM = (Fi[q] * Ur[q] - Fr[q] * Ui[q]) / (Ur[q] * Ur[q] + Ui[q] * Ui[q]);
+                Fr[p] = -OM * Ui[p];
+                Fi[p] = OM * Ur[p];
+            } else if (c->BC == 3) {
+                m = cq_m(Ur, Ui, p);
+                Fr[p] = -(c->s1 * m + c->s2 * m * m - V[p]) * Ui[p];
+                Fi[p] = (c->s1 * m + c->s2 * m * m - V[p]) * Ur[p];
+            } else {
+                Fr[p] = 0.0;
+                Fi[p] = 0.0;
+            }
+        }
+    (void)t;
+}
+
+static void cq_axpy(double *Ar, double *Ai, const double *Br, const double *Bi, const double *Cr,
+                    const double *Ci, double k, long long n) {
+    long long p;
+    for (p = 0; p < n; ++p) {
+        Ar[p] = Br[p] + k * Cr[p];
+        Ai[p] = Bi[p] + k * Ci[p];
+    }
+}
+
+int nlse_oracle_cq2d(int M, int N, const double *Ur, const double *Ui, const double *V, double s1,
+                     double s2, double a, double h2, int BC, int chunk, double k, double *out_r,
+                     double *out_i, int flags) {
+    const long long n = (long long)M * N;
+    cq_t c;
+    double *buf, *Ur0, *Ui0, *Yr, *Yi, *Kr, *Ki, *Tr, *Ti, *Dr, *Di;
+    const double k2 = k / 2.0, k6 = k / 6.0;
+    int step;
+    if (M < 3 || N < 3 || BC < 1 || BC > 3 || chunk < 0) return -1;
+    c.M = M;
+    c.N = N;
+    c.BC = BC;
+    c.guard = flags & 1;
+    c.s1 = s1;
+    c.s2 = s2;
+    c.a = a;
+    c.l_a = 1.0 / a;
+    c.lh2 = 1.0 / h2;
+    c.a1_6h2 = a * (1.0 / (6.0 * h2));
+    c.a1_12 = a * (1.0 / 12.0);
+    buf = (double *)calloc((size_t)(10 * n), sizeof(double));
+    if (!buf) return -5;
+    Ur0 = buf; Ui0 = buf + n; Yr = buf + 2 * n; Yi = buf + 3 * n; Kr = buf + 4 * n;
+    Ki = buf + 5 * n; Tr = buf + 6 * n; Ti = buf + 7 * n; Dr = buf + 8 * n; Di = buf + 9 * n;
+    memcpy(Ur0, Ur, sizeof(double) * n);
+    if (Ui) memcpy(Ui0, Ui, sizeof(double) * n);
+    for (step = 0; step < chunk; ++step) {
+        cq_F(&c, Ur0, Ui0, V, Dr, Di, Kr, Ki);
+        cq_axpy(Yr, Yi, Ur0, Ui0, Kr, Ki, k2, n);
+        cq_F(&c, Yr, Yi, V, Dr, Di, Tr, Ti);
+        cq_axpy(Kr, Ki, Kr, Ki, Tr, Ti, 2.0, n);
+        cq_axpy(Yr, Yi, Ur0, Ui0, Tr, Ti, k2, n);
+        cq_F(&c, Yr, Yi, V, Dr, Di, Tr, Ti);
+        cq_axpy(Kr, Ki, Kr, Ki, Tr, Ti, 2.0, n);
+        cq_axpy(Yr, Yi, Ur0, Ui0, Tr, Ti, k, n);
+        cq_F(&c, Yr, Yi, V, Dr, Di, Tr, Ti);
+        cq_axpy(Kr, Ki, Kr, Ki, Tr, Ti, 1.0, n);
+        cq_axpy(Ur0, Ui0, Ur0, Ui0, Kr, Ki, k6, n);
+    }
+    memcpy(out_r, Ur0, sizeof(double) * n);
+    memcpy(out_i, Ui0, sizeof(double) * n);
+    free(buf);
+    return 0;
+}

@@ -199,3 +199,32 @@ def test_vorticity_of_a_straight_vortex_line():
     assert core.max() > 10 * far
     mid = (slice(3, n - 3),) * 3
     assert np.abs(wx[mid]).max() > 5 * max(np.abs(wy[mid]).max(), np.abs(wz[mid]).max())
+
+
+# ---- 2D cubic-quintic 2SHOC (src_old/NLSE2D_v1/CQNLSE2D_TAKE_STEPS_2SHOC.c) -----
+@pytest.mark.parametrize("shape", [(9, 7), (16, 23), (5, 5), (40, 31)])
+@pytest.mark.parametrize("BC", [1, 2, 3])
+def test_cq2d_oracle_matches_reference(shape, BC):
+    if not oracle.ref_available():
+        pytest.skip("reference checkout not present")
+    rng = np.random.default_rng(shape[0] * 7 + BC)
+    U = (1 + 0.3 * rng.standard_normal(shape)) + 0.3j * rng.standard_normal(shape)
+    V = 0.1 * rng.random(shape)
+    args = (U, V, -1.0, 0.3, 1.2, 0.09, BC, 7, 0.004)
+    got = oracle.cq2d(*args, flags=0)  # the file has no zero-neighbour guard
+    want = oracle.ref_cq2d(*args)
+    assert np.array_equal(np.ascontiguousarray(got).view(np.float64),
+                          np.ascontiguousarray(want).view(np.float64))
+
+
+def test_cq2d_reduces_to_cubic_interior_when_s2_is_zero():
+    # with s2 = 0 and Dirichlet / Laplacian-zero boundaries the cubic-quintic
+    # file's formulas are those of the cubic 2D 2SHOC integrator up to
+    # operand order: the two agree to rounding
+    rng = np.random.default_rng(11)
+    U = (1 + 0.2 * rng.standard_normal((20, 18))) + 0.2j * rng.standard_normal((20, 18))
+    V = 0.05 * rng.random((20, 18))
+    for BC in (1, 3):
+        a = oracle.cq2d(U, V, -1.0, 0.0, 1.0, 0.09, BC, 5, 0.004)
+        b = oracle.take_steps(U, V, -1.0, 1.0, 0.09, BC, 5, 0.004, method=2, precision=2)
+        assert np.max(np.abs(a - b)) < 1e-12
