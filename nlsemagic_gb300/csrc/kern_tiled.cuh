@@ -623,7 +623,7 @@ cudaError_t launch3d(const Geom& g, const typename Pol::Args& A, const void* in0
 }
 
 // --------------------------------------------------------------------------
-// entry points used by the launchers in kern_exact.cu / kern_mixed.cu
+// entry point used by the launcher in kern_exact.cu
 // --------------------------------------------------------------------------
 template <typename R, int DIM, int METHOD, int BC>
 cudaError_t launch_exact(const Geom& g, const Consts<R>& c, const ExactStageArgs<R>& a, int stage,
@@ -631,15 +631,6 @@ cudaError_t launch_exact(const Geom& g, const Consts<R>& c, const ExactStageArgs
   if (DIM != 3 || BC == 4) return cudaErrorNotSupported;
   typename ExactPol<R>::Args A{a, c, stage, error_word()};
   return launch3d<ExactPol<R>, METHOD, BC == 4 ? 1 : BC>(g, A, a.Yin, nullptr, st);
-}
-
-template <int DIM, int METHOD, int BC>
-cudaError_t launch_mixed(const Geom& g, const Consts<float>& c, const MixedStageArgs& a, int stage,
-                         cudaStream_t st) {
-  if (DIM != 3 || BC == 4) return cudaErrorNotSupported;
-  MixedPol::Args A{a, c, stage, error_word()};
-  return launch3d<MixedPol, METHOD, BC == 4 ? 1 : BC>(g, A, a.hi_in,
-                                                      stage == 1 ? a.lo_in : a.e_in, st);
 }
 
 }  // namespace tiled
