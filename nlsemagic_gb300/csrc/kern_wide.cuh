@@ -58,9 +58,14 @@ using tiled::tma_load_3d;
 
 typedef tiled::MixedPol::Args Args;
 
+// rows of the CTA's column (TX = 32 columns, one warp per row)
+#ifndef NLSE_WIDE_TY
+#define NLSE_WIDE_TY 8
+#endif
+
 template <int METHOD>
 struct WShape {
-  static constexpr int TX = 32, TY = 8, NT = TX * TY;
+  static constexpr int TX = 32, TY = NLSE_WIDE_TY, NT = TX * TY;
   static constexpr int H = METHOD == 2 ? 2 : 1;   // stencil reach along each axis
   static constexpr int XO = 2;                    // plane origin x0 - 2 (16-byte aligned)
   static constexpr int PX = TX + 4;               // [x0-2, x0+TX+2)
@@ -110,7 +115,7 @@ __device__ __forceinline__ mixed::HE he_of(float4 v) {
 #endif
 
 template <int METHOD, int STAGE, bool TMA>
-__global__ void __launch_bounds__(256, NLSE_WIDE_MIN_BLOCKS) wide3d(
+__global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3d(
     Geom g, Args A, int zc, GhostLayout gl, const __grid_constant__ CUtensorMap tm0,
     const __grid_constant__ CUtensorMap tm1) {
   typedef WShape<METHOD> SH;
@@ -534,7 +539,8 @@ inline int sm_count() {
 // prefers), and at least 16 planes so the 2H-plane queue fill stays small.
 inline int default_zc(const Geom& g, int H, int occ) {
   (void)H;
-  const long long cols = (long long)((g.M + 31) / 32) * ((g.N + 7) / 8);
+  const long long cols =
+      (long long)((g.M + 31) / 32) * ((g.N + NLSE_WIDE_TY - 1) / NLSE_WIDE_TY);
   const long long want = 8LL * sm_count() * (occ > 0 ? occ : 1);
   long long nbz = (want + cols - 1) / cols;
   if (nbz < 1) nbz = 1;
