@@ -145,14 +145,13 @@ __device__ __forceinline__ float4 ghost_value(const Consts<float>& c, const mixe
   return ghost_from_sums<BC>(c, ub, vb, uq, vq, lq6, mixed::lapsum<4>(ub, tn));
 }
 
-// mixed::lapsum over NN neighbours fetched by nb(t) (same operation order);
-// the accessor form lets the compiler schedule the loads without holding
-// all neighbours at once
+// mixed::lapsum over NN neighbours fetched one at a time by nb(t), in a loop
+// that is not unrolled (one neighbour live at a time; same operation order)
 template <int NN, class F>
-__device__ __forceinline__ float2 lapsum_fn(const mixed::HE& c, F nb) {
+__device__ __forceinline__ float2 lapsum_seq(const mixed::HE& c, F nb) {
   const mixed::HE n0 = nb(0);
   float2 sh = mixed::psub(n0.h, c.h), se = n0.e;
-#pragma unroll
+#pragma unroll 1
   for (int t = 1; t < NN; ++t) {
     const mixed::HE n = nb(t);
     sh = mixed::padd(sh, mixed::psub(n.h, c.h));
@@ -377,9 +376,7 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
   // is sB (planes zb-1, zb+1 in slots sD, sU), into the halo cell of plane
   // zb beyond the face.  Only the interior point next to the face reads that
   // cell, after the next barrier.
-  // (vb, vq: V at b and q, fetched by the caller ahead of the plane wait)
-  auto ghost_task = [&](unsigned tk, unsigned ob, int sD, int sB, int sU, int zb, float vb,
-                        float vq) {
+  auto ghost_task = [&](unsigned tk, unsigned ob, int sD, int sB, int sU, int zb) {
     float2 *hB = hplane(sB), *eB = eplane(sB);
     const float2 *hD = hplane(sD), *eD = eplane(sD), *hU = hplane(sU), *eU = eplane(sU);
     const unsigned pb = (unsigned)zb * MN + ob;
@@ -390,19 +387,20 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
     // (+gtp, -gtp, z+, z-)
     float2 lq6 = make_float2(0.f, 0.f);
     if (BC == 2)
-      lq6 = lapsum_fn<6>(uq, [&](int t) -> HE {
+      lq6 = lapsum_seq<6>(uq, [&](int t) -> HE {
         const int o = t < 2 ? cq : cq + (t == 2 ? PX : (t == 3 ? -PX : (t == 4 ? 1 : -1)));
         const float2* hp = t == 0 ? hU : (t == 1 ? hD : hB);
         const float2* ep = t == 0 ? eU : (t == 1 ? eD : eB);
         return HE{hp[o], ep[o]};
       });
-    const float2 st = lapsum_fn<4>(ub, [&](int t) -> HE {
+    const float2 st = lapsum_seq<4>(ub, [&](int t) -> HE {
       const int o = t < 2 ? cb + (t == 0 ? gtp : -gtp) : cb;
       const float2* hp = t < 2 ? hB : (t == 2 ? hU : hD);
       const float2* ep = t < 2 ? eB : (t == 2 ? eU : eD);
       return HE{hp[o], ep[o]};
     });
-    const float4 G = ghost_from_sums<BC>(A.c, ub, vb, uq, vq, lq6, st);
+    const float4 G =
+        ghost_from_sums<BC>(A.c, ub, A.a.V[pb], uq, A.a.V[pb + t_gstep(tk)], lq6, st);
     hB[cb - gdn] = make_float2(G.x, G.y);
     eB[cb - gdn] = make_float2(G.z, G.w);
     if (TMA) fence_proxy_async();  // before the slot's next TMA refill
@@ -442,10 +440,7 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
     if (FUSE && edge) {
       unsigned tk, ob;
       tasks(tk, ob);
-      if ((tk >> 24) & 1u) {  // planes zs-1, zs, zs+1
-        const unsigned pb = (unsigned)zs * MN + ob;
-        ghost_task(tk, ob, H - 1, H, H + 1, zs, A.a.V[pb], A.a.V[pb + t_gstep(tk)]);
-      }
+      if ((tk >> 24) & 1u) ghost_task(tk, ob, H - 1, H, H + 1, zs);  // planes zs-1, zs, zs+1
     }
     __syncthreads();  // slot 0 is refilled in the first iteration (2SHOC)
   }
@@ -470,13 +465,6 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
         const unsigned p = (unsigned)z * MN + pxy;
         float v = 0.f;
         float2 lo = make_float2(0.f, 0.f), kv = lo;
-        // fused ghost task of plane z+1: V at its face point and neighbour
-        float gvb = 0.f, gvq = 0.f;
-        if (FUSE && EDGE && ((tk >> 24) & 1u) && z + 1 < ze) {
-          const unsigned pg = (unsigned)(z + 1) * MN + ob;
-          gvb = A.a.V[pg];
-          gvq = A.a.V[pg + t_gstep(tk)];
-        }
         if (inner) {
           v = A.a.V[p];
           if (STAGE >= 2) lo = A.a.lo_in[p];
@@ -567,7 +555,7 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
           // this iteration's barrier), then the ghosts of plane z+1
           if (((tk >> 25) & 1u) && z > zs) rim_update(tk, ob, z - 1);
           if (((tk >> 24) & 1u) && z + 1 < ze)
-            ghost_task(tk, ob, sc, (u + H + 1) % NU, sn, z + 1, gvb, gvq);
+            ghost_task(tk, ob, sc, (u + H + 1) % NU, sn, z + 1);
         }
       }
     }
