@@ -389,11 +389,9 @@ def run_gpu(args, w):
         "frac": achieved / peak,
         "traffic": (traffic_ppt * n / 4.0) if traffic_ppt else None,
         "peak_kind": peak_kind,
-        "kernel": "RK4 stage (%s; %d launches per RK4 step, timed as CUDA graphs); "
-                  "achieved and traffic per average stage" %
-                  ("wide3d with the face work fused in" if solver.launches_per_step == 4
-                   else "face-ghost, interior wide3d and face kernels",
-                   solver.launches_per_step),
+        "kernel": "RK4 stage (face-ghost, interior wide3d and face kernels; %d launches "
+                  "per RK4 step, timed as CUDA graphs); achieved and traffic per average "
+                  "stage" % solver.launches_per_step,
         "algorithmic_bytes_per_point_step": BYTES_MODEL_MIXED,
         "algorithmic_bytes_per_stage": BYTES_MODEL_MIXED / 4.0 * n,
         "design_bytes_per_point_step": BYTES_DESIGN_MIXED,
@@ -406,8 +404,6 @@ def run_gpu(args, w):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32-stage/f32x2-accumulate",
         "data": "synthetic (seeded vortex rings in a harmonic trap)",
         "config": {"workload": w.name, "grid": list(w.U.shape), "method": "2SHOC", "bc": "MSD",
-                   "stage_form": "fused (face work in the interior kernel)" if args.fuse
-                   else "three kernels (face ghosts, interior, faces)",
                    "rk4_steps_per_job": steps, "k": w.k, "h": w.h,
                    "precision": "mixed (FP32 stages, compensated FP32 hi/lo state)",
                    "parallelism": "replicas x%d" % world,
@@ -584,15 +580,9 @@ def main():
     ap.add_argument("--serve-max3d", type=int, default=128)
     ap.add_argument("--serve-max-steps", type=int, default=2000)
     ap.add_argument("--serve-pool-gb", type=int, default=64)
-    ap.add_argument("--fuse", type=int, default=1, choices=[0, 1],
-                    help="mixed 3D 2SHOC form: 1 face work fused into the interior kernel "
-                         "(one launch per stage), 0 three kernels per stage (same bits)")
     ap.add_argument("--only", choices=["batched", "serving"], default=None,
                     help="run one auxiliary section alone and print its JSON (for profiling)")
     args = ap.parse_args()
-    if args.impl == "ours":
-        from nlsemagic_gb300 import autotune
-        autotune.set_knob("wide.fuse", args.fuse)
     if args.only:
         import nlsemagic_gb300 as ng
         ng.load()

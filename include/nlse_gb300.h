@@ -253,11 +253,6 @@ int nlse_take_steps_noalloc(const nlse_problem *p, const double *dUr, const doub
  *   "wide.zc"      z-chunk length of the mixed-precision 3D kernel (planes a
  *                  CTA streams through); 0 = built-in heuristic.
  *   "graph.steps"  RK4 steps per captured graph for new solvers (default 8).
- *   "wide.fuse"    1 (default): mixed-precision 3D 2SHOC solvers created
- *                  afterwards do their face work inside the interior kernel
- *                  (one launch per RK4 stage, no ghost / F scratch); 0: the
- *                  three-kernel form (face ghosts, interior, faces).  Both
- *                  give the same bits.
  * ---------------------------------------------------------------------- */
 int nlse_tune_set(const char *key, long long value);
 int nlse_tune_get(const char *key, long long *value);

@@ -11,10 +11,6 @@ knobs and keeps the fastest:
 * ``graph.steps``  RK4 steps captured per CUDA graph (launch overhead against
                    graph size; matters for small grids).
 
-The library has one more knob, ``wide.fuse`` (1 by default: the face work
-of the mixed-precision 3D 2SHOC kernel runs inside the interior kernel; 0:
-three kernels per stage).  Both give the same bits; it is not tuned here.
-
 Results are cached in a JSON file (``$NLSE_TUNE_CACHE`` or
 ``~/.cache/nlse_gb300/tune.json``) keyed by device name and problem class;
 :func:`apply` sets the knobs from the cache before a workload runs.  The

@@ -29,7 +29,6 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "--extended-lambda", "-Xcompiler", "
 UNITS = {
     "kern_exact.cu": ["-fmad=false"],
     "kern_mixed.cu": [],
-    "kern_wfuse.cu": [],
     "kern_util.cu": [],
     "nlse_abi.cu": [],
     "nlse_batch.cu": ["-fmad=false"],

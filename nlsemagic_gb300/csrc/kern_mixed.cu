@@ -7,7 +7,6 @@
 namespace nlse {
 namespace wide {
 int g_zc_override = 0;
-int g_fuse = 1;  // 3D 2SHOC: face work inside the interior kernel (one launch per stage)
 }
 
 template <int DIM, int METHOD, int BC>
@@ -51,16 +50,9 @@ static bool wide_path(const Geom& g, int BC, int kernel_kind) {
   return kernel_kind == KERNEL_TILED && g.ndim == 3 && tiled_supported(g, 3) && BC != 4;
 }
 
-// 3D 2SHOC on the wide path runs fused (no ghost / F-scratch buffers) when
-// wide::g_fuse is set at the time the buffers are sized
-static bool fused(const Geom& g, int method, int BC, int kernel_kind) {
-  return method == 2 && wide_path(g, BC, kernel_kind) && wide::g_fuse;
-}
-
-int mixed_stage_launches(const Geom& g, int method, int BC, int kernel_kind, bool ghost_buffers) {
+int mixed_stage_launches(const Geom& g, int method, int BC, int kernel_kind) {
   if (!wide_path(g, BC, kernel_kind)) return method == 2 ? 2 : 1;  // (D,) F
-  if (method == 2) return ghost_buffers ? 3 : 1;  // ghosts, interior, faces -- or fused
-  return 2;                                       // interior, faces
+  return method == 2 ? 3 : 2;  // (ghosts,) interior, faces
 }
 
 long long mixed_dsc_entries(const Geom& g, int method, int BC, int kernel_kind) {
@@ -68,13 +60,12 @@ long long mixed_dsc_entries(const Geom& g, int method, int BC, int kernel_kind) 
 }
 
 long long mixed_ghost_entries(const Geom& g, int method, int BC, int kernel_kind) {
-  if (!wide_path(g, BC, kernel_kind) || method != 2 || fused(g, method, BC, kernel_kind)) return 0;
+  if (!wide_path(g, BC, kernel_kind) || method != 2) return 0;
   return wide::GhostLayout(g).total;
 }
 
 long long mixed_fq_entries(const Geom& g, int method, int BC, int kernel_kind) {
   if (!wide_path(g, BC, kernel_kind) || method != 2 || BC != 2) return 0;
-  if (fused(g, method, BC, kernel_kind)) return 0;
   return g.n;
 }
 

@@ -82,13 +82,6 @@ struct WShape {
   static constexpr int B_OFF = NU * SLOT;
   static constexpr int SMEM = B_OFF + NU * 8;
   static constexpr unsigned TX_BYTES = (unsigned)(2 * PX * PY * 8);
-  // Fused face work (2SHOC): F of the points next to an x / y face for the
-  // face updates (two planes, by parity), F at planes 1 and L-2 for the z
-  // faces, and the ghost of each column one cell beyond a z face.
-  static constexpr int FQ_OFF = round_up(SMEM, 16);
-  static constexpr int FZ_OFF = FQ_OFF + 2 * NT * 8;
-  static constexpr int FG_OFF = FZ_OFF + 2 * NT * 8;
-  static constexpr int SMEM_F = FG_OFF + NT * 16;
 };
 
 // Ghost array layout: one entry (hi, E as float4) per point of each face,
@@ -116,176 +109,38 @@ __device__ __forceinline__ mixed::HE he_of(float4 v) {
   return r;
 }
 
-// Ghost value one cell outside the face point b:
-//   G = (h_b, E_b + delta),  delta = h^2 D_bc(b) - (Y_q - Y_b) - sum_t (Y_t - Y_b)
-// q = b's inward neighbour, t = b's four in-face neighbours; D_bc is the
-// compact scheme's boundary-condition D (for MSD from the interior D at q,
-// lh2 lq6, lq6 = sum_n (Y_n - Y_q) over q's six neighbours); st = sum_t
-// (Y_t - Y_b).
-template <int BC>
-__device__ __forceinline__ float4 ghost_from_sums(const Consts<float>& c, const mixed::HE& ub,
-                                                  float vb, const mixed::HE& uq, float vq,
-                                                  float2 lq6, float2 st) {
-  float2 dq = make_float2(0.f, 0.f);
-  if (BC == 2) dq = mixed::pmul(mixed::P2(c.lh2), lq6);  // mixed::d_interior<3>
-  const float2 dbc = mixed::d_boundary<BC>(c, ub, vb, uq, vq, dq, nullptr);
-  const float2 sq = mixed::lapsum<1>(ub, &uq);
-  const float2 delta = mixed::psub(mixed::pmul(mixed::P2(c.h2), dbc), mixed::padd(sq, st));
-  const float2 ge = mixed::padd(ub.e, delta);
-  return make_float4(ub.h.x, ub.h.y, ge.x, ge.y);
-}
-
-// the same from the neighbour values: nq = q's six neighbours in the order
-// (z+, z-, y+, y-, x+, x-), tn = b's four in-face neighbours
-template <int BC>
-__device__ __forceinline__ float4 ghost_value(const Consts<float>& c, const mixed::HE& ub, float vb,
-                                              const mixed::HE& uq, float vq, const mixed::HE* nq,
-                                              const mixed::HE* tn) {
-  const float2 lq6 = BC == 2 ? mixed::lapsum<6>(uq, nq) : make_float2(0.f, 0.f);
-  return ghost_from_sums<BC>(c, ub, vb, uq, vq, lq6, mixed::lapsum<4>(ub, tn));
-}
-
-// mixed::lapsum over NN neighbours fetched one at a time by nb(t), in a loop
-// that is not unrolled (one neighbour live at a time; same operation order)
-template <int NN, class F>
-__device__ __forceinline__ float2 lapsum_seq(const mixed::HE& c, F nb) {
-  const mixed::HE n0 = nb(0);
-  float2 sh = mixed::psub(n0.h, c.h), se = n0.e;
-#pragma unroll 1
-  for (int t = 1; t < NN; ++t) {
-    const mixed::HE n = nb(t);
-    sh = mixed::padd(sh, mixed::psub(n.h, c.h));
-    se = mixed::padd(se, n.e);
-  }
-  se = mixed::pfma(c.e, mixed::P2(-(float)NN), se);
-  return mixed::padd(sh, se);
-}
-
-// Boundary-condition F and the RK4 stage update of face point pb, from its
-// MSD neighbour pq and F there (fq, MSD only); the inputs are read from HBM.
-template <int BC, int STAGE>
-__device__ __forceinline__ void face_update(const Consts<float>& c, const MixedStageArgs& a,
-                                            const float2* Ein, unsigned pb, unsigned pq,
-                                            float2 fq) {
-  mixed::HE ub, uq;
-  ub.h = a.hi_in[pb];
-  ub.e = Ein[pb];
-  uq.h = a.hi_in[pq];
-  uq.e = Ein[pq];
-  const float2 T = mixed::f_boundary<2, BC>(c, ub, a.V[pb], uq, fq, nullptr);
-  mixed::update(c, STAGE, pb, T, a.hi_in, a.lo_in, a.e_in, a.K, a.e_out, a.hi_out, a.lo_out);
-}
-
 // resident CTAs per SM the interior kernel is compiled for (register budget)
 #ifndef NLSE_WIDE_MIN_BLOCKS
 #define NLSE_WIDE_MIN_BLOCKS 4
 #endif
 
-// FUSE (2SHOC): the face work runs in this kernel, one launch per stage.
-//   Tiles start at (32 bx - sx, TY by - sy), sx in {0, 2}, sy in {0, 1}
-//   chosen so that no tile starts at x = M-1 or y = N-1, and the last z
-//   chunk runs to L: every face point then lies in the tile and chunk of its
-//   MSD neighbour q (all coordinates clamped into [1, n-2]).
-//   - x / y ghosts of plane z+1 are computed at iteration z from the staged
-//     planes z..z+2 (by the threads of a face row, and for x faces by TY
-//     lanes of one warp) and written into the halo cell of plane z+1, which
-//     the barrier of iteration z+1 publishes to the reading thread;
-//   - the z ghosts come from HBM (plane -1 before the prologue queue load,
-//     plane L after it, each into the thread's own shared-memory entry);
-//   - F at the points next to a face is exchanged through shared memory and
-//     the face points of plane z are updated at iteration z+1 (z-face points
-//     after the loop) with the boundary formulas, reading their inputs from
-//     HBM (L2-resident: the planes were staged moments earlier).
-// The arithmetic is that of ghost3d / face2shoc, so both forms give the
-// same bits.
-template <int METHOD, int STAGE, bool TMA, int BC = 0, bool FUSE = false>
+template <int METHOD, int STAGE, bool TMA>
 __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3d(
-    Geom g, Args A, int zc, int sx, int sy, GhostLayout gl,
-    const __grid_constant__ CUtensorMap tm0, const __grid_constant__ CUtensorMap tm1) {
+    Geom g, Args A, int zc, GhostLayout gl, const __grid_constant__ CUtensorMap tm0,
+    const __grid_constant__ CUtensorMap tm1) {
   typedef WShape<METHOD> SH;
   typedef mixed::HE HE;
   constexpr int TX = SH::TX, TY = SH::TY, NT = SH::NT, H = SH::H, XO = SH::XO, PX = SH::PX,
                 PY = SH::PY, NU = SH::NU, P = SH::P;
-  static_assert(!FUSE || (METHOD == 2 && TY >= 4 && 2 * TY <= TX), "fused face work: 2SHOC");
 
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned long long* bars = reinterpret_cast<unsigned long long*>(smem + SH::B_OFF);
-  float2* FQ = reinterpret_cast<float2*>(smem + SH::FQ_OFF);
-  float2* FZ = reinterpret_cast<float2*>(smem + SH::FZ_OFF);
-  float4* FG = reinterpret_cast<float4*>(smem + SH::FG_OFF);
 
   const int M = g.M, N = g.N, L = g.L;
-  const int x0 = (int)blockIdx.x * TX - sx, y0 = (int)blockIdx.y * TY - sy;
-  const int z0 = blockIdx.z * zc;
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * zc;
   if (x0 >= M || y0 >= N || z0 >= L) return;
-  // owned planes [z0, z1)
-  const int z1 = FUSE ? (blockIdx.z == gridDim.z - 1 ? L : z0 + zc) : (z0 + zc < L ? z0 + zc : L);
-  const int zs = z0 > 1 ? z0 : 1;  // interior planes of this chunk: [zs, ze)
+  const int z1 = z0 + zc < L ? z0 + zc : L;  // owned planes [z0, z1)
+  const int zs = z0 > 1 ? z0 : 1;            // interior planes of this chunk: [zs, ze)
   const int ze = z1 < L - 1 ? z1 : L - 1;
   if (zs >= ze) return;
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
   const int x = x0 + tx, y = y0 + ty;
   const bool inner = x >= 1 && x <= M - 2 && y >= 1 && y <= N - 2;
-  // 2SHOC: CTA-uniform pre-check for columns at (or next to) an x / y face
-  const bool edge = METHOD == 2 && (FUSE ? (x0 <= 0 || x0 + TX > M - 1 || y0 <= 0 ||
-                                            y0 + TY > N - 1)
-                                         : (x0 == 0 || x0 + TX > M - 2 || y0 == 0 ||
-                                            y0 + TY > N - 2));
+  // 2SHOC: threads next to an x / y face take their +-2 neighbour across
+  // that face from the ghost array (CTA-uniform pre-check)
+  const bool edge = METHOD == 2 && (x0 == 0 || x0 + TX > M - 2 || y0 == 0 || y0 + TY > N - 2);
   const float2* Ein = STAGE == 1 ? A.a.lo_in : A.a.e_in;
   const float4* GH = A.a.gh;
-  // point offsets fit 32 bits (grids have fewer than 2^31 points)
-  const unsigned MN = (unsigned)M * (unsigned)N;
-
-  // ---- fused face tasks of this thread (constant over z) ----
-  // At most one face point b per thread, at in-plane offset ob in HBM, with a
-  // ghost task (the ghost beyond b, per plane) and / or an update task (b's
-  // stage update, per plane).  Packed into one word:
-  //   bits 0-9   cell of b in a staged plane
-  //   bits 10-11 face: 0 x = 0, 1 x = M-1, 2 y = 0, 3 y = N-1
-  //   bits 12-21 FQ index of b's MSD neighbour q
-  //   bits 22-23 x(q) - x(b) + 1 (face rows: edge points move inward in x)
-  //   bit 24     ghost task;  bit 25 update task
-  // Computed where used (in the edge-tile loop and after it), so that the
-  // interior-only loop carries none of it.
-  auto tasks = [&](unsigned& tk, unsigned& ob) {
-    tk = 0;
-    ob = 0;
-    if (!(FUSE && edge)) return;
-    if ((y == 0 || y == N - 1) && x >= 0 && x < M) {  // a face row: its own points
-      const int dy = y == 0 ? 1 : -1;
-      const int cx = x < 1 ? 1 : (x > M - 2 ? M - 2 : x);
-      ob = (unsigned)y * M + x;
-      tk = (unsigned)((ty + H) * PX + tx + XO) | (y == 0 ? 2u : 3u) << 10 |
-           (unsigned)((ty + dy) * TX + (cx - x0)) << 12 | (unsigned)(cx - x + 1) << 22 | 1u << 25;
-      if (x >= 1 && x <= M - 2) tk |= 1u << 24;
-    }
-    // x faces: lanes [0, TY) the face x = 0, [TY, 2 TY) the face x = M-1,
-    // one row each; ghosts in warp wg, updates in warp wu (not face rows)
-    int wg = TY / 2 - 1, wu = TY / 2;
-    if (y0 + wg == 0 || y0 + wg == N - 1) --wg;
-    if (y0 + wu == 0 || y0 + wu == N - 1) ++wu;
-    if ((ty == wg || ty == wu) && tx < 2 * TY) {
-      const bool hi = tx >= TY;
-      const int l = hi ? tx - TY : tx, yy = y0 + l, xf = hi ? M - 1 : 0, dx = hi ? -1 : 1;
-      if ((hi ? x0 + TX > M - 1 : x0 <= 0) && yy >= 1 && yy <= N - 2) {
-        ob = (unsigned)yy * M + xf;
-        tk = (unsigned)((l + H) * PX + (xf - x0 + XO)) | (hi ? 1u : 0u) << 10 |
-             (unsigned)(l * TX + (xf + dx - x0)) << 12 | 1u << 22 |
-             (ty == wg ? 1u << 24 : 1u << 25);
-      }
-    }
-  };
-  static_assert(NT <= 1024 && PX * PY <= 1024, "task word fields");
-  // decoded at use: face, inward cell step, in-plane HBM step from b inward
-  auto t_face = [](unsigned tk) -> unsigned { return (tk >> 10) & 3u; };
-  auto t_cdn = [&](unsigned tk) -> int {
-    const unsigned f = t_face(tk);
-    return f == 0 ? 1 : (f == 1 ? -1 : (f == 2 ? PX : -PX));
-  };
-  auto t_gstep = [&](unsigned tk) -> int {
-    const unsigned f = t_face(tk);
-    return f == 0 ? 1 : (f == 1 ? -1 : (f == 2 ? M : -M));
-  };
 
   if (TMA && (su32(smem) & 127u) != 0) {  // TMA destinations must be 128-byte aligned
     if (tid == 0) atomicExch(A.err, NLSE_ERR_STATE);
@@ -338,26 +193,13 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
   };
 
   const int own = (ty + H) * PX + tx + XO;
-  const unsigned pxy = (unsigned)y * (unsigned)M + (unsigned)x;
-  // fused: ghost of this column's z-face point (plane zb; q in plane zq), from HBM
-  auto zghost = [&](int zb, int zq) -> float4 {
-    const mixed::YIn Y{A.a.hi_in, Ein};
-    const unsigned pb = (unsigned)zb * MN + pxy, pq = (unsigned)zq * MN + pxy;
-    const HE ub = Y.at(pb), uq = Y.at(pq);
-    const HE nq[6] = {Y.at(pq + MN), Y.at(pq - MN), Y.at(pq + M),
-                      Y.at(pq - M),  Y.at(pq + 1),  Y.at(pq - 1)};
-    const HE tn[4] = {Y.at(pb + 1), Y.at(pb - 1), Y.at(pb + M), Y.at(pb - M)};
-    return ghost_value<BC>(A.c, ub, A.a.V[pb], uq, A.a.V[pq], nq, tn);
-  };
   // this thread's column value of plane zz (slot s); outside a z face (2SHOC)
-  // the ghost value of the face point below / above (fused: the thread's
-  // own FG entry, filled before the plane is queued)
+  // the ghost value of the face point below / above
   auto qload = [&](int zz, int s) -> HE {
     if (METHOD == 2 && (zz < 0 || zz >= L)) {
       HE r;
       r.h = r.e = make_float2(0.f, 0.f);
-      if (inner)
-        r = he_of(FUSE ? FG[tid] : GH[(zz < 0 ? gl.zlo : gl.zhi) + x + (long long)M * y]);
+      if (inner) r = he_of(GH[(zz < 0 ? gl.zlo : gl.zhi) + x + (long long)M * y]);
       return r;
     }
     HE r;
@@ -366,59 +208,11 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
     return r;
   };
   HE q[NU];  // q[s]: this thread's column value of the plane in slot s
-  // fused: z ghosts, each written and read by the same thread -- plane -1
-  // for the prologue, then plane L for the last iteration
-  auto zghosts = [&](bool lo) {
-    if (!(FUSE && inner)) return;
-    if (lo ? zs == 1 : ze == L - 1) FG[tid] = zghost(lo ? 0 : L - 1, lo ? 1 : L - 2);
-  };
-  // fused: x / y ghost of this thread's ghost task for plane zb, whose slot
-  // is sB (planes zb-1, zb+1 in slots sD, sU), into the halo cell of plane
-  // zb beyond the face.  Only the interior point next to the face reads that
-  // cell, after the next barrier.
-  auto ghost_task = [&](unsigned tk, unsigned ob, int sD, int sB, int sU, int zb) {
-    float2 *hB = hplane(sB), *eB = eplane(sB);
-    const float2 *hD = hplane(sD), *eD = eplane(sD), *hU = hplane(sU), *eU = eplane(sU);
-    const unsigned pb = (unsigned)zb * MN + ob;
-    const int gdn = t_cdn(tk), gtp = t_face(tk) < 2 ? PX : 1;
-    const int cb = (int)(tk & 1023u), cq = cb + gdn;
-    const HE ub = {hB[cb], eB[cb]}, uq = {hB[cq], eB[cq]};
-    // q's neighbours (z+, z-, y+, y-, x+, x-); b's in-face neighbours
-    // (+gtp, -gtp, z+, z-)
-    float2 lq6 = make_float2(0.f, 0.f);
-    if (BC == 2)
-      lq6 = lapsum_seq<6>(uq, [&](int t) -> HE {
-        const int o = t < 2 ? cq : cq + (t == 2 ? PX : (t == 3 ? -PX : (t == 4 ? 1 : -1)));
-        const float2* hp = t == 0 ? hU : (t == 1 ? hD : hB);
-        const float2* ep = t == 0 ? eU : (t == 1 ? eD : eB);
-        return HE{hp[o], ep[o]};
-      });
-    const float2 st = lapsum_seq<4>(ub, [&](int t) -> HE {
-      const int o = t < 2 ? cb + (t == 0 ? gtp : -gtp) : cb;
-      const float2* hp = t < 2 ? hB : (t == 2 ? hU : hD);
-      const float2* ep = t < 2 ? eB : (t == 2 ? eU : eD);
-      return HE{hp[o], ep[o]};
-    });
-    const float4 G =
-        ghost_from_sums<BC>(A.c, ub, A.a.V[pb], uq, A.a.V[pb + t_gstep(tk)], lq6, st);
-    hB[cb - gdn] = make_float2(G.x, G.y);
-    eB[cb - gdn] = make_float2(G.z, G.w);
-    if (TMA) fence_proxy_async();  // before the slot's next TMA refill
-  };
-  // fused: the face update of this thread's update task in plane zz
-  auto rim_update = [&](unsigned tk, unsigned ob, int zz) {
-    const unsigned pb = (unsigned)zz * MN + ob;
-    const int qs = t_gstep(tk) + (int)((tk >> 22) & 3u) - 1;
-    const float2 fq =
-        BC == 2 ? FQ[(zz & 1) * NT + (int)((tk >> 12) & 1023u)] : make_float2(0.f, 0.f);
-    face_update<BC, STAGE>(A.c, A.a, Ein, pb, pb + qs, fq);
-  };
 
   // ---- prologue: stage planes pfirst .. pfirst+2H+P-1 (slots 0..2H+P-1),
   // queue planes pfirst .. pfirst+2H-1
 #pragma unroll
   for (int t = 0; t < 2 * H + P; ++t) issue(pfirst + t, t);
-  zghosts(true);
   {
     bool ok = true;
     if (TMA && tid == 0) {
@@ -436,22 +230,16 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
     }
 #pragma unroll
     for (int t = 0; t < 2 * H; ++t) q[t] = qload(pfirst + t, t);
-    zghosts(false);
-    if (FUSE && edge) {
-      unsigned tk, ob;
-      tasks(tk, ob);
-      if ((tk >> 24) & 1u) ghost_task(tk, ob, H - 1, H, H + 1, zs);  // planes zs-1, zs, zs+1
-    }
     __syncthreads();  // slot 0 is refilled in the first iteration (2SHOC)
   }
 
+  // point offsets fit 32 bits (grids have fewer than 2^31 points)
+  const unsigned MN = (unsigned)M * (unsigned)N;
+  const unsigned pxy = (unsigned)y * (unsigned)M + (unsigned)x;
   // The z loop, instantiated for CTAs whose column touches an x / y face
   // (EDGE: ghost cells, F next to those faces) and for the others.
-  // Returns false if a wait timed out (the CTA then ends).
-  auto stream = [&](auto edge_tag) -> bool {
+  auto stream = [&](auto edge_tag) {
     constexpr bool EDGE = decltype(edge_tag)::value;
-    unsigned tk = 0, ob = 0;
-    if (FUSE && EDGE) tasks(tk, ob);
     for (int zb = zs; zb < ze; zb += NU) {
       const unsigned blk = (unsigned)((zb - zs) / NU) & 1u;
 #pragma unroll
@@ -474,7 +262,7 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
           // iterations ago, refilled two iterations on).  Only this thread
           // reads that cell (it lies outside the grid, two cells from this
           // point), so program order makes it visible.
-          if (METHOD == 2 && !FUSE && EDGE && (x == 1 || x == M - 2 || y == 1 || y == N - 2)) {
+          if (METHOD == 2 && EDGE && (x == 1 || x == M - 2 || y == 1 || y == N - 2)) {
             float2* hpc = hplane(sc);
             float2* epc = eplane(sc);
             auto put = [&](int i, float4 gv) {
@@ -499,7 +287,7 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
         }
         if (__syncthreads_or(!ok)) {
           drain(z + H + P);
-          return false;
+          return;
         }
         if (TMA) (void)tiled::mbar_try_wait(&bars[sn], par);
         q[sn] = qload(z + H, sn);
@@ -526,14 +314,7 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
                          {hp[own - 2], ep[own - 2]}};
             T = mixed::f_wide_2shoc<3>(A.c, u0, v, fn, f2n);
             // F next to a face, for the MSD formula of the face points
-            if (FUSE) {
-              if (BC == 2) {
-                if (EDGE && (x == 1 || x == M - 2 || y == 1 || y == N - 2))
-                  FQ[(z & 1) * NT + tid] = T;
-                if (z == 1) FZ[tid] = T;
-                if (z == L - 2) FZ[NT + tid] = T;
-              }
-            } else if (A.a.fq) {
+            if (A.a.fq) {
               const bool nz = z == 1 || z == L - 2;
               if (EDGE ? (nz || x == 1 || x == M - 2 || y == 1 || y == N - 2) : nz)
                 A.a.fq[p] = T;
@@ -550,38 +331,13 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
             A.a.lo_out[p] = lo2;
           }
         }
-        if (FUSE && EDGE) {
-          // face points of plane z-1 (F of their neighbours published by
-          // this iteration's barrier), then the ghosts of plane z+1
-          if (((tk >> 25) & 1u) && z > zs) rim_update(tk, ob, z - 1);
-          if (((tk >> 24) & 1u) && z + 1 < ze)
-            ghost_task(tk, ob, sc, (u + H + 1) % NU, sn, z + 1);
-        }
       }
     }
-    return true;
   };
-  const bool done = edge ? stream(std::integral_constant<bool, true>())
-                         : stream(std::integral_constant<bool, false>());
-  if (!FUSE || !done) return;
-  __syncthreads();  // F of plane ze-1 and of planes 1 / L-2 (FQ, FZ)
-  if (edge) {
-    unsigned tk, ob;
-    tasks(tk, ob);
-    if ((tk >> 25) & 1u) rim_update(tk, ob, ze - 1);
-  }
-  // z-face points of this column, q = (clamped x, clamped y, 1 or L-2)
-  if (x >= 0 && x < M && y >= 0 && y < N && (z0 == 0 || z1 == L)) {
-    const int cx = x < 1 ? 1 : (x > M - 2 ? M - 2 : x);
-    const int cy = y < 1 ? 1 : (y > N - 2 ? N - 2 : y);
-    const unsigned cxy = (unsigned)cy * M + cx;
-    const int fi = (cy - y0) * TX + (cx - x0);
-    const float2 z2 = make_float2(0.f, 0.f);
-    if (z0 == 0) face_update<BC, STAGE>(A.c, A.a, Ein, pxy, MN + cxy, BC == 2 ? FZ[fi] : z2);
-    if (z1 == L)
-      face_update<BC, STAGE>(A.c, A.a, Ein, (unsigned)(L - 1) * MN + pxy,
-                             (unsigned)(L - 2) * MN + cxy, BC == 2 ? FZ[NT + fi] : z2);
-  }
+  if (edge)
+    stream(std::integral_constant<bool, true>());
+  else
+    stream(std::integral_constant<bool, false>());
 }
 
 // ---- shell enumeration ------------------------------------------------------
@@ -726,17 +482,19 @@ __global__ void __launch_bounds__(256) ghost3d(Geom g, Args A, const ShellMap<1>
     }
     const long long pq = pb + dn;
     const mixed::HE ub = Y.at(pb), uq = Y.at(pq);
-    mixed::HE nq[6];
+    float2 dq = make_float2(0.f, 0.f);
     if (BC == 2) {
-      nq[0] = Y.at(pq + P);
-      nq[1] = Y.at(pq - P);
-      nq[2] = Y.at(pq + M);
-      nq[3] = Y.at(pq - M);
-      nq[4] = Y.at(pq + 1);
-      nq[5] = Y.at(pq - 1);
+      mixed::HE nq[6] = {Y.at(pq + P), Y.at(pq - P), Y.at(pq + M),
+                         Y.at(pq - M), Y.at(pq + 1), Y.at(pq - 1)};
+      dq = mixed::d_interior<3>(A.c, uq, nq);
     }
-    const mixed::HE tn[4] = {Y.at(pb + t1), Y.at(pb - t1), Y.at(pb + t2), Y.at(pb - t2)};
-    A.a.gh[gi] = ghost_value<BC>(A.c, ub, A.a.V[pb], uq, A.a.V[pq], nq, tn);
+    const float2 dbc = mixed::d_boundary<BC>(A.c, ub, A.a.V[pb], uq, A.a.V[pq], dq, nullptr);
+    mixed::HE tn[4] = {Y.at(pb + t1), Y.at(pb - t1), Y.at(pb + t2), Y.at(pb - t2)};
+    const float2 st = mixed::lapsum<4>(ub, tn);
+    const float2 sq = mixed::lapsum<1>(ub, &uq);
+    const float2 delta = mixed::psub(mixed::pmul(mixed::P2(A.c.h2), dbc), mixed::padd(sq, st));
+    const float2 ge = mixed::padd(ub.e, delta);
+    A.a.gh[gi] = make_float4(ub.h.x, ub.h.y, ge.x, ge.y);
   }
 }
 
@@ -792,44 +550,33 @@ inline int default_zc(const Geom& g, int H, int occ) {
   return zc;
 }
 
-// Tile origin shifts of the fused kernel: no x tile may start at M-1 and no
-// y tile at N-1 (a face and its inward neighbour share a tile).  x shifts
-// by 2 to keep the TMA box origin a multiple of 16 bytes.
-inline int fuse_sx(const Geom& g) { return (g.M - 1) % 32 == 0 ? 2 : 0; }
-inline int fuse_sy(const Geom& g) { return (g.N - 1) % NLSE_WIDE_TY == 0 ? 1 : 0; }
-
-template <int METHOD, int STAGE, bool TMA, int BC, bool FUSE>
+template <int METHOD, int STAGE, bool TMA>
 cudaError_t launch_inner(const Geom& g, const Args& A, cudaStream_t st, const CUtensorMap& m0,
                          const CUtensorMap& m1) {
   typedef WShape<METHOD> SH;
-  auto kern = wide3d<METHOD, STAGE, TMA, BC, FUSE>;
-  constexpr int SMEM = FUSE ? SH::SMEM_F : SH::SMEM;
+  auto kern = wide3d<METHOD, STAGE, TMA>;
   static int occ = 0;
   if (!occ) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
+    cudaError_t e =
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SH::SMEM);
     if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, SH::NT, SMEM);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, SH::NT, SH::SMEM);
     if (e != cudaSuccess || occ < 1) occ = 1;
   }
-  int zc = g_zc_override > 0 ? g_zc_override : default_zc(g, SH::H, occ);
-  if (zc > g.L) zc = g.L;
-  if (FUSE && zc < 2) zc = 2;  // every chunk then holds an interior plane
-  const int sx = FUSE ? fuse_sx(g) : 0, sy = FUSE ? fuse_sy(g) : 0;
-  // fused: chunks start below L-1 and the last one runs to L
-  const int nbz = FUSE ? (g.L - 1 + zc - 1) / zc : (g.L + zc - 1) / zc;
-  dim3 grid((g.M + sx + SH::TX - 1) / SH::TX, (g.N + sy + SH::TY - 1) / SH::TY, nbz);
-  kern<<<grid, dim3(SH::TX, SH::TY), SMEM, st>>>(g, A, zc, sx, sy, GhostLayout(g), m0, m1);
+  const int zc = g_zc_override > 0 ? g_zc_override : default_zc(g, SH::H, occ);
+  dim3 grid((g.M + SH::TX - 1) / SH::TX, (g.N + SH::TY - 1) / SH::TY, (g.L + zc - 1) / zc);
+  kern<<<grid, dim3(SH::TX, SH::TY), SH::SMEM, st>>>(g, A, zc, GhostLayout(g), m0, m1);
   return cudaGetLastError();
 }
 
-template <int METHOD, bool TMA, int BC, bool FUSE>
+template <int METHOD, bool TMA>
 cudaError_t launch_inner_stage(const Geom& g, const Args& A, cudaStream_t st,
                                const CUtensorMap& m0, const CUtensorMap& m1) {
   switch (A.stage) {
-    case 1: return launch_inner<METHOD, 1, TMA, BC, FUSE>(g, A, st, m0, m1);
-    case 2: return launch_inner<METHOD, 2, TMA, BC, FUSE>(g, A, st, m0, m1);
-    case 3: return launch_inner<METHOD, 3, TMA, BC, FUSE>(g, A, st, m0, m1);
-    case 4: return launch_inner<METHOD, 4, TMA, BC, FUSE>(g, A, st, m0, m1);
+    case 1: return launch_inner<METHOD, 1, TMA>(g, A, st, m0, m1);
+    case 2: return launch_inner<METHOD, 2, TMA>(g, A, st, m0, m1);
+    case 3: return launch_inner<METHOD, 3, TMA>(g, A, st, m0, m1);
+    case 4: return launch_inner<METHOD, 4, TMA>(g, A, st, m0, m1);
   }
   return cudaErrorInvalidValue;
 }
@@ -840,48 +587,27 @@ inline unsigned face_blocks(long long pts) {
   return (unsigned)(b < 1 ? 1 : (b > cap ? cap : b));
 }
 
-inline bool make_maps(const Geom& g, const Args& A, int PX, int PY, CUtensorMap& m0,
-                      CUtensorMap& m1) {
-  memset(&m0, 0, sizeof(m0));
-  memset(&m1, 0, sizeof(m1));
-  const void* ein = A.stage == 1 ? (const void*)A.a.lo_in : (const void*)A.a.e_in;
-  return tiled::make_map(&m0, A.a.hi_in, g, 1, PX, PY) &&
-         tiled::make_map(&m1, ein, g, 1, PX, PY);
-}
-
-// 2SHOC with the face work inside the interior kernel: one launch per stage
-// (instantiated for BC 1-3 in kern_wfuse.cu).
-template <int BC>
-cudaError_t launch_fused(const Geom& g, const Args& A, cudaStream_t st) {
-  typedef WShape<2> SH;
-  CUtensorMap m0, m1;
-  return make_maps(g, A, SH::PX, SH::PY, m0, m1)
-             ? launch_inner_stage<2, true, BC, true>(g, A, st, m0, m1)
-             : launch_inner_stage<2, false, BC, true>(g, A, st, m0, m1);
-}
-extern template cudaError_t launch_fused<1>(const Geom&, const Args&, cudaStream_t);
-extern template cudaError_t launch_fused<2>(const Geom&, const Args&, cudaStream_t);
-extern template cudaError_t launch_fused<3>(const Geom&, const Args&, cudaStream_t);
-
-// 3D grids, every dimension >= 3.  2SHOC: with A.a.gh (and A.a.fq for MSD)
-// three launches (ghost3d, wide3d, face2shoc); without, the fused wide3d.
+// 3D grids, every dimension >= 3.  2SHOC needs A.a.gh (and A.a.fq for MSD).
 template <int METHOD, int BC>
 cudaError_t launch(const Geom& g, const Args& A, cudaStream_t st) {
   typedef WShape<METHOD> SH;
-  if (METHOD == 2 && !A.a.gh) return launch_fused<BC>(g, A, st);
   const ShellMap<1> faces(g);
   const unsigned nb = face_blocks(faces.total);
   if (METHOD == 2) {
-    if (BC == 2 && !A.a.fq) return cudaErrorInvalidValue;
+    if (!A.a.gh || (BC == 2 && !A.a.fq)) return cudaErrorInvalidValue;
     ghost3d<BC><<<nb, 256, 0, st>>>(g, A, faces, GhostLayout(g));
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
   {
     CUtensorMap m0, m1;
-    cudaError_t e = make_maps(g, A, SH::PX, SH::PY, m0, m1)
-                        ? launch_inner_stage<METHOD, true, 0, false>(g, A, st, m0, m1)
-                        : launch_inner_stage<METHOD, false, 0, false>(g, A, st, m0, m1);
+    memset(&m0, 0, sizeof(m0));
+    memset(&m1, 0, sizeof(m1));
+    const void* ein = A.stage == 1 ? (const void*)A.a.lo_in : (const void*)A.a.e_in;
+    bool tma = tiled::make_map(&m0, A.a.hi_in, g, 1, SH::PX, SH::PY) &&
+               tiled::make_map(&m1, ein, g, 1, SH::PX, SH::PY);
+    cudaError_t e = tma ? launch_inner_stage<METHOD, true>(g, A, st, m0, m1)
+                        : launch_inner_stage<METHOD, false>(g, A, st, m0, m1);
     if (e != cudaSuccess) return e;
   }
   if (METHOD == 2)

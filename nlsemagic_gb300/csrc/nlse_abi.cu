@@ -55,7 +55,6 @@ extern "C" const char* nlse_version(void) { return "nlse_gb300 1.0 (sm_103a)"; }
 namespace nlse {
 namespace wide {
 extern int g_zc_override;
-extern int g_fuse;
 }
 }  // namespace nlse
 static int g_default_graph_steps = 8;
@@ -65,11 +64,6 @@ extern "C" int nlse_tune_set(const char* key, long long value) {
   if (!strcmp(key, "wide.zc")) {
     if (value < 0 || value > (1 << 20)) return fail(NLSE_ERR_ARG, "wide.zc out of range");
     nlse::wide::g_zc_override = (int)value;
-    return NLSE_OK;
-  }
-  if (!strcmp(key, "wide.fuse")) {
-    if (value != 0 && value != 1) return fail(NLSE_ERR_ARG, "wide.fuse must be 0 or 1");
-    nlse::wide::g_fuse = (int)value;
     return NLSE_OK;
   }
   if (!strcmp(key, "graph.steps")) {
@@ -84,10 +78,6 @@ extern "C" int nlse_tune_get(const char* key, long long* value) {
   if (!key || !value) return fail(NLSE_ERR_ARG, "NULL argument");
   if (!strcmp(key, "wide.zc")) {
     *value = nlse::wide::g_zc_override;
-    return NLSE_OK;
-  }
-  if (!strcmp(key, "wide.fuse")) {
-    *value = nlse::wide::g_fuse;
     return NLSE_OK;
   }
   if (!strcmp(key, "graph.steps")) {
@@ -585,8 +575,7 @@ extern "C" int nlse_solver_launches_per_step(const nlse_solver* s) {
   if (!s) return 0;
   if (s->prob.precision != NLSE_PREC_MIXED) return s->dsc ? 8 : 4;
   // mixed-precision 3D grids on the tiled path: deep-point kernel + shell kernel(s) per stage
-  return 4 * mixed_stage_launches(s->g, s->prob.method, s->prob.bc, s->kernel_kind,
-                                  s->gh != nullptr);
+  return 4 * mixed_stage_launches(s->g, s->prob.method, s->prob.bc, s->kernel_kind);
 }
 
 extern "C" long long nlse_solver_bytes_for(const nlse_problem* p) {

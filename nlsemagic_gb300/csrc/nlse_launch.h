@@ -32,7 +32,6 @@ struct MixedStageArgs {
   float2* hi_out;      // stage 4 output (a different buffer from hi_in)
   float2* lo_out;
   // 3D 2SHOC on the tiled path (null otherwise):
-  // (gh null: the face work runs inside the interior kernel)
   float4* gh;          // ghost values (hi, E) one cell outside each face, mixed_ghost_entries()
   float2* fq;          // F at the points next to a face (n entries, MSD only)
   float2* dsc;         // 2SHOC on the gather path: D scratch (n points), or null
@@ -50,8 +49,7 @@ cudaError_t launch_mixed_stage(const Geom& g, int method, int BC, const Consts<f
 // Kernel launches one mixed stage issues (launch_mixed_stage), and the
 // scratch the tiled 3D 2SHOC path needs: ghost entries (float4) and F
 // entries (float2) for MixedStageArgs::gh / ::fq (0 when not needed).
-// launches per RK4 stage; ghost_buffers: a 3D 2SHOC solver holds ghost3d's buffers
-int mixed_stage_launches(const Geom& g, int method, int BC, int kernel_kind, bool ghost_buffers);
+int mixed_stage_launches(const Geom& g, int method, int BC, int kernel_kind);
 long long mixed_ghost_entries(const Geom& g, int method, int BC, int kernel_kind);
 long long mixed_fq_entries(const Geom& g, int method, int BC, int kernel_kind);
 // Points of D scratch (ExactStageArgs / MixedStageArgs ::dsc) a 2SHOC stage on
