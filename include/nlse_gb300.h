@@ -253,6 +253,11 @@ int nlse_take_steps_noalloc(const nlse_problem *p, const double *dUr, const doub
  *   "wide.zc"      z-chunk length of the mixed-precision 3D kernel (planes a
  *                  CTA streams through); 0 = built-in heuristic.
  *   "graph.steps"  RK4 steps per captured graph for new solvers (default 8).
+ *   "wide.pdl"     1 (default): the mixed-precision 3D 2SHOC stage kernels
+ *                  (face ghosts, interior, faces) are launched with
+ *                  programmatic dependent launch, so a stage's interior
+ *                  tiles run while the face kernels of the stage before
+ *                  finish; 0: plain stream order.  Same bits either way.
  * ---------------------------------------------------------------------- */
 int nlse_tune_set(const char *key, long long value);
 int nlse_tune_get(const char *key, long long *value);

@@ -11,6 +11,10 @@ knobs and keeps the fastest:
 * ``graph.steps``  RK4 steps captured per CUDA graph (launch overhead against
                    graph size; matters for small grids).
 
+The library has one more knob, ``wide.pdl`` (1 by default: the 3D 2SHOC
+stage kernels overlap through programmatic dependent launch; 0: plain stream
+order).  Both give the same bits; it is not tuned here.
+
 Results are cached in a JSON file (``$NLSE_TUNE_CACHE`` or
 ``~/.cache/nlse_gb300/tune.json``) keyed by device name and problem class;
 :func:`apply` sets the knobs from the cache before a workload runs.  The

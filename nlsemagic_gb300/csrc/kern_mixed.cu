@@ -7,6 +7,7 @@
 namespace nlse {
 namespace wide {
 int g_zc_override = 0;
+int g_pdl = 1;  // 3D 2SHOC stage kernels launched with PDL
 }
 
 template <int DIM, int METHOD, int BC>

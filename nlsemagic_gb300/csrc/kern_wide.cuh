@@ -40,6 +40,7 @@
 #pragma once
 
 #include <type_traits>
+#include <utility>
 
 #include "kern_gather.cuh"
 #include "kern_tiled.cuh"
@@ -109,6 +110,64 @@ __device__ __forceinline__ mixed::HE he_of(float4 v) {
   return r;
 }
 
+// ---- programmatic dependent launch (PDL) --------------------------------------
+// A kernel launched with programmatic stream serialization may start once
+// every block of the preceding kernel has started and triggered (or exited).
+// griddepcontrol.wait blocks until that kernel has completed and its writes
+// are visible; launch_dependents is this block's trigger.  Without the launch
+// attribute both are no-ops.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Order of the interior kernel's tiles: first those whose staged region
+// (tile, 2-cell halo, chunk +-2 planes) holds no face point and no ghost, then
+// the others.  Only the others read what the kernels just before produce
+// (face points, ghosts), so only they wait on them, and as the last CTAs to
+// be dispatched they rarely wait at all.  Interior tiles: bx in
+// [ix0, ix0+nxI), by in [iy0, iy0+nyI), bz in [iz0, iz0+nzI); the rest in
+// three parts: z slabs outside the interior chunks (whole tile planes), then
+// y rows outside the interior rows, then x ends.
+struct TileOrder {
+  int nbx, nby, nbz;
+  int ix0, nxI, iy0, nyI, iz0, nzI;
+  unsigned nI, nZ, nY;  // interior tiles, z-slab tiles, y-row tiles
+  __host__ __device__ void tile(unsigned b, int& bx, int& by, int& bz) const {
+    if (b < nI) {
+      const unsigned r = b / (unsigned)nxI;
+      bx = ix0 + (int)(b - r * (unsigned)nxI);
+      by = iy0 + (int)(r % (unsigned)nyI);
+      bz = iz0 + (int)(r / (unsigned)nyI);
+      return;
+    }
+    unsigned s = b - nI;
+    const unsigned pl = (unsigned)nbx * (unsigned)nby;
+    if (s < nZ) {  // a z slab below or above the interior chunks
+      const unsigned k = s / pl, r = s - k * pl;
+      bz = (int)k < iz0 ? (int)k : (int)k + nzI;
+      by = (int)(r / (unsigned)nbx);
+      bx = (int)(r - (unsigned)by * (unsigned)nbx);
+      return;
+    }
+    s -= nZ;
+    if (s < nY) {  // a tile row below or above the interior rows
+      const unsigned ny = (unsigned)(nby - nyI), per = ny * (unsigned)nbx;
+      const unsigned k = s / per, r = s - k * per, row = r / (unsigned)nbx;
+      bz = iz0 + (int)k;
+      by = (int)row < iy0 ? (int)row : (int)row + nyI;
+      bx = (int)(r - row * (unsigned)nbx);
+      return;
+    }
+    s -= nY;  // a tile at either x end
+    const unsigned nx = (unsigned)(nbx - nxI), per = nx * (unsigned)nyI;
+    const unsigned k = s / per, r = s - k * per, row = r / nx, e = r - row * nx;
+    bz = iz0 + (int)k;
+    by = iy0 + (int)row;
+    bx = (int)e < ix0 ? (int)e : (int)e + nxI;
+  }
+};
+
 // resident CTAs per SM the interior kernel is compiled for (register budget)
 #ifndef NLSE_WIDE_MIN_BLOCKS
 #define NLSE_WIDE_MIN_BLOCKS 4
@@ -116,7 +175,7 @@ __device__ __forceinline__ mixed::HE he_of(float4 v) {
 
 template <int METHOD, int STAGE, bool TMA>
 __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3d(
-    Geom g, Args A, int zc, GhostLayout gl, const __grid_constant__ CUtensorMap tm0,
+    Geom g, Args A, int zc, TileOrder to, GhostLayout gl, const __grid_constant__ CUtensorMap tm0,
     const __grid_constant__ CUtensorMap tm1) {
   typedef WShape<METHOD> SH;
   typedef mixed::HE HE;
@@ -127,7 +186,12 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
   unsigned long long* bars = reinterpret_cast<unsigned long long*>(smem + SH::B_OFF);
 
   const int M = g.M, N = g.N, L = g.L;
-  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * zc;
+  int bx, by, bz;
+  to.tile(blockIdx.x, bx, by, bz);
+  const int x0 = bx * TX, y0 = by * TY, z0 = bz * zc;
+  // tiles that stage a face point or a ghost wait for the kernels that made
+  // them (PDL); interior tiles read only data complete before this launch
+  if (blockIdx.x >= to.nI) pdl_wait();
   if (x0 >= M || y0 >= N || z0 >= L) return;
   const int z1 = z0 + zc < L ? z0 + zc : L;  // owned planes [z0, z1)
   const int zs = z0 > 1 ? z0 : 1;            // interior planes of this chunk: [zs, ze)
@@ -255,8 +319,11 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
         float2 lo = make_float2(0.f, 0.f), kv = lo;
         if (inner) {
           v = A.a.V[p];
-          if (STAGE >= 2) lo = A.a.lo_in[p];
-          if (STAGE == 4) kv = A.a.K[p];
+          // lo and K change from step to step: read through L2 (an interior
+          // tile may start while the previous kernels still run, so no
+          // stale L1 line may serve it)
+          if (STAGE >= 2) lo = __ldcg(A.a.lo_in + p);
+          if (STAGE == 4) kv = __ldcg(A.a.K + p);
           // 2SHOC next to an x / y face: write the ghost across that face
           // into this thread's own halo cell of plane z (slot sc, landed two
           // iterations ago, refilled two iterations on).  Only this thread
@@ -452,6 +519,10 @@ __global__ void __launch_bounds__(256) shell3d(Geom g, Args A, const ShellMap<1>
 template <int BC>
 __global__ void __launch_bounds__(256) ghost3d(Geom g, Args A, const ShellMap<1> sm,
                                                GhostLayout gl) {
+  // the interior kernel's interior tiles need none of this kernel's output:
+  // let it start now, and wait for the face points of the previous stage
+  pdl_trigger();
+  pdl_wait();
   const float2* Ein = A.stage == 1 ? A.a.lo_in : A.a.e_in;
   mixed::YIn Y{A.a.hi_in, Ein};
   const int M = g.M, N = g.N, L = g.L;
@@ -501,6 +572,8 @@ __global__ void __launch_bounds__(256) ghost3d(Geom g, Args A, const ShellMap<1>
 // ---- 2SHOC: face points ------------------------------------------------------
 template <int BC>
 __global__ void __launch_bounds__(256) face2shoc(Geom g, Args A, const ShellMap<1> sm) {
+  pdl_wait();  // F next to the faces and the interior points of this stage
+  pdl_trigger();
   const float2* Ein = A.stage == 1 ? A.a.lo_in : A.a.e_in;
   mixed::YIn Y{A.a.hi_in, Ein};
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < sm.total;
@@ -550,6 +623,58 @@ inline int default_zc(const Geom& g, int H, int occ) {
   return zc;
 }
 
+extern int g_pdl;  // 2SHOC: launch the stage kernels with PDL (1) or plainly (0)
+
+// cudaLaunchKernelEx, with programmatic stream serialization when pdl is set
+template <typename... KA, typename... AA>
+cudaError_t launch_k(void (*k)(KA...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                     bool pdl, AA&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, k, std::forward<AA>(args)...);
+}
+
+// Interior ranges of the tile order: the staged region of tile bx is
+// [32 bx - 2, 32 bx + 34) in x (rows [TY by - H, TY by + TY + H), planes
+// [z0 - H, z1 - 1 + H] of the chunk's interior planes) and must lie in
+// [1, n-2] on every axis.
+inline TileOrder tile_order(const Geom& g, int TX, int TY, int H, int zc) {
+  TileOrder t;
+  t.nbx = (g.M + TX - 1) / TX;
+  t.nby = (g.N + TY - 1) / TY;
+  t.nbz = (g.L + zc - 1) / zc;
+  auto range = [](int nb, int first_ok, int last_ok, int& i0, int& n) {
+    i0 = first_ok < 0 ? 0 : first_ok;
+    const int e = last_ok < nb - 1 ? last_ok : nb - 1;
+    n = e >= i0 ? e - i0 + 1 : 0;
+  };
+  // x: 32 bx - 2 >= 1 and 32 bx + TX + 1 <= M - 2
+  range(t.nbx, (3 + TX - 1) / TX, g.M - 3 - TX >= 0 ? (g.M - 3 - TX) / TX : -1, t.ix0, t.nxI);
+  // y: TY by - H >= 1 and TY by + TY + H - 1 <= N - 2
+  range(t.nby, (H + 1 + TY - 1) / TY, g.N - 1 - TY - H >= 0 ? (g.N - 1 - TY - H) / TY : -1, t.iy0,
+        t.nyI);
+  // z: zc bz - H >= 1 and zc bz + zc - 1 + H <= L - 2 (the chunk's last plane + H)
+  range(t.nbz, (H + 1 + zc - 1) / zc, g.L - 1 - zc - H >= 0 ? (g.L - 1 - zc - H) / zc : -1,
+        t.iz0, t.nzI);
+  if (t.nxI == 0 || t.nyI == 0 || t.nzI == 0) {  // no interior tile: all in z slabs
+    t.nxI = t.nyI = t.nzI = 0;
+    t.ix0 = t.iy0 = 0;
+    t.iz0 = t.nbz;
+  }
+  t.nI = (unsigned)t.nxI * (unsigned)t.nyI * (unsigned)t.nzI;
+  t.nZ = (unsigned)(t.nbz - t.nzI) * (unsigned)t.nbx * (unsigned)t.nby;
+  t.nY = (unsigned)t.nzI * (unsigned)(t.nby - t.nyI) * (unsigned)t.nbx;
+  return t;
+}
+
 template <int METHOD, int STAGE, bool TMA>
 cudaError_t launch_inner(const Geom& g, const Args& A, cudaStream_t st, const CUtensorMap& m0,
                          const CUtensorMap& m1) {
@@ -564,9 +689,10 @@ cudaError_t launch_inner(const Geom& g, const Args& A, cudaStream_t st, const CU
     if (e != cudaSuccess || occ < 1) occ = 1;
   }
   const int zc = g_zc_override > 0 ? g_zc_override : default_zc(g, SH::H, occ);
-  dim3 grid((g.M + SH::TX - 1) / SH::TX, (g.N + SH::TY - 1) / SH::TY, (g.L + zc - 1) / zc);
-  kern<<<grid, dim3(SH::TX, SH::TY), SH::SMEM, st>>>(g, A, zc, GhostLayout(g), m0, m1);
-  return cudaGetLastError();
+  const TileOrder to = tile_order(g, SH::TX, SH::TY, SH::H, zc);
+  const unsigned nb = (unsigned)to.nbx * (unsigned)to.nby * (unsigned)to.nbz;
+  return launch_k(kern, dim3(nb), dim3(SH::TX, SH::TY), SH::SMEM, st, METHOD == 2 && g_pdl, g, A,
+                  zc, to, GhostLayout(g), m0, m1);
 }
 
 template <int METHOD, bool TMA>
@@ -595,8 +721,8 @@ cudaError_t launch(const Geom& g, const Args& A, cudaStream_t st) {
   const unsigned nb = face_blocks(faces.total);
   if (METHOD == 2) {
     if (!A.a.gh || (BC == 2 && !A.a.fq)) return cudaErrorInvalidValue;
-    ghost3d<BC><<<nb, 256, 0, st>>>(g, A, faces, GhostLayout(g));
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = launch_k(ghost3d<BC>, dim3(nb), dim3(256), 0, st, g_pdl != 0, g, A, faces,
+                             GhostLayout(g));
     if (e != cudaSuccess) return e;
   }
   {
@@ -610,10 +736,8 @@ cudaError_t launch(const Geom& g, const Args& A, cudaStream_t st) {
                         : launch_inner_stage<METHOD, false>(g, A, st, m0, m1);
     if (e != cudaSuccess) return e;
   }
-  if (METHOD == 2)
-    face2shoc<BC><<<nb, 256, 0, st>>>(g, A, faces);
-  else
-    shell3d<METHOD, BC><<<nb, 256, 0, st>>>(g, A, faces);
+  if (METHOD == 2) return launch_k(face2shoc<BC>, dim3(nb), dim3(256), 0, st, g_pdl != 0, g, A, faces);
+  shell3d<METHOD, BC><<<nb, 256, 0, st>>>(g, A, faces);
   return cudaGetLastError();
 }
 

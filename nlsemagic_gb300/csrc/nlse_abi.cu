@@ -55,6 +55,7 @@ extern "C" const char* nlse_version(void) { return "nlse_gb300 1.0 (sm_103a)"; }
 namespace nlse {
 namespace wide {
 extern int g_zc_override;
+extern int g_pdl;
 }
 }  // namespace nlse
 static int g_default_graph_steps = 8;
@@ -64,6 +65,11 @@ extern "C" int nlse_tune_set(const char* key, long long value) {
   if (!strcmp(key, "wide.zc")) {
     if (value < 0 || value > (1 << 20)) return fail(NLSE_ERR_ARG, "wide.zc out of range");
     nlse::wide::g_zc_override = (int)value;
+    return NLSE_OK;
+  }
+  if (!strcmp(key, "wide.pdl")) {
+    if (value != 0 && value != 1) return fail(NLSE_ERR_ARG, "wide.pdl must be 0 or 1");
+    nlse::wide::g_pdl = (int)value;
     return NLSE_OK;
   }
   if (!strcmp(key, "graph.steps")) {
@@ -78,6 +84,10 @@ extern "C" int nlse_tune_get(const char* key, long long* value) {
   if (!key || !value) return fail(NLSE_ERR_ARG, "NULL argument");
   if (!strcmp(key, "wide.zc")) {
     *value = nlse::wide::g_zc_override;
+    return NLSE_OK;
+  }
+  if (!strcmp(key, "wide.pdl")) {
+    *value = nlse::wide::g_pdl;
     return NLSE_OK;
   }
   if (!strcmp(key, "graph.steps")) {
@@ -241,7 +251,7 @@ struct nlse_solver {
   void *psi, *K, *ya, *yb, *V;
   void* dsc;  // 2SHOC on the gather path: D scratch (C2<R> or float2 per point)
   // mixed precision
-  float2 *hi[2], *lo[2], *mK, *da, *db, *fq;
+  float2 *hi[2], *lo[2], *mK, *da, *db, *dc, *fq;
   float4* gh;
   float* Vf;
   int cur;
@@ -290,7 +300,7 @@ extern "C" int nlse_solver_destroy(nlse_solver* s) {
   if (s->stream) cudaStreamSynchronize(s->stream);
   free_graphs(s);
   void* ptrs[] = {s->psi, s->K, s->ya, s->yb, s->V, s->hi[0], s->hi[1], s->lo[0], s->lo[1],
-                  s->mK, s->da, s->db, s->fq, s->gh, s->Vf, s->stage, s->d_mass, s->d_bad,
+                  s->mK, s->da, s->db, s->dc, s->fq, s->gh, s->Vf, s->stage, s->d_mass, s->d_bad,
                   s->dsc, s->vort, s->d_diag};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -346,6 +356,7 @@ extern "C" int nlse_solver_create(const nlse_problem* p, nlse_solver** out) {
     if (!r) r = dalloc(s, (void**)&s->mK, sizeof(float2) * n);
     if (!r) r = dalloc(s, (void**)&s->da, sizeof(float2) * n);
     if (!r) r = dalloc(s, (void**)&s->db, sizeof(float2) * n);
+    if (!r) r = dalloc(s, (void**)&s->dc, sizeof(float2) * n);
     if (!r) r = dalloc(s, (void**)&s->Vf, sizeof(float) * n);
     const long long ng = mixed_ghost_entries(s->g, p->method, p->bc, s->kernel_kind);
     const long long nf = mixed_fq_entries(s->g, p->method, p->bc, s->kernel_kind);
@@ -488,8 +499,10 @@ static int enqueue_step(nlse_solver* s) {
     float2* D = (float2*)s->dsc;
     MixedStageArgs a1{s->hi[c], s->lo[c], nullptr, s->Vf, s->mK, s->da, nullptr, nullptr, G, F, D};
     MixedStageArgs a2{s->hi[c], s->lo[c], s->da, s->Vf, s->mK, s->db, nullptr, nullptr, G, F, D};
-    MixedStageArgs a3{s->hi[c], s->lo[c], s->db, s->Vf, s->mK, s->da, nullptr, nullptr, G, F, D};
-    MixedStageArgs a4{s->hi[c], s->lo[c], s->da, s->Vf, s->mK, nullptr, s->hi[1 - c], s->lo[1 - c],
+    // three E buffers: a stage's interior kernel may start while the face
+    // kernels of the stage before still read that stage's input (PDL)
+    MixedStageArgs a3{s->hi[c], s->lo[c], s->db, s->Vf, s->mK, s->dc, nullptr, nullptr, G, F, D};
+    MixedStageArgs a4{s->hi[c], s->lo[c], s->dc, s->Vf, s->mK, nullptr, s->hi[1 - c], s->lo[1 - c],
                       G, F, D};
     const MixedStageArgs* as[4] = {&a1, &a2, &a3, &a4};
     for (int st = 1; st <= 4 && e == cudaSuccess; ++st)
@@ -588,7 +601,7 @@ extern "C" long long nlse_solver_bytes_for(const nlse_problem* p) {
     const long long es = p->precision == NLSE_PREC_DOUBLE ? 8 : 4;
     b = 4 * 2 * es * n + es * n + 2 * es * exact_dsc_entries(g, p->method, p->bc, kind);
   } else {
-    b = 7 * 8 * n + 4 * n + 16 * mixed_ghost_entries(g, p->method, p->bc, kind) +
+    b = 8 * 8 * n + 4 * n + 16 * mixed_ghost_entries(g, p->method, p->bc, kind) +
         8 * mixed_fq_entries(g, p->method, p->bc, kind) +
         8 * mixed_dsc_entries(g, p->method, p->bc, kind);
   }
