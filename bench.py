@@ -404,6 +404,8 @@ def run_gpu(args, w):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32-stage/f32x2-accumulate",
         "data": "synthetic (seeded vortex rings in a harmonic trap)",
         "config": {"workload": w.name, "grid": list(w.U.shape), "method": "2SHOC", "bc": "MSD",
+                   "launch": "programmatic dependent launch (interior tiles overlap the face "
+                   "kernels)" if args.pdl else "stream order",
                    "rk4_steps_per_job": steps, "k": w.k, "h": w.h,
                    "precision": "mixed (FP32 stages, compensated FP32 hi/lo state)",
                    "parallelism": "replicas x%d" % world,
@@ -580,9 +582,15 @@ def main():
     ap.add_argument("--serve-max3d", type=int, default=128)
     ap.add_argument("--serve-max-steps", type=int, default=2000)
     ap.add_argument("--serve-pool-gb", type=int, default=64)
+    ap.add_argument("--pdl", type=int, default=1, choices=[0, 1],
+                    help="3D 2SHOC stage kernels: 1 overlap through programmatic dependent "
+                         "launch, 0 plain stream order (same bits)")
     ap.add_argument("--only", choices=["batched", "serving"], default=None,
                     help="run one auxiliary section alone and print its JSON (for profiling)")
     args = ap.parse_args()
+    if args.impl == "ours":
+        from nlsemagic_gb300 import autotune
+        autotune.set_knob("wide.pdl", args.pdl)
     if args.only:
         import nlsemagic_gb300 as ng
         ng.load()

@@ -258,6 +258,8 @@ int nlse_take_steps_noalloc(const nlse_problem *p, const double *dUr, const doub
  *                  programmatic dependent launch, so a stage's interior
  *                  tiles run while the face kernels of the stage before
  *                  finish; 0: plain stream order.  Same bits either way.
+ *   "face.blocks_per_sm"  blocks of 256 threads per SM of the 3D face
+ *                  kernels (1-64, default 8; grid-stride beyond).
  * ---------------------------------------------------------------------- */
 int nlse_tune_set(const char *key, long long value);
 int nlse_tune_get(const char *key, long long *value);

@@ -707,9 +707,11 @@ cudaError_t launch_inner_stage(const Geom& g, const Args& A, cudaStream_t st,
   return cudaErrorInvalidValue;
 }
 
+extern int g_face_bps;  // face-kernel blocks per SM (grid-stride beyond)
+
 inline unsigned face_blocks(long long pts) {
   long long b = (pts + 255) / 256;
-  const long long cap = (long long)sm_count() * 16;
+  const long long cap = (long long)sm_count() * g_face_bps;
   return (unsigned)(b < 1 ? 1 : (b > cap ? cap : b));
 }
 

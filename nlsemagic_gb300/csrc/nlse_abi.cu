@@ -56,6 +56,7 @@ namespace nlse {
 namespace wide {
 extern int g_zc_override;
 extern int g_pdl;
+extern int g_face_bps;
 }
 }  // namespace nlse
 static int g_default_graph_steps = 8;
@@ -65,6 +66,11 @@ extern "C" int nlse_tune_set(const char* key, long long value) {
   if (!strcmp(key, "wide.zc")) {
     if (value < 0 || value > (1 << 20)) return fail(NLSE_ERR_ARG, "wide.zc out of range");
     nlse::wide::g_zc_override = (int)value;
+    return NLSE_OK;
+  }
+  if (!strcmp(key, "face.blocks_per_sm")) {
+    if (value < 1 || value > 64) return fail(NLSE_ERR_ARG, "face.blocks_per_sm out of range");
+    nlse::wide::g_face_bps = (int)value;
     return NLSE_OK;
   }
   if (!strcmp(key, "wide.pdl")) {
@@ -84,6 +90,10 @@ extern "C" int nlse_tune_get(const char* key, long long* value) {
   if (!key || !value) return fail(NLSE_ERR_ARG, "NULL argument");
   if (!strcmp(key, "wide.zc")) {
     *value = nlse::wide::g_zc_override;
+    return NLSE_OK;
+  }
+  if (!strcmp(key, "face.blocks_per_sm")) {
+    *value = nlse::wide::g_face_bps;
     return NLSE_OK;
   }
   if (!strcmp(key, "wide.pdl")) {
