@@ -81,10 +81,9 @@ struct WShape {
   static constexpr int PLANE = round_up(PX * PY * 8, 128);
   static constexpr int SLOT = 2 * PLANE;          // hi plane + E plane
   static constexpr int B_OFF = NU * SLOT;
-  // NU "full" mbarriers (plane landed), then per slot the count of warps
-  // done with its plane and the plane last issued into it, then the CTA's
-  // abort flag
-  static constexpr int SMEM = B_OFF + NU * 8 + 2 * NU * 4 + 16;
+  // mbarriers: NU "full" (plane landed), NU "empty" (plane released by every
+  // warp), then the CTA's abort flag
+  static constexpr int SMEM = B_OFF + 2 * NU * 8 + 16;
   static constexpr unsigned TX_BYTES = (unsigned)(2 * PX * PY * 8);
 };
 
@@ -171,6 +170,9 @@ struct TileOrder {
   }
 };
 
+__device__ __forceinline__ void mbar_arrive(unsigned long long* b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tiled::su32(b)) : "memory");
+}
 // bounded wait for mbarrier phase `parity`, given up early when the CTA's
 // abort flag is set
 __device__ __forceinline__ bool mbar_wait_or_abort(unsigned long long* b, unsigned parity,
@@ -224,21 +226,18 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
     if (tid == 0) atomicExch(A.err, NLSE_ERR_STATE);
     return;
   }
-  // TMA staging runs as a pipeline.  full[s] completes when the plane in
-  // slot s has landed; each warp waits for it on its own.  When a warp is
-  // done with a plane it counts itself in the slot's counter, and the last
-  // warp to do so refills the slot with the plane NU further on.  There is no
-  // CTA barrier per plane: warps drift apart by up to the ring's slack, and
-  // a refill goes out as soon as the slowest warp has released the slot.
-  int* cnt = reinterpret_cast<int*>(smem + SH::B_OFF + NU * 8);
-  volatile int* occ = cnt + NU;  // plane last issued into each slot (drain)
-  volatile int* abort_flag = reinterpret_cast<volatile int*>(cnt + 2 * NU);
+  // TMA staging runs as a pipeline: full[s] completes when the plane in
+  // slot s has landed; empty[s] when every warp has done with it (one
+  // arrival per warp).  The producer (thread 0) refills a slot only after its
+  // previous plane is released, so warps drift apart by up to the ring's
+  // slack instead of meeting at a CTA barrier every plane.
+  unsigned long long* emp = bars + NU;
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + SH::B_OFF + 2 * NU * 8);
   const int lane = tid & 31;
   if (TMA && tid == 0) {
     for (int s = 0; s < NU; ++s) {
       mbar_init(&bars[s], 1);
-      cnt[s] = 0;
-      occ[s] = -1;
+      mbar_init(&emp[s], NT / 32);
     }
     *abort_flag = 0;
     fence_mbar_init();
@@ -252,8 +251,7 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
   auto eplane = [&](int s) -> float2* {
     return reinterpret_cast<float2*>(smem + s * SH::SLOT + SH::PLANE);
   };
-  auto issue_tma = [&](int zz, int s) {
-    occ[s] = zz;
+  auto issue_tma = [&](int zz, int s) {  // thread 0
     fence_proxy_async();  // earlier generic accesses of the slot before the async write
     mbar_expect_tx(&bars[s], SH::TX_BYTES);
     tma_load_3d(hplane(s), &tm0, x0 - XO, y0 - H, zz, &bars[s]);
@@ -278,28 +276,13 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
       }
     }
   };
-  // error path of the pipeline: wait (bounded) until the last plane issued
-  // into each slot has landed, so that no copy is in flight when the CTA
-  // ends.  Every lane 0 does this before leaving; one that issues later
-  // drains again on its own way out.
-  auto drain_all = [&]() {
-    if (!TMA || lane != 0) return;
-    for (int s = 0; s < NU; ++s) {
-      const int o = occ[s];
-      if (o >= pfirst) mbar_wait(&bars[s], (unsigned)(((o - pfirst) / NU) & 1));
-    }
-  };
-  // the warp is done with plane zz (slot s): count it; the last warp refills
-  // the slot with plane zz + NU
-  auto release = [&](int zz, int s) {
-    __syncwarp();
-    if (lane != 0) return;
-    __threadfence_block();  // this warp's reads of the slot before the count
-    if (atomicAdd(&cnt[s], 1) == NT / 32 - 1) {
-      cnt[s] = 0;
-      __threadfence_block();  // every warp's reads before the refill
-      if (zz + NU <= plast && !*abort_flag) issue_tma(zz + NU, s);
-    }
+  // bounded wait for every plane issued up to `upto` (error path only)
+  auto drain = [&](int upto) {
+    if (!TMA || tid != 0) return;
+    if (upto > plast) upto = plast;
+    int from = upto - NU + 1 > pfirst ? upto - NU + 1 : pfirst;
+    for (int zz = from; zz <= upto; ++zz)
+      mbar_wait(&bars[(zz - pfirst) % NU], (unsigned)(((zz - pfirst) / NU) & 1));
   };
 
   const int own = (ty + H) * PX + tx + XO;
@@ -318,16 +301,13 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
     return r;
   };
   HE q[NU];  // q[s]: this thread's column value of the plane in slot s
+  // last plane thread 0 has issued (TMA pipeline; for drain on abort)
+  int issued = pfirst + 2 * H + P - 1 < plast ? pfirst + 2 * H + P - 1 : plast;
 
   // ---- prologue: stage planes pfirst .. pfirst+2H+P-1 (slots 0..2H+P-1),
   // queue planes pfirst .. pfirst+2H-1
 #pragma unroll
   for (int t = 0; t < 2 * H + P; ++t) issue(pfirst + t, t);
-  if (TMA && tid == 0) {  // the pipeline fills the whole ring up front
-#pragma unroll
-    for (int t = 2 * H + P; t < NU; ++t)
-      if (pfirst + t <= plast) issue_tma(pfirst + t, t);
-  }
   {
     bool ok = true;
     if (TMA && tid == 0) {
@@ -336,7 +316,7 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
       if (!ok) atomicExch(A.err, NLSE_ERR_TIMEOUT);
     }
     if (__syncthreads_or(!ok)) {
-      drain_all();  // TMA: every copy issued so far lands before the CTA ends
+      drain(pfirst + 2 * H + P - 1);
       return;
     }
     if (TMA) {
@@ -347,8 +327,11 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
     for (int t = 0; t < 2 * H; ++t) q[t] = qload(pfirst + t, t);
     if (TMA) {
       // planes pfirst .. zs-1 are read only here: release their slots
+      __syncwarp();
+      if (lane == 0) {
 #pragma unroll
-      for (int t = 0; t < H; ++t) release(pfirst + t, t);
+        for (int t = 0; t < H; ++t) mbar_arrive(&emp[t]);
+      }
     } else {
       __syncthreads();  // slot 0 is refilled in the first iteration (2SHOC)
     }
@@ -369,7 +352,26 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
         if (z >= ze) break;
         const int sc = (u + H) % NU;      // slot of plane z
         const int sn = (u + 2 * H) % NU;  // slot of plane z+H (queue head)
-        if (!TMA) {
+        if (TMA) {
+          // refill slot (u+2H+P) % NU with plane z+H+P once every warp has
+          // released the slot's previous plane zi - NU (its k-th release
+          // completes phase k of empty[slot])
+          const int zi = z + H + P;
+          if (tid == 0 && zi <= plast) {
+            const int slot = (u + 2 * H + P) % NU, pp = zi - NU;
+            bool okp = true;
+            if (pp >= pfirst)
+              okp = mbar_wait_or_abort(&emp[slot], (unsigned)(((pp - pfirst) / NU) & 1),
+                                       abort_flag);
+            if (okp) {
+              issue_tma(zi, slot);
+              issued = zi;
+            } else if (!*abort_flag) {
+              *abort_flag = 1;
+              atomicExch(A.err, NLSE_ERR_TIMEOUT);
+            }
+          }
+        } else {
           issue(z + H + P, (u + 2 * H + P) % NU);
         }
         // pointwise operands of the interior point, fetched before the wait
@@ -413,7 +415,7 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
           }
           __syncwarp();
           if (*abort_flag) {
-            drain_all();  // copies in flight land before the CTA ends
+            drain(issued);  // thread 0: copies in flight land before the CTA ends
             return;
           }
           (void)tiled::mbar_try_wait(&bars[sn], par);
@@ -462,7 +464,10 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
             A.a.lo_out[p] = lo2;
           }
         }
-        if (TMA) release(z, sc);  // this warp is done with plane z
+        if (TMA) {  // this warp is done with plane z
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&emp[sc]);
+        }
       }
     }
   };
