@@ -81,9 +81,7 @@ struct WShape {
   static constexpr int PLANE = round_up(PX * PY * 8, 128);
   static constexpr int SLOT = 2 * PLANE;          // hi plane + E plane
   static constexpr int B_OFF = NU * SLOT;
-  // mbarriers: NU "full" (plane landed), NU "empty" (plane released by every
-  // warp), then the CTA's abort flag
-  static constexpr int SMEM = B_OFF + 2 * NU * 8 + 16;
+  static constexpr int SMEM = B_OFF + NU * 8;
   static constexpr unsigned TX_BYTES = (unsigned)(2 * PX * PY * 8);
 };
 
@@ -170,20 +168,6 @@ struct TileOrder {
   }
 };
 
-__device__ __forceinline__ void mbar_arrive(unsigned long long* b) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tiled::su32(b)) : "memory");
-}
-// bounded wait for mbarrier phase `parity`, given up early when the CTA's
-// abort flag is set
-__device__ __forceinline__ bool mbar_wait_or_abort(unsigned long long* b, unsigned parity,
-                                                   const volatile int* abort) {
-  for (int it = 0; it < (1 << 22); ++it) {
-    if (tiled::mbar_try_wait(b, parity)) return true;
-    if (*abort) return false;
-  }
-  return false;
-}
-
 // resident CTAs per SM the interior kernel is compiled for (register budget)
 #ifndef NLSE_WIDE_MIN_BLOCKS
 #define NLSE_WIDE_MIN_BLOCKS 4
@@ -226,20 +210,8 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
     if (tid == 0) atomicExch(A.err, NLSE_ERR_STATE);
     return;
   }
-  // TMA staging runs as a pipeline: full[s] completes when the plane in
-  // slot s has landed; empty[s] when every warp has done with it (one
-  // arrival per warp).  The producer (thread 0) refills a slot only after its
-  // previous plane is released, so warps drift apart by up to the ring's
-  // slack instead of meeting at a CTA barrier every plane.
-  unsigned long long* emp = bars + NU;
-  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + SH::B_OFF + 2 * NU * 8);
-  const int lane = tid & 31;
   if (TMA && tid == 0) {
-    for (int s = 0; s < NU; ++s) {
-      mbar_init(&bars[s], 1);
-      mbar_init(&emp[s], NT / 32);
-    }
-    *abort_flag = 0;
+    for (int s = 0; s < NU; ++s) mbar_init(&bars[s], 1);
     fence_mbar_init();
   }
   __syncthreads();
@@ -251,16 +223,15 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
   auto eplane = [&](int s) -> float2* {
     return reinterpret_cast<float2*>(smem + s * SH::SLOT + SH::PLANE);
   };
-  auto issue_tma = [&](int zz, int s) {  // thread 0
-    fence_proxy_async();  // earlier generic accesses of the slot before the async write
-    mbar_expect_tx(&bars[s], SH::TX_BYTES);
-    tma_load_3d(hplane(s), &tm0, x0 - XO, y0 - H, zz, &bars[s]);
-    tma_load_3d(eplane(s), &tm1, x0 - XO, y0 - H, zz, &bars[s]);
-  };
   auto issue = [&](int zz, int s) {
     if (zz > plast) return;
     if (TMA) {
-      if (tid == 0) issue_tma(zz, s);
+      if (tid == 0) {
+        fence_proxy_async();  // earlier generic accesses of the slot before the async write
+        mbar_expect_tx(&bars[s], SH::TX_BYTES);
+        tma_load_3d(hplane(s), &tm0, x0 - XO, y0 - H, zz, &bars[s]);
+        tma_load_3d(eplane(s), &tm1, x0 - XO, y0 - H, zz, &bars[s]);
+      }
     } else {
       for (int t = tid; t < PX * PY; t += NT) {
         int ux = t % PX, uy = t / PX;
@@ -301,8 +272,6 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
     return r;
   };
   HE q[NU];  // q[s]: this thread's column value of the plane in slot s
-  // last plane thread 0 has issued (TMA pipeline; for drain on abort)
-  int issued = pfirst + 2 * H + P - 1 < plast ? pfirst + 2 * H + P - 1 : plast;
 
   // ---- prologue: stage planes pfirst .. pfirst+2H+P-1 (slots 0..2H+P-1),
   // queue planes pfirst .. pfirst+2H-1
@@ -325,16 +294,7 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
     }
 #pragma unroll
     for (int t = 0; t < 2 * H; ++t) q[t] = qload(pfirst + t, t);
-    if (TMA) {
-      // planes pfirst .. zs-1 are read only here: release their slots
-      __syncwarp();
-      if (lane == 0) {
-#pragma unroll
-        for (int t = 0; t < H; ++t) mbar_arrive(&emp[t]);
-      }
-    } else {
-      __syncthreads();  // slot 0 is refilled in the first iteration (2SHOC)
-    }
+    __syncthreads();  // slot 0 is refilled in the first iteration (2SHOC)
   }
 
   // point offsets fit 32 bits (grids have fewer than 2^31 points)
@@ -352,28 +312,7 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
         if (z >= ze) break;
         const int sc = (u + H) % NU;      // slot of plane z
         const int sn = (u + 2 * H) % NU;  // slot of plane z+H (queue head)
-        if (TMA) {
-          // refill slot (u+2H+P) % NU with plane z+H+P once every warp has
-          // released the slot's previous plane zi - NU (its k-th release
-          // completes phase k of empty[slot])
-          const int zi = z + H + P;
-          if (tid == 0 && zi <= plast) {
-            const int slot = (u + 2 * H + P) % NU, pp = zi - NU;
-            bool okp = true;
-            if (pp >= pfirst)
-              okp = mbar_wait_or_abort(&emp[slot], (unsigned)(((pp - pfirst) / NU) & 1),
-                                       abort_flag);
-            if (okp) {
-              issue_tma(zi, slot);
-              issued = zi;
-            } else if (!*abort_flag) {
-              *abort_flag = 1;
-              atomicExch(A.err, NLSE_ERR_TIMEOUT);
-            }
-          }
-        } else {
-          issue(z + H + P, (u + 2 * H + P) % NU);
-        }
+        issue(z + H + P, (u + 2 * H + P) % NU);
         // pointwise operands of the interior point, fetched before the wait
         const unsigned p = (unsigned)z * MN + pxy;
         float v = 0.f;
@@ -404,25 +343,20 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
             if (TMA) fence_proxy_async();  // before the slot's next TMA refill
           }
         }
+        // one thread waits for the queue-head plane (bounded); the barrier
+        // releases the rest, and each thread then takes the completed phase
+        // with one try_wait (succeeds at once; acquires the TMA writes)
         const unsigned par = blk ^ (unsigned)((u + 2 * H) / NU);
-        if (TMA) {
-          // one lane per warp waits for the queue-head plane (bounded), then
-          // every lane takes the completed phase with one try_wait (succeeds
-          // at once; acquires the TMA writes)
-          if (lane == 0 && !mbar_wait_or_abort(&bars[sn], par, abort_flag) && !*abort_flag) {
-            *abort_flag = 1;
-            atomicExch(A.err, NLSE_ERR_TIMEOUT);
-          }
-          __syncwarp();
-          if (*abort_flag) {
-            drain(issued);  // thread 0: copies in flight land before the CTA ends
-            return;
-          }
-          (void)tiled::mbar_try_wait(&bars[sn], par);
-        } else {
-          // plain staging: the CTA barrier orders the cooperative stores
-          if (__syncthreads_or(0)) return;
+        bool ok = true;
+        if (TMA && tid == 0) {
+          ok = mbar_wait(&bars[sn], par);
+          if (!ok) atomicExch(A.err, NLSE_ERR_TIMEOUT);
         }
+        if (__syncthreads_or(!ok)) {
+          drain(z + H + P);
+          return;
+        }
+        if (TMA) (void)tiled::mbar_try_wait(&bars[sn], par);
         q[sn] = qload(z + H, sn);
 
         if (inner) {
@@ -463,10 +397,6 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
             A.a.hi_out[p] = ho;
             A.a.lo_out[p] = lo2;
           }
-        }
-        if (TMA) {  // this warp is done with plane z
-          __syncwarp();
-          if (lane == 0) mbar_arrive(&emp[sc]);
         }
       }
     }
