@@ -515,10 +515,45 @@ __global__ void __launch_bounds__(256) shell3d(Geom g, Args A, const ShellMap<1>
 // For every face-interior point b (exactly one boundary coordinate):
 //   G = (h_b, E_b + delta),  delta = h^2 D_bc(b) - (Y_q - Y_b) - sum_t (Y_t - Y_b)
 // with D_bc the boundary-condition D of the compact scheme (mixed::d_boundary,
-// for MSD from the interior D at q).  Edge and corner points have no ghost.
+// for MSD from the interior D at q), q = b's inward neighbour, nq = q's six
+// neighbours (z+, z-, y+, y-, x+, x-), tn = b's four in-face neighbours.
+// Edge and corner points have no ghost.
+template <int BC>
+__device__ __forceinline__ float4 ghost_value(const Consts<float>& c, const mixed::HE& ub, float vb,
+                                              const mixed::HE& uq, float vq, const mixed::HE* nq,
+                                              const mixed::HE* tn) {
+  float2 dq = make_float2(0.f, 0.f);
+  if (BC == 2) dq = mixed::d_interior<3>(c, uq, nq);
+  const float2 dbc = mixed::d_boundary<BC>(c, ub, vb, uq, vq, dq, nullptr);
+  const float2 st = mixed::lapsum<4>(ub, tn);
+  const float2 sq = mixed::lapsum<1>(ub, &uq);
+  const float2 delta = mixed::psub(mixed::pmul(mixed::P2(c.h2), dbc), mixed::padd(sq, st));
+  const float2 ge = mixed::padd(ub.e, delta);
+  return make_float4(ub.h.x, ub.h.y, ge.x, ge.y);
+}
+
+// x-face ghosts by patches of XG_Y rows x XG_Z planes of one face per block.
+// x faces are strided in memory: a ghost there touches ten 32-byte sectors
+// (five rows or planes, hi and E) of which it uses one or two elements, and
+// neighbouring ghosts re-request the same sectors.  A block stages the four
+// columns next to the face for its patch and a one-cell halo with 32-byte
+// row segments, so each sector is read once per patch.
+constexpr int XG_Y = 32, XG_Z = 8;
+struct XPatches {
+  int npy, npz;
+  unsigned nblk;  // 2 faces x npy x npz
+  explicit XPatches(const Geom& g) {
+    npy = (g.N - 2 + XG_Y - 1) / XG_Y;
+    npz = (g.L - 2 + XG_Z - 1) / XG_Z;
+    nblk = 2u * (unsigned)npy * (unsigned)npz;
+  }
+};
+
+// Blocks [0, xp.nblk): x-face patches; the rest: the y and z faces (the
+// shell map's z slabs and y rows, which hold no x-face-interior point).
 template <int BC>
 __global__ void __launch_bounds__(256) ghost3d(Geom g, Args A, const ShellMap<1> sm,
-                                               GhostLayout gl) {
+                                               GhostLayout gl, XPatches xp) {
   // the interior kernel's interior tiles need none of this kernel's output:
   // let it start now, and wait for the face points of the previous stage
   pdl_trigger();
@@ -527,20 +562,71 @@ __global__ void __launch_bounds__(256) ghost3d(Geom g, Args A, const ShellMap<1>
   mixed::YIn Y{A.a.hi_in, Ein};
   const int M = g.M, N = g.N, L = g.L;
   const long long P = (long long)M * N;
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < sm.total;
-       t += (long long)gridDim.x * blockDim.x) {
+  typedef mixed::HE HE;
+  if (blockIdx.x < xp.nblk) {
+    __shared__ float2 sh[XG_Z + 2][XG_Y + 2][4], se[XG_Z + 2][XG_Y + 2][4];
+    const unsigned per = (unsigned)xp.npy * (unsigned)xp.npz;
+    const int side = blockIdx.x >= per;
+    const unsigned r = blockIdx.x - (side ? per : 0u);
+    const int pz = (int)(r / (unsigned)xp.npy), py = (int)(r - (unsigned)pz * xp.npy);
+    const int ya = 1 + XG_Y * py, za = 1 + XG_Z * pz;
+    const int ny = N - 1 - ya < XG_Y ? N - 1 - ya : XG_Y;
+    const int nz = L - 1 - za < XG_Z ? L - 1 - za : XG_Z;
+    const int xb = side ? M - 4 : 0;  // grid x of staged column 0
+    const int R = ny + 2, cells = R * (nz + 2) * 4;
+    for (int i = threadIdx.x; i < cells; i += blockDim.x) {
+      const int c = i & 3, k = i >> 2, rr = k % R, zz = k / R;
+      const int gx = xb + c;
+      float2 h = make_float2(0.f, 0.f), e = h;
+      if (gx >= 0 && gx < M) {
+        const long long p = ((long long)(za - 1 + zz) * N + (ya - 1 + rr)) * M + gx;
+        h = A.a.hi_in[p];
+        e = Ein[p];
+      }
+      sh[zz][rr][c] = h;
+      se[zz][rr][c] = e;
+    }
+    __syncthreads();
+    const int ly = threadIdx.x % XG_Y, lz = threadIdx.x / XG_Y;
+    if (ly < ny && lz < nz) {
+      const int cb = side ? M - 1 - xb : 0, dn = side ? -1 : 1, cq = cb + dn;
+      const int rr = ly + 1, zz = lz + 1;
+      auto at = [&](int z_, int r_, int c_) -> HE {
+        HE v;
+        v.h = sh[z_][r_][c_];
+        v.e = se[z_][r_][c_];
+        return v;
+      };
+      const HE ub = at(zz, rr, cb), uq = at(zz, rr, cq);
+      HE nq[6];
+      if (BC == 2) {
+        nq[0] = at(zz + 1, rr, cq);
+        nq[1] = at(zz - 1, rr, cq);
+        nq[2] = at(zz, rr + 1, cq);
+        nq[3] = at(zz, rr - 1, cq);
+        nq[4] = at(zz, rr, cq + 1);
+        nq[5] = at(zz, rr, cq - 1);
+      }
+      const HE tn[4] = {at(zz, rr + 1, cb), at(zz, rr - 1, cb), at(zz + 1, rr, cb),
+                        at(zz - 1, rr, cb)};
+      const int y = ya + ly, z = za + lz;
+      const long long pb = ((long long)z * N + y) * M + (side ? M - 1 : 0);
+      A.a.gh[(side ? gl.xhi : gl.xlo) + y + (long long)N * z] =
+          ghost_value<BC>(A.c, ub, A.a.V[pb], uq, A.a.V[pb + dn], nq, tn);
+    }
+    return;
+  }
+  const long long nyz = sm.nz + sm.ny;
+  const long long stride = (long long)(gridDim.x - xp.nblk) * blockDim.x;
+  for (long long t = (long long)(blockIdx.x - xp.nblk) * blockDim.x + threadIdx.x; t < nyz;
+       t += stride) {
     int x, y, z;
     shell_coord(sm, t, x, y, z);
     const bool bx = x == 0 || x == M - 1, by = y == 0 || y == N - 1, bz = z == 0 || z == L - 1;
     if ((int)bx + (int)by + (int)bz != 1) continue;
     const long long pb = lin(g, z, y, x);
     long long dn, t1, t2, gi;  // inward step, in-face steps, ghost index
-    if (bx) {
-      dn = x == 0 ? 1 : -1;
-      t1 = M;
-      t2 = P;
-      gi = (x == 0 ? gl.xlo : gl.xhi) + y + (long long)N * z;
-    } else if (by) {
+    if (by) {
       dn = y == 0 ? M : -(long long)M;
       t1 = 1;
       t2 = P;
@@ -552,20 +638,18 @@ __global__ void __launch_bounds__(256) ghost3d(Geom g, Args A, const ShellMap<1>
       gi = (z == 0 ? gl.zlo : gl.zhi) + x + (long long)M * y;
     }
     const long long pq = pb + dn;
-    const mixed::HE ub = Y.at(pb), uq = Y.at(pq);
-    float2 dq = make_float2(0.f, 0.f);
+    const HE ub = Y.at(pb), uq = Y.at(pq);
+    HE nq[6];
     if (BC == 2) {
-      mixed::HE nq[6] = {Y.at(pq + P), Y.at(pq - P), Y.at(pq + M),
-                         Y.at(pq - M), Y.at(pq + 1), Y.at(pq - 1)};
-      dq = mixed::d_interior<3>(A.c, uq, nq);
+      nq[0] = Y.at(pq + P);
+      nq[1] = Y.at(pq - P);
+      nq[2] = Y.at(pq + M);
+      nq[3] = Y.at(pq - M);
+      nq[4] = Y.at(pq + 1);
+      nq[5] = Y.at(pq - 1);
     }
-    const float2 dbc = mixed::d_boundary<BC>(A.c, ub, A.a.V[pb], uq, A.a.V[pq], dq, nullptr);
-    mixed::HE tn[4] = {Y.at(pb + t1), Y.at(pb - t1), Y.at(pb + t2), Y.at(pb - t2)};
-    const float2 st = mixed::lapsum<4>(ub, tn);
-    const float2 sq = mixed::lapsum<1>(ub, &uq);
-    const float2 delta = mixed::psub(mixed::pmul(mixed::P2(A.c.h2), dbc), mixed::padd(sq, st));
-    const float2 ge = mixed::padd(ub.e, delta);
-    A.a.gh[gi] = make_float4(ub.h.x, ub.h.y, ge.x, ge.y);
+    const HE tn[4] = {Y.at(pb + t1), Y.at(pb - t1), Y.at(pb + t2), Y.at(pb - t2)};
+    A.a.gh[gi] = ghost_value<BC>(A.c, ub, A.a.V[pb], uq, A.a.V[pq], nq, tn);
   }
 }
 
@@ -723,8 +807,10 @@ cudaError_t launch(const Geom& g, const Args& A, cudaStream_t st) {
   const unsigned nb = face_blocks(faces.total);
   if (METHOD == 2) {
     if (!A.a.gh || (BC == 2 && !A.a.fq)) return cudaErrorInvalidValue;
-    cudaError_t e = launch_k(ghost3d<BC>, dim3(nb), dim3(256), 0, st, g_pdl != 0, g, A, faces,
-                             GhostLayout(g));
+    const XPatches xp(g);
+    const unsigned ng = xp.nblk + face_blocks(faces.nz + faces.ny);
+    cudaError_t e = launch_k(ghost3d<BC>, dim3(ng), dim3(256), 0, st, g_pdl != 0, g, A, faces,
+                             GhostLayout(g), xp);
     if (e != cudaSuccess) return e;
   }
   {
