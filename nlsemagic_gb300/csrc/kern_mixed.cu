@@ -12,6 +12,7 @@ int g_pdl = 1;  // 3D 2SHOC stage kernels launched with PDL
 // room for the next interior kernel's tiles under PDL: 22.1 Gpt-steps/s at
 // 320^3 against 21.7 with 16 (and 20.3 with 1, 22.0 with 4).
 int g_face_bps = 8;
+int g_tile_order = 1;
 }
 
 template <int DIM, int METHOD, int BC>

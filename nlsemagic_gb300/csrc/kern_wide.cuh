@@ -133,7 +133,51 @@ struct TileOrder {
   int nbx, nby, nbz;
   int ix0, nxI, iy0, nyI, iz0, nzI;
   unsigned nI, nZ, nY;  // interior tiles, z-slab tiles, y-row tiles
+  int chunk_major;      // 1: chunk by chunk (see tile_cm)
+  // whether tile b stages a face point or a ghost (and so waits)
+  __host__ __device__ bool waits(unsigned b) const {
+    if (!chunk_major) return b >= nI;
+    const unsigned T = (unsigned)nbx * (unsigned)nby;
+    return b >= (unsigned)nzI * T || b % T >= (unsigned)nxI * (unsigned)nyI;
+  }
+  // Chunk-major order: the interior z chunks one after another, each with
+  // its interior tiles first and then its tiles at an x / y face; then the
+  // chunks at a z face.  Neighbouring tiles run close in time, so the halo
+  // they share is read from DRAM once (and served from L2 the second time).
+  __host__ __device__ void tile_cm(unsigned b, int& bx, int& by, int& bz) const {
+    const unsigned T = (unsigned)nbx * (unsigned)nby, k = b / T, r = b - k * T;
+    if (k >= (unsigned)nzI) {  // a chunk at a z face: plain (bx, by) order
+      const int kk = (int)(k - (unsigned)nzI);
+      bz = kk < iz0 ? kk : kk + nzI;
+      by = (int)(r / (unsigned)nbx);
+      bx = (int)(r - (unsigned)by * (unsigned)nbx);
+      return;
+    }
+    bz = iz0 + (int)k;
+    const unsigned nIxy = (unsigned)nxI * (unsigned)nyI;
+    if (r < nIxy) {
+      by = iy0 + (int)(r / (unsigned)nxI);
+      bx = ix0 + (int)(r % (unsigned)nxI);
+      return;
+    }
+    unsigned e = r - nIxy;
+    const unsigned nrows = (unsigned)(nby - nyI) * (unsigned)nbx;
+    if (e < nrows) {
+      const int row = (int)(e / (unsigned)nbx);
+      by = row < iy0 ? row : row + nyI;
+      bx = (int)(e - (unsigned)row * (unsigned)nbx);
+      return;
+    }
+    e -= nrows;
+    const unsigned nx = (unsigned)(nbx - nxI), row = e / nx, ex = e - row * nx;
+    by = iy0 + (int)row;
+    bx = (int)ex < ix0 ? (int)ex : (int)ex + nxI;
+  }
   __host__ __device__ void tile(unsigned b, int& bx, int& by, int& bz) const {
+    if (chunk_major) {
+      tile_cm(b, bx, by, bz);
+      return;
+    }
     if (b < nI) {
       const unsigned r = b / (unsigned)nxI;
       bx = ix0 + (int)(b - r * (unsigned)nxI);
@@ -191,7 +235,7 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
   const int x0 = bx * TX, y0 = by * TY, z0 = bz * zc;
   // tiles that stage a face point or a ghost wait for the kernels that made
   // them (PDL); interior tiles read only data complete before this launch
-  if (blockIdx.x >= to.nI) pdl_wait();
+  if (to.waits(blockIdx.x)) pdl_wait();
   if (x0 >= M || y0 >= N || z0 >= L) return;
   const int z1 = z0 + zc < L ? z0 + zc : L;  // owned planes [z0, z1)
   const int zs = z0 > 1 ? z0 : 1;            // interior planes of this chunk: [zs, ze)
@@ -708,6 +752,7 @@ inline int default_zc(const Geom& g, int H, int occ) {
 }
 
 extern int g_pdl;  // 2SHOC: launch the stage kernels with PDL (1) or plainly (0)
+extern int g_tile_order;  // interior kernel tile order: 1 chunk-major, 0 interior-first
 
 // cudaLaunchKernelEx, with programmatic stream serialization when pdl is set
 template <typename... KA, typename... AA>
@@ -754,6 +799,7 @@ inline TileOrder tile_order(const Geom& g, int TX, int TY, int H, int zc) {
     t.iz0 = t.nbz;
   }
   t.nI = (unsigned)t.nxI * (unsigned)t.nyI * (unsigned)t.nzI;
+  t.chunk_major = g_tile_order;
   t.nZ = (unsigned)(t.nbz - t.nzI) * (unsigned)t.nbx * (unsigned)t.nby;
   t.nY = (unsigned)t.nzI * (unsigned)(t.nby - t.nyI) * (unsigned)t.nbx;
   return t;

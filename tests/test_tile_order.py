@@ -14,12 +14,14 @@ SRC = r'''
 #include "kern_wide.cuh"
 #include <cstdio>
 #include <vector>
+namespace nlse { namespace wide { int g_tile_order = 1; int g_pdl = 1; int g_face_bps = 8; int g_zc_override = 0; } }
 using namespace nlse;
 using namespace nlse::wide;
-int check(int M, int N, int L, int zc) {
+int check(int M, int N, int L, int zc, int cm) {
   Geom g; g.ndim = 3; g.M = M; g.N = N; g.L = L; g.n = (long long)M * N * L;
   const int TX = 32, TY = NLSE_WIDE_TY, H = 2;
   TileOrder t = tile_order(g, TX, TY, H, zc);
+  t.chunk_major = cm;
   const long long nb = (long long)t.nbx * t.nby * t.nbz;
   std::vector<int> seen(nb, 0);
   for (long long b = 0; b < nb; ++b) {
@@ -30,9 +32,9 @@ int check(int M, int N, int L, int zc) {
     const int x0 = bx * TX, y0 = by * TY, z0 = bz * zc, z1 = z0 + zc < L ? z0 + zc : L;
     const bool inside = x0 - 2 >= 1 && x0 + TX + 1 <= M - 2 && y0 - H >= 1 &&
                         y0 + TY + H - 1 <= N - 2 && z0 - H >= 1 && z1 - 1 + H <= L - 2;
-    if (b < (long long)t.nI && !inside) return 2;   // a non-waiting tile touches a face
-    if (b >= (long long)t.nI && inside) return 3;   // an interior tile waits (allowed, but
-                                                    // the order should not do it)
+    if (!t.waits((unsigned)b) && !inside) return 2;  // a non-waiting tile touches a face
+    if (t.waits((unsigned)b) && inside) return 3;    // an interior tile waits (allowed, but
+                                                     // the order should not do it)
   }
   for (long long i = 0; i < nb; ++i)
     if (seen[i] != 1) return 4;
@@ -45,9 +47,11 @@ int main() {
   for (int M : dims) for (int N : dims) for (int L : {3, 4, 5, 8, 9, 20, 37, 64, 320})
     for (int zc : zcs) {
       if (zc > L) continue;
-      int r = check(M, N, L, zc);
-      if (r) { printf("FAIL %d %d %d %d code %d\n", M, N, L, zc, r); return 1; }
-      ++n;
+      for (int cm = 0; cm < 2; ++cm) {
+        int r = check(M, N, L, zc, cm);
+        if (r) { printf("FAIL %d %d %d %d order %d code %d\n", M, N, L, zc, cm, r); return 1; }
+        ++n;
+      }
     }
   printf("OK %lld\n", n);
   return 0;
