@@ -451,6 +451,250 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
     stream(std::integral_constant<bool, false>());
 }
 
+// ---- two planes per iteration (2SHOC, TMA staging) ---------------------------
+// The same computation as wide3d<2, STAGE, true>, but each thread advances two
+// consecutive planes (zA, zB = zA + 1) per iteration.  The per-plane costs --
+// the CTA barrier, the plane wait, loop and index work -- are paid once for
+// two points.  The register queue holds the thread's column for planes
+// zA-2 .. zA+3 (six live entries, as for one plane).  Ring of NU = 8 slots:
+// iteration j waits for planes zA+2, zA+3 and refills the slots of planes
+// zA-4, zA-3 -- last read at iteration j-2, so the barrier of iteration j-1
+// orders the refill after every read -- with planes zA+4, zA+5.
+struct WShape2 {
+  static constexpr int TX = 32, TY = NLSE_WIDE_TY, NT = TX * TY, H = 2, XO = 2;
+  static constexpr int PX = TX + 4, PY = TY + 2 * H, NU = 8;
+  static constexpr int PLANE = round_up(PX * PY * 8, 128);
+  static constexpr int SLOT = 2 * PLANE;
+  static constexpr int B_OFF = NU * SLOT;
+  static constexpr int SMEM = B_OFF + NU * 8;
+  static constexpr unsigned TX_BYTES = (unsigned)(2 * PX * PY * 8);
+};
+
+template <int STAGE>
+__global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3d_z2(
+    Geom g, Args A, int zc, TileOrder to, GhostLayout gl, const __grid_constant__ CUtensorMap tm0,
+    const __grid_constant__ CUtensorMap tm1) {
+  typedef WShape2 SH;
+  typedef mixed::HE HE;
+  constexpr int TX = SH::TX, TY = SH::TY, H = SH::H, XO = SH::XO, PX = SH::PX, NU = SH::NU;
+
+  extern __shared__ __align__(128) unsigned char smem[];
+  unsigned long long* bars = reinterpret_cast<unsigned long long*>(smem + SH::B_OFF);
+
+  const int M = g.M, N = g.N, L = g.L;
+  int bx, by, bz;
+  to.tile(blockIdx.x, bx, by, bz);
+  const int x0 = bx * TX, y0 = by * TY, z0 = bz * zc;
+  // tiles that stage a face point or a ghost wait for the kernels that made
+  // them (PDL); interior tiles read only data complete before this launch
+  if (to.waits(blockIdx.x)) pdl_wait();
+  if (x0 >= M || y0 >= N || z0 >= L) return;
+  const int z1 = z0 + zc < L ? z0 + zc : L;  // owned planes [z0, z1)
+  const int zs = z0 > 1 ? z0 : 1;            // interior planes of this chunk: [zs, ze)
+  const int ze = z1 < L - 1 ? z1 : L - 1;
+  if (zs >= ze) return;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+  const int x = x0 + tx, y = y0 + ty;
+  const bool inner = x >= 1 && x <= M - 2 && y >= 1 && y <= N - 2;
+  const bool edge = x0 == 0 || x0 + TX > M - 2 || y0 == 0 || y0 + TY > N - 2;
+  const float2* Ein = STAGE == 1 ? A.a.lo_in : A.a.e_in;
+  const float4* GH = A.a.gh;
+
+  if ((su32(smem) & 127u) != 0) {  // TMA destinations must be 128-byte aligned
+    if (tid == 0) atomicExch(A.err, NLSE_ERR_STATE);
+    return;
+  }
+  if (tid == 0) {
+    for (int s = 0; s < NU; ++s) mbar_init(&bars[s], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  // plane zz lives in slot (zz - pfirst) % NU; its k-th use of that slot
+  // completes mbarrier phase k, k = (zz - pfirst) / NU
+  const int pfirst = zs - H, plast = ze - 1 + H;
+  auto hplane = [&](int s) -> float2* { return reinterpret_cast<float2*>(smem + s * SH::SLOT); };
+  auto eplane = [&](int s) -> float2* {
+    return reinterpret_cast<float2*>(smem + s * SH::SLOT + SH::PLANE);
+  };
+  auto issue = [&](int zz, int s) {  // thread 0
+    fence_proxy_async();  // earlier generic accesses of the slot before the async write
+    mbar_expect_tx(&bars[s], SH::TX_BYTES);
+    tma_load_3d(hplane(s), &tm0, x0 - XO, y0 - H, zz, &bars[s]);
+    tma_load_3d(eplane(s), &tm1, x0 - XO, y0 - H, zz, &bars[s]);
+  };
+  // bounded wait for every plane issued up to `upto` (error path only)
+  auto drain = [&](int upto) {
+    if (tid != 0) return;
+    if (upto > plast) upto = plast;
+    int from = upto - NU + 1 > pfirst ? upto - NU + 1 : pfirst;
+    for (int zz = from; zz <= upto; ++zz)
+      mbar_wait(&bars[(zz - pfirst) % NU], (unsigned)(((zz - pfirst) / NU) & 1));
+  };
+
+  const int own = (ty + H) * PX + tx + XO;
+  // this thread's column value of plane zz (slot s); outside a z face the
+  // ghost value of the face point below / above
+  auto qload = [&](int zz, int s) -> HE {
+    HE r;
+    if (zz < 0 || zz >= L) {
+      r.h = r.e = make_float2(0.f, 0.f);
+      if (inner) r = he_of(GH[(zz < 0 ? gl.zlo : gl.zhi) + x + (long long)M * y]);
+      return r;
+    }
+    r.h = hplane(s)[own];
+    r.e = eplane(s)[own];
+    return r;
+  };
+  HE q[NU];  // q[s]: this thread's column value of the plane in slot s
+
+  // ---- prologue: stage planes pfirst .. pfirst+NU-1, queue pfirst .. pfirst+2H-1
+  if (tid == 0) {
+#pragma unroll
+    for (int t = 0; t < NU; ++t)
+      if (pfirst + t <= plast) issue(pfirst + t, t);
+  }
+  {
+    bool ok = true;
+    if (tid == 0) {
+#pragma unroll
+      for (int t = 0; t < 2 * H; ++t) ok &= mbar_wait(&bars[t], 0u);
+      if (!ok) atomicExch(A.err, NLSE_ERR_TIMEOUT);
+    }
+    if (__syncthreads_or(!ok)) {
+      drain(pfirst + NU - 1);
+      return;
+    }
+#pragma unroll
+    for (int t = 0; t < 2 * H; ++t) {
+      (void)tiled::mbar_try_wait(&bars[t], 0u);
+      q[t] = qload(pfirst + t, t);
+    }
+    __syncthreads();
+  }
+
+  // point offsets fit 32 bits (grids have fewer than 2^31 points)
+  const unsigned MN = (unsigned)M * (unsigned)N;
+  const unsigned pxy = (unsigned)y * (unsigned)M + (unsigned)x;
+
+  // one point of plane z (slot sc): F in the wide form from its in-plane
+  // neighbours (shared memory) and its column (z+-1: zp1/zm1, z+-2: zp2/zm2)
+  auto point = [&](int z, unsigned p, int sc, const HE& u0, const HE& zp1, const HE& zm1,
+                   const HE& zp2, const HE& zm2, float v, float2 lo, float2 kv, bool edge_pt) {
+    const float2* hp = hplane(sc);
+    const float2* ep = eplane(sc);
+    HE fn[6] = {zp1, zm1, {hp[own + PX], ep[own + PX]}, {hp[own - PX], ep[own - PX]},
+                {hp[own + 1], ep[own + 1]}, {hp[own - 1], ep[own - 1]}};
+    HE f2n[6] = {zp2, zm2, {hp[own + 2 * PX], ep[own + 2 * PX]},
+                 {hp[own - 2 * PX], ep[own - 2 * PX]}, {hp[own + 2], ep[own + 2]},
+                 {hp[own - 2], ep[own - 2]}};
+    const float2 T = mixed::f_wide_2shoc<3>(A.c, u0, v, fn, f2n);
+    // F next to a face, for the MSD formula of the face points
+    if (A.a.fq) {
+      const bool nz = z == 1 || z == L - 2;
+      if (nz || edge_pt) A.a.fq[p] = T;
+    }
+    if (STAGE == 1) lo = u0.e;
+    float2 eo, ko, ho, lo2;
+    mixed::stage_update(A.c, STAGE, T, u0.h, lo, u0.e, kv, eo, ko, ho, lo2);
+    if (STAGE == 2) A.a.K[p] = ko;
+    if (STAGE < 4) {
+      A.a.e_out[p] = eo;
+    } else {
+      A.a.hi_out[p] = ho;
+      A.a.lo_out[p] = lo2;
+    }
+  };
+
+  auto stream = [&](auto edge_tag) {
+    constexpr bool EDGE = decltype(edge_tag)::value;
+    const bool edge_pt = EDGE && (x == 1 || x == M - 2 || y == 1 || y == N - 2);
+    for (int zb = zs; zb < ze; zb += NU) {
+      const unsigned blk = (unsigned)((zb - zs) / NU) & 1u;
+#pragma unroll
+      for (int u = 0; u < NU / 2; ++u) {
+        const int zA = zb + 2 * u;
+        if (zA >= ze) break;
+        const bool hasB = zA + 1 < ze;
+        // slot of plane zA + c (zb - zs is a multiple of NU): (2u + H + c) mod NU
+#define NLSE_Z2_SLOT(c) ((2 * u + H + (c) + 2 * NU) % NU)
+        const int s0 = NLSE_Z2_SLOT(0), s1 = NLSE_Z2_SLOT(1), s2 = NLSE_Z2_SLOT(2),
+                  s3 = NLSE_Z2_SLOT(3), s4 = NLSE_Z2_SLOT(4), s5 = NLSE_Z2_SLOT(5),
+                  sm1 = NLSE_Z2_SLOT(-1), sm2 = NLSE_Z2_SLOT(-2);
+#undef NLSE_Z2_SLOT
+        // refill the slots of planes zA-4, zA-3 with zA+4, zA+5
+        if (tid == 0) {
+          if (zA + 4 >= pfirst + NU && zA + 4 <= plast) issue(zA + 4, s4);
+          if (zA + 5 >= pfirst + NU && zA + 5 <= plast) issue(zA + 5, s5);
+        }
+        // pointwise operands of both points, fetched before the wait
+        const unsigned pA = (unsigned)zA * MN + pxy, pB = pA + MN;
+        float vA = 0.f, vB = 0.f;
+        float2 loA = make_float2(0.f, 0.f), loB = loA, kA = loA, kB = loA;
+        if (inner) {
+          vA = A.a.V[pA];
+          if (STAGE >= 2) loA = __ldcg(A.a.lo_in + pA);
+          if (STAGE == 4) kA = __ldcg(A.a.K + pA);
+          if (hasB) {
+            vB = A.a.V[pB];
+            if (STAGE >= 2) loB = __ldcg(A.a.lo_in + pB);
+            if (STAGE == 4) kB = __ldcg(A.a.K + pB);
+          }
+          // next to an x / y face: the ghost across that face into this
+          // thread's own halo cells of planes zA and zB (landed at the last
+          // wait; only this thread reads those cells)
+          if (edge_pt) {
+            auto patch = [&](int zz, int s) {
+              float2* hpc = hplane(s);
+              float2* epc = eplane(s);
+              auto put = [&](int i, float4 gv) {
+                hpc[i] = make_float2(gv.x, gv.y);
+                epc[i] = make_float2(gv.z, gv.w);
+              };
+              if (x == M - 2) put(own + 2, GH[gl.xhi + y + (long long)N * zz]);
+              if (x == 1) put(own - 2, GH[gl.xlo + y + (long long)N * zz]);
+              if (y == N - 2) put(own + 2 * PX, GH[gl.yhi + x + (long long)M * zz]);
+              if (y == 1) put(own - 2 * PX, GH[gl.ylo + x + (long long)M * zz]);
+            };
+            patch(zA, s0);
+            if (hasB) patch(zA + 1, s1);
+            fence_proxy_async();  // before the slots' next TMA refill
+          }
+        }
+        // one thread waits for planes zA+2, zA+3 (bounded); the barrier
+        // releases the rest, and each thread takes the completed phases
+        const unsigned par2 = blk ^ (unsigned)(((2 * u + H + 2) / NU) & 1);
+        const unsigned par3 = blk ^ (unsigned)(((2 * u + H + 3) / NU) & 1);
+        const bool has3 = zA + 3 <= plast;
+        bool ok = true;
+        if (tid == 0) {
+          ok = mbar_wait(&bars[s2], par2);
+          if (has3) ok &= mbar_wait(&bars[s3], par3);
+          if (!ok) atomicExch(A.err, NLSE_ERR_TIMEOUT);
+        }
+        if (__syncthreads_or(!ok)) {
+          drain(zA + 5);
+          return;
+        }
+        (void)tiled::mbar_try_wait(&bars[s2], par2);
+        q[s2] = qload(zA + 2, s2);
+        if (has3) {
+          (void)tiled::mbar_try_wait(&bars[s3], par3);
+          q[s3] = qload(zA + 3, s3);
+        }
+        if (inner) {
+          point(zA, pA, s0, q[s0], q[s1], q[sm1], q[s2], q[sm2], vA, loA, kA, edge_pt);
+          if (hasB) point(zA + 1, pB, s1, q[s1], q[s2], q[s0], q[s3], q[sm1], vB, loB, kB, edge_pt);
+        }
+      }
+    }
+  };
+  if (edge)
+    stream(std::integral_constant<bool, true>());
+  else
+    stream(std::integral_constant<bool, false>());
+}
+
 // ---- shell enumeration ------------------------------------------------------
 // The points within W cells of a face of an M x N x L grid, enumerated as
 //   z < W or z >= L-W: whole planes;
@@ -805,6 +1049,28 @@ inline TileOrder tile_order(const Geom& g, int TX, int TY, int H, int zc) {
   return t;
 }
 
+extern int g_z2;  // 2SHOC with TMA staging: two planes per iteration (1) or one (0)
+
+template <int STAGE>
+cudaError_t launch_inner_z2(const Geom& g, const Args& A, cudaStream_t st, const CUtensorMap& m0,
+                            const CUtensorMap& m1) {
+  typedef WShape2 SH;
+  auto kern = wide3d_z2<STAGE>;
+  static int occ = 0;
+  if (!occ) {
+    cudaError_t e =
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SH::SMEM);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, SH::NT, SH::SMEM);
+    if (e != cudaSuccess || occ < 1) occ = 1;
+  }
+  const int zc = g_zc_override > 0 ? g_zc_override : default_zc(g, SH::H, occ);
+  const TileOrder to = tile_order(g, SH::TX, SH::TY, SH::H, zc);
+  const unsigned nb = (unsigned)to.nbx * (unsigned)to.nby * (unsigned)to.nbz;
+  return launch_k(kern, dim3(nb), dim3(SH::TX, SH::TY), SH::SMEM, st, g_pdl != 0, g, A, zc, to,
+                  GhostLayout(g), m0, m1);
+}
+
 template <int METHOD, int STAGE, bool TMA>
 cudaError_t launch_inner(const Geom& g, const Args& A, cudaStream_t st, const CUtensorMap& m0,
                          const CUtensorMap& m1) {
@@ -828,6 +1094,14 @@ cudaError_t launch_inner(const Geom& g, const Args& A, cudaStream_t st, const CU
 template <int METHOD, bool TMA>
 cudaError_t launch_inner_stage(const Geom& g, const Args& A, cudaStream_t st,
                                const CUtensorMap& m0, const CUtensorMap& m1) {
+  if (METHOD == 2 && TMA && g_z2) {
+    switch (A.stage) {
+      case 1: return launch_inner_z2<1>(g, A, st, m0, m1);
+      case 2: return launch_inner_z2<2>(g, A, st, m0, m1);
+      case 3: return launch_inner_z2<3>(g, A, st, m0, m1);
+      case 4: return launch_inner_z2<4>(g, A, st, m0, m1);
+    }
+  }
   switch (A.stage) {
     case 1: return launch_inner<METHOD, 1, TMA>(g, A, st, m0, m1);
     case 2: return launch_inner<METHOD, 2, TMA>(g, A, st, m0, m1);

@@ -58,6 +58,7 @@ extern int g_zc_override;
 extern int g_pdl;
 extern int g_face_bps;
 extern int g_tile_order;
+extern int g_z2;
 }
 }  // namespace nlse
 static int g_default_graph_steps = 8;
@@ -67,6 +68,11 @@ extern "C" int nlse_tune_set(const char* key, long long value) {
   if (!strcmp(key, "wide.zc")) {
     if (value < 0 || value > (1 << 20)) return fail(NLSE_ERR_ARG, "wide.zc out of range");
     nlse::wide::g_zc_override = (int)value;
+    return NLSE_OK;
+  }
+  if (!strcmp(key, "wide.z2")) {
+    if (value != 0 && value != 1) return fail(NLSE_ERR_ARG, "wide.z2 must be 0 or 1");
+    nlse::wide::g_z2 = (int)value;
     return NLSE_OK;
   }
   if (!strcmp(key, "wide.tile_order")) {
@@ -96,6 +102,10 @@ extern "C" int nlse_tune_get(const char* key, long long* value) {
   if (!key || !value) return fail(NLSE_ERR_ARG, "NULL argument");
   if (!strcmp(key, "wide.zc")) {
     *value = nlse::wide::g_zc_override;
+    return NLSE_OK;
+  }
+  if (!strcmp(key, "wide.z2")) {
+    *value = nlse::wide::g_z2;
     return NLSE_OK;
   }
   if (!strcmp(key, "wide.tile_order")) {
