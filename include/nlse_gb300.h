@@ -260,6 +260,9 @@ int nlse_take_steps_noalloc(const nlse_problem *p, const double *dUr, const doub
  *                  finish; 0: plain stream order.  Same bits either way.
  *   "face.blocks_per_sm"  blocks of 256 threads per SM of the 3D face
  *                  kernels (1-64, default 8; grid-stride beyond).
+ *   "wide.z2"      1 (default): the mixed-precision 3D 2SHOC interior kernel
+ *                  advances two z planes per iteration (one barrier and
+ *                  plane wait per two points); 0: one plane.  Same bits.
  *   "wide.tile_order"  order of the mixed-precision 3D interior kernel's
  *                  tiles: 1 (default) chunk by chunk (neighbouring tiles
  *                  share their halo through L2), 0 every face tile last.

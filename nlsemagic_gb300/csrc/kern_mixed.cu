@@ -13,7 +13,9 @@ int g_pdl = 1;  // 3D 2SHOC stage kernels launched with PDL
 // 320^3 against 21.7 with 16 (and 20.3 with 1, 22.0 with 4).
 int g_face_bps = 8;
 int g_tile_order = 1;
-int g_z2 = 0;  // 3D 2SHOC interior kernel: two planes per iteration
+// 3D 2SHOC interior kernel (TMA staging): two planes per iteration.  Same
+// bits as one plane; 23.6 Gpt-steps/s at 320^3 against 21.9.
+int g_z2 = 1;
 }
 
 template <int DIM, int METHOD, int BC>
