@@ -36,6 +36,8 @@ UNITS = {
     "kern_vort.cu": ["-fmad=false"],
     "kern_init.cu": [],
     "kern_cq.cu": ["-fmad=false"],
+    "kern_small_exact.cu": ["-fmad=false"],
+    "kern_small_mixed.cu": [],
 }
 
 

@@ -62,6 +62,9 @@ extern int g_z2;
 }
 }  // namespace nlse
 static int g_default_graph_steps = 8;
+// 1D solves of at most this many points run each chunk in one single-block
+// launch (0: never)
+static long long g_small1d_max = 4096;
 
 extern "C" int nlse_tune_set(const char* key, long long value) {
   if (!key) return fail(NLSE_ERR_ARG, "key is NULL");
@@ -88,6 +91,11 @@ extern "C" int nlse_tune_set(const char* key, long long value) {
   if (!strcmp(key, "wide.pdl")) {
     if (value != 0 && value != 1) return fail(NLSE_ERR_ARG, "wide.pdl must be 0 or 1");
     nlse::wide::g_pdl = (int)value;
+    return NLSE_OK;
+  }
+  if (!strcmp(key, "small1d.max_points")) {
+    if (value < 0 || value > 65536) return fail(NLSE_ERR_ARG, "small1d.max_points out of range");
+    g_small1d_max = value;
     return NLSE_OK;
   }
   if (!strcmp(key, "graph.steps")) {
@@ -118,6 +126,10 @@ extern "C" int nlse_tune_get(const char* key, long long* value) {
   }
   if (!strcmp(key, "wide.pdl")) {
     *value = nlse::wide::g_pdl;
+    return NLSE_OK;
+  }
+  if (!strcmp(key, "small1d.max_points")) {
+    *value = g_small1d_max;
     return NLSE_OK;
   }
   if (!strcmp(key, "graph.steps")) {
@@ -569,10 +581,39 @@ static int ensure_graph(nlse_solver* s, int parity) {
   return NLSE_OK;
 }
 
+// Small 1D solves: the whole chunk in single-block launches (at most 2^16
+// steps per launch, so that no launch runs for long).
+static int run_small1d(nlse_solver* s, long long nsteps) {
+  const nlse_problem& p = s->prob;
+  while (nsteps > 0) {
+    const long long m = nsteps < 65536 ? nsteps : 65536;
+    cudaError_t e;
+    if (p.precision == NLSE_PREC_DOUBLE) {
+      typedef C2<double> T;
+      e = launch_small1d_exact<double>(s->g, p.method, p.bc, s->cd, (T*)s->psi, (T*)s->K,
+                                       (T*)s->ya, (T*)s->yb, (const double*)s->V, (T*)s->dsc, m,
+                                       s->stream);
+    } else if (p.precision == NLSE_PREC_SINGLE) {
+      typedef C2<float> T;
+      e = launch_small1d_exact<float>(s->g, p.method, p.bc, s->cf, (T*)s->psi, (T*)s->K,
+                                      (T*)s->ya, (T*)s->yb, (const float*)s->V, (T*)s->dsc, m,
+                                      s->stream);
+    } else {
+      e = launch_small1d_mixed(s->g, p.method, p.bc, s->cf, s->hi, s->lo, s->mK, s->da, s->db,
+                               s->dc, s->Vf, (float2*)s->dsc, s->cur, m, s->stream);
+      if (e == cudaSuccess && (m & 1)) s->cur = 1 - s->cur;
+    }
+    if (e != cudaSuccess) return fail(NLSE_ERR_CUDA, "small 1D launch failed: %s", cudaGetErrorString(e));
+    nsteps -= m;
+  }
+  return NLSE_OK;
+}
+
 extern "C" int nlse_solver_run(nlse_solver* s, long long nsteps) {
   if (!s) return fail(NLSE_ERR_ARG, "solver is NULL");
   if (nsteps < 0) return fail(NLSE_ERR_ARG, "nsteps must be >= 0");
   CUDA_TRY(cudaSetDevice(s->device));
+  if (s->g.ndim == 1 && s->g.n <= g_small1d_max && nsteps > 0) return run_small1d(s, nsteps);
   const int G = s->graph_steps;
   if (G > 0 && nsteps >= G) {
     long long reps = nsteps / G;

@@ -49,6 +49,17 @@ cudaError_t launch_mixed_stage(const Geom& g, int method, int BC, const Consts<f
 // Kernel launches one mixed stage issues (launch_mixed_stage), and the
 // scratch the tiled 3D 2SHOC path needs: ghost entries (float4) and F
 // entries (float2) for MixedStageArgs::gh / ::fq (0 when not needed).
+// Small 1D solves: every pass of nsteps RK4 steps in one single-block launch
+// (kern_small.cuh); same buffers and results as the stage launches.
+template <typename R>
+cudaError_t launch_small1d_exact(const Geom& g, int method, int BC, const Consts<R>& c, C2<R>* psi,
+                                 C2<R>* K, C2<R>* ya, C2<R>* yb, const R* V, C2<R>* D,
+                                 long long nsteps, cudaStream_t st);
+cudaError_t launch_small1d_mixed(const Geom& g, int method, int BC, const Consts<float>& c,
+                                 float2* const hi[2], float2* const lo[2], float2* K, float2* da,
+                                 float2* db, float2* dc, const float* V, float2* D, int cur,
+                                 long long nsteps, cudaStream_t st);
+
 int mixed_stage_launches(const Geom& g, int method, int BC, int kernel_kind);
 long long mixed_ghost_entries(const Geom& g, int method, int BC, int kernel_kind);
 long long mixed_fq_entries(const Geom& g, int method, int BC, int kernel_kind);
