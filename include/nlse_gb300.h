@@ -260,6 +260,10 @@ int nlse_take_steps_noalloc(const nlse_problem *p, const double *dUr, const doub
  *                  finish; 0: plain stream order.  Same bits either way.
  *   "face.blocks_per_sm"  blocks of 256 threads per SM of the 3D face
  *                  kernels (1-64, default 8; grid-stride beyond).
+ *   "small1d.max_points"  FP32 and mixed 1D solves of at most this many
+ *                  points (default 2048, 0 = never, at most 65536) run each
+ *                  chunk in single-block launches instead of a launch per
+ *                  pass.  Same bits.
  *   "wide.z2"      1 (default): the mixed-precision 3D 2SHOC interior kernel
  *                  advances two z planes per iteration (one barrier and
  *                  plane wait per two points); 0: one plane.  Same bits.

@@ -62,9 +62,11 @@ extern int g_z2;
 }
 }  // namespace nlse
 static int g_default_graph_steps = 8;
-// 1D solves of at most this many points run each chunk in one single-block
-// launch (0: never)
-static long long g_small1d_max = 4096;
+// FP32 and mixed 1D solves of at most this many points run each chunk in
+// single-block launches (0: never).  At the 1024-point configuration this
+// runs 2.0-2.6x faster than a launch per pass; FP64 does not gain (one SM's
+// FP64 rate is the limit there) and keeps the stage launches.
+static long long g_small1d_max = 2048;
 
 extern "C" int nlse_tune_set(const char* key, long long value) {
   if (!key) return fail(NLSE_ERR_ARG, "key is NULL");
@@ -613,7 +615,9 @@ extern "C" int nlse_solver_run(nlse_solver* s, long long nsteps) {
   if (!s) return fail(NLSE_ERR_ARG, "solver is NULL");
   if (nsteps < 0) return fail(NLSE_ERR_ARG, "nsteps must be >= 0");
   CUDA_TRY(cudaSetDevice(s->device));
-  if (s->g.ndim == 1 && s->g.n <= g_small1d_max && nsteps > 0) return run_small1d(s, nsteps);
+  if (s->g.ndim == 1 && s->g.n <= g_small1d_max && s->prob.precision != NLSE_PREC_DOUBLE &&
+      nsteps > 0)
+    return run_small1d(s, nsteps);
   const int G = s->graph_steps;
   if (G > 0 && nsteps >= G) {
     long long reps = nsteps / G;

@@ -1,9 +1,9 @@
-"""Small 1D solves run each chunk in one single-block launch (every pass of
-every RK4 step separated by block barriers).  The per-point arithmetic and
-the buffers are those of the launch-per-pass path, so the results must be
-the same bits: every precision class, both methods, every boundary code
-(BC 4 included), odd and even step counts (the mixed state pair flips per
-step), and the size limit."""
+"""Small FP32 and mixed 1D solves run each chunk in one single-block launch
+(every pass of every RK4 step separated by block barriers).  The per-point
+arithmetic and the buffers are those of the launch-per-pass path, so the
+results must be the same bits: both precision classes, both methods, every
+boundary code (BC 4 included), odd and even step counts (the mixed state
+pair flips per step), and sizes up to the limit."""
 import numpy as np
 import pytest
 
@@ -29,7 +29,7 @@ def _run(n, method, prec, BC, steps, small_max):
         autotune.set_knob("small1d.max_points", old)
 
 
-@pytest.mark.parametrize("prec", [1, 2, 3])
+@pytest.mark.parametrize("prec", [1, 3])
 @pytest.mark.parametrize("method", [1, 2])
 @pytest.mark.parametrize("BC", [1, 2, 3, 4])
 @pytest.mark.parametrize("n,steps", [(64, 7), (1024, 20), (4096, 9)])
