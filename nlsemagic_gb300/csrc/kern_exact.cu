@@ -16,16 +16,16 @@ static cudaError_t launch_one(const Geom& g, const Consts<R>& c, const ExactStag
   long long blocks = (g.n + 255) / 256;
   if (blocks > 152LL * 32) blocks = 152LL * 32;
   if (METHOD == 2 && a.dsc) {
-    exact::d_stage<R, DIM, BC><<<(unsigned)blocks, 256, 0, st>>>(g, c, a.Yin, a.V, a.dsc);
-    cudaError_t e = cudaGetLastError();
+    const bool pdl = wide::g_pdl != 0;
+    cudaError_t e = launch_k(exact::d_stage<R, DIM, BC>, dim3((unsigned)blocks), dim3(256), 0, st,
+                             pdl, g, c, (const C2<R>*)a.Yin, a.V, a.dsc);
     if (e != cudaSuccess) return e;
-    exact::gather_stage_d<R, DIM, BC><<<(unsigned)blocks, 256, 0, st>>>(
-        g, c, a.Yin, a.Psi, a.V, a.K, a.Yout, a.dsc, stage);
-    return cudaGetLastError();
+    return launch_k(exact::gather_stage_d<R, DIM, BC>, dim3((unsigned)blocks), dim3(256), 0, st,
+                    pdl, g, c, (const C2<R>*)a.Yin, a.Psi, a.V, a.K, a.Yout,
+                    (const C2<R>*)a.dsc, stage);
   }
-  exact::gather_stage<R, DIM, METHOD, BC><<<(unsigned)blocks, 256, 0, st>>>(
-      g, c, a.Yin, a.Psi, a.V, a.K, a.Yout, stage);
-  return cudaGetLastError();
+  return launch_k(exact::gather_stage<R, DIM, METHOD, BC>, dim3((unsigned)blocks), dim3(256), 0,
+                  st, wide::g_pdl != 0, g, c, (const C2<R>*)a.Yin, a.Psi, a.V, a.K, a.Yout, stage);
 }
 
 long long exact_dsc_entries(const Geom& g, int method, int BC, int kernel_kind) {

@@ -10,6 +10,8 @@
 #include "nlse_exact.cuh"
 #include "nlse_mixed.cuh"
 
+#include "nlse_pdl.cuh"
+
 namespace nlse {
 
 __device__ __forceinline__ void decompose(const Geom& g, long long p, int& i, int& j, int& k) {
@@ -157,6 +159,8 @@ __global__ void __launch_bounds__(256) gather_stage(Geom g, Consts<R> c,
                                                     C2<R>* Psi, const R* __restrict__ V,
                                                     C2<R>* __restrict__ K,
                                                     C2<R>* __restrict__ Yout, int stage) {
+  pdl_trigger();  // the next kernel may launch; it waits for this one
+  pdl_wait();     // the previous kernel's output
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < g.n;
        p += (long long)gridDim.x * blockDim.x) {
     int i, j, k;
@@ -171,6 +175,8 @@ __global__ void __launch_bounds__(256) gather_stage(Geom g, Consts<R> c,
 template <typename R, int DIM, int BC>
 __global__ void __launch_bounds__(256) d_stage(Geom g, Consts<R> c, const C2<R>* __restrict__ Yin,
                                                const R* __restrict__ V, C2<R>* __restrict__ D) {
+  pdl_trigger();  // the next kernel may launch; it waits for this one
+  pdl_wait();     // the previous kernel's output
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < g.n;
        p += (long long)gridDim.x * blockDim.x) {
     int i, j, k;
@@ -186,6 +192,8 @@ __global__ void __launch_bounds__(256) gather_stage_d(Geom g, Consts<R> c,
                                                       C2<R>* __restrict__ K,
                                                       C2<R>* __restrict__ Yout,
                                                       const C2<R>* __restrict__ D, int stage) {
+  pdl_trigger();  // the next kernel may launch; it waits for this one
+  pdl_wait();     // the previous kernel's output
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < g.n;
        p += (long long)gridDim.x * blockDim.x) {
     int i, j, k;
@@ -437,6 +445,8 @@ __global__ void __launch_bounds__(256) gather_stage(Geom g, Consts<float> c,
                                                     float2* __restrict__ d_out,
                                                     float2* __restrict__ hi_out,
                                                     float2* __restrict__ lo_out, int stage) {
+  pdl_trigger();  // the next kernel may launch; it waits for this one
+  pdl_wait();     // the previous kernel's output
   YIn Y{hi_in, stage == 1 ? lo_in : d_in};
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < g.n;
        p += (long long)gridDim.x * blockDim.x) {
@@ -454,6 +464,8 @@ __global__ void __launch_bounds__(256) d_stage(Geom g, Consts<float> c,
                                                const float2* __restrict__ e_in,
                                                const float* __restrict__ V,
                                                float2* __restrict__ D) {
+  pdl_trigger();  // the next kernel may launch; it waits for this one
+  pdl_wait();     // the previous kernel's output
   YIn Y{hi_in, e_in};
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < g.n;
        p += (long long)gridDim.x * blockDim.x) {
@@ -474,6 +486,8 @@ __global__ void __launch_bounds__(256) gather_stage_d(Geom g, Consts<float> c,
                                                       float2* __restrict__ hi_out,
                                                       float2* __restrict__ lo_out,
                                                       const float2* __restrict__ D, int stage) {
+  pdl_trigger();  // the next kernel may launch; it waits for this one
+  pdl_wait();     // the previous kernel's output
   YIn Y{hi_in, stage == 1 ? lo_in : d_in};
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < g.n;
        p += (long long)gridDim.x * blockDim.x) {

@@ -27,18 +27,19 @@ static cudaError_t launch_one(const Geom& g, const Consts<float>& c, const Mixed
   }
   long long blocks = (g.n + 255) / 256;
   if (blocks > 152LL * 32) blocks = 152LL * 32;
+  const bool pdl = wide::g_pdl != 0;
   if (METHOD == 2 && a.dsc) {
-    mixed::d_stage<DIM, BC><<<(unsigned)blocks, 256, 0, st>>>(
-        g, c, a.hi_in, stage == 1 ? a.lo_in : a.e_in, a.V, a.dsc);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = launch_k(mixed::d_stage<DIM, BC>, dim3((unsigned)blocks), dim3(256), 0, st,
+                             pdl, g, c, (const float2*)a.hi_in,
+                             (const float2*)(stage == 1 ? a.lo_in : a.e_in), a.V, a.dsc);
     if (e != cudaSuccess) return e;
-    mixed::gather_stage_d<DIM, BC><<<(unsigned)blocks, 256, 0, st>>>(
-        g, c, a.hi_in, a.lo_in, a.e_in, a.V, a.K, a.e_out, a.hi_out, a.lo_out, a.dsc, stage);
-    return cudaGetLastError();
+    return launch_k(mixed::gather_stage_d<DIM, BC>, dim3((unsigned)blocks), dim3(256), 0, st, pdl,
+                    g, c, (const float2*)a.hi_in, (const float2*)a.lo_in, (const float2*)a.e_in,
+                    a.V, a.K, a.e_out, a.hi_out, a.lo_out, (const float2*)a.dsc, stage);
   }
-  mixed::gather_stage<DIM, METHOD, BC><<<(unsigned)blocks, 256, 0, st>>>(
-      g, c, a.hi_in, a.lo_in, a.e_in, a.V, a.K, a.e_out, a.hi_out, a.lo_out, stage);
-  return cudaGetLastError();
+  return launch_k(mixed::gather_stage<DIM, METHOD, BC>, dim3((unsigned)blocks), dim3(256), 0, st,
+                  pdl, g, c, (const float2*)a.hi_in, (const float2*)a.lo_in,
+                  (const float2*)a.e_in, a.V, a.K, a.e_out, a.hi_out, a.lo_out, stage);
 }
 
 template <int DIM, int METHOD>

@@ -110,17 +110,6 @@ __device__ __forceinline__ mixed::HE he_of(float4 v) {
   return r;
 }
 
-// ---- programmatic dependent launch (PDL) --------------------------------------
-// A kernel launched with programmatic stream serialization may start once
-// every block of the preceding kernel has started and triggered (or exited).
-// griddepcontrol.wait blocks until that kernel has completed and its writes
-// are visible; launch_dependents is this block's trigger.  Without the launch
-// attribute both are no-ops.
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-__device__ __forceinline__ void pdl_trigger() {
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-}
-
 // Order of the interior kernel's tiles: first those whose staged region
 // (tile, 2-cell halo, chunk +-2 planes) holds no face point and no ghost, then
 // the others.  Only the others read what the kernels just before produce
@@ -995,25 +984,7 @@ inline int default_zc(const Geom& g, int H, int occ) {
   return zc;
 }
 
-extern int g_pdl;  // 2SHOC: launch the stage kernels with PDL (1) or plainly (0)
 extern int g_tile_order;  // interior kernel tile order: 1 chunk-major, 0 interior-first
-
-// cudaLaunchKernelEx, with programmatic stream serialization when pdl is set
-template <typename... KA, typename... AA>
-cudaError_t launch_k(void (*k)(KA...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
-                     bool pdl, AA&&... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = block;
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = st;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = pdl ? 1 : 0;
-  return cudaLaunchKernelEx(&cfg, k, std::forward<AA>(args)...);
-}
 
 // Interior ranges of the tile order: the staged region of tile bx is
 // [32 bx - 2, 32 bx + 34) in x (rows [TY by - H, TY by + TY + H), planes
