@@ -15,10 +15,10 @@
 // formula at b then yields D_bc(b), and the ghost enters the wide form and
 // the D's it replaces with opposite signs.  (Algebraic identity; checked in
 // FP64 against the compact form for BCs 1-3, edges and corners included.)
-// The ghosts are computed per stage by ghost3d into a small face array; a
-// point next to an x / y face writes its ghost into its own halo cell of the
-// staged plane, and the register queue entry of plane -1 / L holds the z
-// ghost.
+// The ghosts are computed per stage by ghost3d into a small face array (the
+// strided x faces in staged patches); a point next to an x / y face writes
+// its ghost into its own halo cell of the staged plane, and the register
+// queue entry of plane -1 / L holds the z ghost.
 //
 // One CTA owns a TX x TY column and streams through a chunk of z planes:
 //   - each plane (with a 2-cell x/y halo) is staged into a shared-memory ring
@@ -30,9 +30,16 @@
 //     entry per ring slot, so each plane value is read from shared memory
 //     once as a queue entry;
 //   - the z loop is unrolled by the ring length, so ring slots, mbarrier
-//     parities and register-queue entries are compile-time indices.
+//     parities and register-queue entries are compile-time indices;
+//   - for 2SHOC with TMA staging, wide3d_z2 advances two planes per
+//     iteration (one CTA barrier and plane wait per two points).
 // Every mbarrier wait is bounded (NLSE_ERR_TIMEOUT in the error word, copies
 // in flight drained, CTA returns).
+//
+// The tiles run chunk by chunk (TileOrder); with programmatic dependent
+// launch (nlse_pdl.cuh) the tiles whose staged region holds no face point
+// and no ghost start while the face kernels of the previous stage finish,
+// and only the others wait for them.
 //
 // Face points -- face2shoc (2SHOC: the boundary-condition F; for MSD from the
 // inward neighbour's F, which wide3d stores for the points next to a face)
