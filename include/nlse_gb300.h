@@ -264,9 +264,10 @@ int nlse_take_steps_noalloc(const nlse_problem *p, const double *dUr, const doub
  *                  points (default 2048, 0 = never, at most 65536) run each
  *                  chunk in single-block launches instead of a launch per
  *                  pass.  Same bits.
- *   "wide.z2"      1 (default): the mixed-precision 3D 2SHOC interior kernel
- *                  advances two z planes per iteration (one barrier and
- *                  plane wait per two points); 0: one plane.  Same bits.
+ *   "wide.z2"      1 (default): the mixed-precision 3D interior kernel (TMA
+ *                  staging, both methods) advances two z planes per
+ *                  iteration (one barrier and plane wait per two points);
+ *                  0: one plane.  Same bits.
  *   "wide.tile_order"  order of the mixed-precision 3D interior kernel's
  *                  tiles: 1 (default) chunk by chunk (neighbouring tiles
  *                  share their halo through L2), 0 every face tile last.

@@ -447,17 +447,19 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
     stream(std::integral_constant<bool, false>());
 }
 
-// ---- two planes per iteration (2SHOC, TMA staging) ---------------------------
-// The same computation as wide3d<2, STAGE, true>, but each thread advances two
-// consecutive planes (zA, zB = zA + 1) per iteration.  The per-plane costs --
-// the CTA barrier, the plane wait, loop and index work -- are paid once for
-// two points.  The register queue holds the thread's column for planes
-// zA-2 .. zA+3 (six live entries, as for one plane).  Ring of NU = 8 slots:
-// iteration j waits for planes zA+2, zA+3 and refills the slots of planes
-// zA-4, zA-3 -- last read at iteration j-2, so the barrier of iteration j-1
-// orders the refill after every read -- with planes zA+4, zA+5.
+// ---- two planes per iteration (TMA staging) ----------------------------------
+// The same computation as wide3d<METHOD, STAGE, true>, but each thread
+// advances two consecutive planes (zA, zB = zA + 1) per iteration.  The
+// per-plane costs -- the CTA barrier, the plane wait, loop and index work --
+// are paid once for two points.  The register queue holds the thread's
+// column for planes zA-H .. zA+1+H (six live entries for 2SHOC, four for CD).
+// Ring of NU = 8 slots: iteration j waits for planes zA+H, zA+H+1 and refills
+// the slots of planes zA-4, zA-3 -- last read at iteration j-2 (a plane is
+// last read at the iteration that advances it), so the barrier of iteration
+// j-1 orders the refill after every read -- with planes zA+4, zA+5.
+template <int METHOD>
 struct WShape2 {
-  static constexpr int TX = 32, TY = NLSE_WIDE_TY, NT = TX * TY, H = 2, XO = 2;
+  static constexpr int TX = 32, TY = NLSE_WIDE_TY, NT = TX * TY, H = METHOD == 2 ? 2 : 1, XO = 2;
   static constexpr int PX = TX + 4, PY = TY + 2 * H, NU = 8;
   static constexpr int PLANE = round_up(PX * PY * 8, 128);
   static constexpr int SLOT = 2 * PLANE;
@@ -466,11 +468,11 @@ struct WShape2 {
   static constexpr unsigned TX_BYTES = (unsigned)(2 * PX * PY * 8);
 };
 
-template <int STAGE>
+template <int METHOD, int STAGE>
 __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3d_z2(
     Geom g, Args A, int zc, TileOrder to, GhostLayout gl, const __grid_constant__ CUtensorMap tm0,
     const __grid_constant__ CUtensorMap tm1) {
-  typedef WShape2 SH;
+  typedef WShape2<METHOD> SH;
   typedef mixed::HE HE;
   constexpr int TX = SH::TX, TY = SH::TY, H = SH::H, XO = SH::XO, PX = SH::PX, NU = SH::NU;
 
@@ -492,7 +494,7 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
   const int x = x0 + tx, y = y0 + ty;
   const bool inner = x >= 1 && x <= M - 2 && y >= 1 && y <= N - 2;
-  const bool edge = x0 == 0 || x0 + TX > M - 2 || y0 == 0 || y0 + TY > N - 2;
+  const bool edge = METHOD == 2 && (x0 == 0 || x0 + TX > M - 2 || y0 == 0 || y0 + TY > N - 2);
   const float2* Ein = STAGE == 1 ? A.a.lo_in : A.a.e_in;
   const float4* GH = A.a.gh;
 
@@ -533,7 +535,7 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
   // ghost value of the face point below / above
   auto qload = [&](int zz, int s) -> HE {
     HE r;
-    if (zz < 0 || zz >= L) {
+    if (METHOD == 2 && (zz < 0 || zz >= L)) {
       r.h = r.e = make_float2(0.f, 0.f);
       if (inner) r = he_of(GH[(zz < 0 ? gl.zlo : gl.zhi) + x + (long long)M * y]);
       return r;
@@ -573,22 +575,27 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
   const unsigned MN = (unsigned)M * (unsigned)N;
   const unsigned pxy = (unsigned)y * (unsigned)M + (unsigned)x;
 
-  // one point of plane z (slot sc): F in the wide form from its in-plane
-  // neighbours (shared memory) and its column (z+-1: zp1/zm1, z+-2: zp2/zm2)
+  // one point of plane z (slot sc): F from its in-plane neighbours (shared
+  // memory) and its column (z+-1: zp1/zm1; 2SHOC, wide form: z+-2: zp2/zm2)
   auto point = [&](int z, unsigned p, int sc, const HE& u0, const HE& zp1, const HE& zm1,
                    const HE& zp2, const HE& zm2, float v, float2 lo, float2 kv, bool edge_pt) {
     const float2* hp = hplane(sc);
     const float2* ep = eplane(sc);
     HE fn[6] = {zp1, zm1, {hp[own + PX], ep[own + PX]}, {hp[own - PX], ep[own - PX]},
                 {hp[own + 1], ep[own + 1]}, {hp[own - 1], ep[own - 1]}};
-    HE f2n[6] = {zp2, zm2, {hp[own + 2 * PX], ep[own + 2 * PX]},
-                 {hp[own - 2 * PX], ep[own - 2 * PX]}, {hp[own + 2], ep[own + 2]},
-                 {hp[own - 2], ep[own - 2]}};
-    const float2 T = mixed::f_wide_2shoc<3>(A.c, u0, v, fn, f2n);
-    // F next to a face, for the MSD formula of the face points
-    if (A.a.fq) {
-      const bool nz = z == 1 || z == L - 2;
-      if (nz || edge_pt) A.a.fq[p] = T;
+    float2 T;
+    if (METHOD == 1) {
+      T = mixed::f_interior_cd<3>(A.c, u0, v, fn);
+    } else {
+      HE f2n[6] = {zp2, zm2, {hp[own + 2 * PX], ep[own + 2 * PX]},
+                   {hp[own - 2 * PX], ep[own - 2 * PX]}, {hp[own + 2], ep[own + 2]},
+                   {hp[own - 2], ep[own - 2]}};
+      T = mixed::f_wide_2shoc<3>(A.c, u0, v, fn, f2n);
+      // F next to a face, for the MSD formula of the face points
+      if (A.a.fq) {
+        const bool nz = z == 1 || z == L - 2;
+        if (nz || edge_pt) A.a.fq[p] = T;
+      }
     }
     if (STAGE == 1) lo = u0.e;
     float2 eo, ko, ho, lo2;
@@ -604,7 +611,7 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
 
   auto stream = [&](auto edge_tag) {
     constexpr bool EDGE = decltype(edge_tag)::value;
-    const bool edge_pt = EDGE && (x == 1 || x == M - 2 || y == 1 || y == N - 2);
+    const bool edge_pt = METHOD == 2 && EDGE && (x == 1 || x == M - 2 || y == 1 || y == N - 2);
     for (int zb = zs; zb < ze; zb += NU) {
       const unsigned blk = (unsigned)((zb - zs) / NU) & 1u;
 #pragma unroll
@@ -617,6 +624,8 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
         const int s0 = NLSE_Z2_SLOT(0), s1 = NLSE_Z2_SLOT(1), s2 = NLSE_Z2_SLOT(2),
                   s3 = NLSE_Z2_SLOT(3), s4 = NLSE_Z2_SLOT(4), s5 = NLSE_Z2_SLOT(5),
                   sm1 = NLSE_Z2_SLOT(-1), sm2 = NLSE_Z2_SLOT(-2);
+        // the planes this iteration queues: zA+H and zA+H+1
+        const int sqa = NLSE_Z2_SLOT(H), sqb = NLSE_Z2_SLOT(H + 1);
 #undef NLSE_Z2_SLOT
         // refill the slots of planes zA-4, zA-3 with zA+4, zA+5
         if (tid == 0) {
@@ -639,7 +648,7 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
           // next to an x / y face: the ghost across that face into this
           // thread's own halo cells of planes zA and zB (landed at the last
           // wait; only this thread reads those cells)
-          if (edge_pt) {
+          if (METHOD == 2 && edge_pt) {
             auto patch = [&](int zz, int s) {
               float2* hpc = hplane(s);
               float2* epc = eplane(s);
@@ -657,26 +666,26 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
             fence_proxy_async();  // before the slots' next TMA refill
           }
         }
-        // one thread waits for planes zA+2, zA+3 (bounded); the barrier
+        // one thread waits for planes zA+H, zA+H+1 (bounded); the barrier
         // releases the rest, and each thread takes the completed phases
-        const unsigned par2 = blk ^ (unsigned)(((2 * u + H + 2) / NU) & 1);
-        const unsigned par3 = blk ^ (unsigned)(((2 * u + H + 3) / NU) & 1);
-        const bool has3 = zA + 3 <= plast;
+        const unsigned para = blk ^ (unsigned)(((2 * u + 2 * H) / NU) & 1);
+        const unsigned parb = blk ^ (unsigned)(((2 * u + 2 * H + 1) / NU) & 1);
+        const bool hasqb = zA + H + 1 <= plast;
         bool ok = true;
         if (tid == 0) {
-          ok = mbar_wait(&bars[s2], par2);
-          if (has3) ok &= mbar_wait(&bars[s3], par3);
+          ok = mbar_wait(&bars[sqa], para);
+          if (hasqb) ok &= mbar_wait(&bars[sqb], parb);
           if (!ok) atomicExch(A.err, NLSE_ERR_TIMEOUT);
         }
         if (__syncthreads_or(!ok)) {
           drain(zA + 5);
           return;
         }
-        (void)tiled::mbar_try_wait(&bars[s2], par2);
-        q[s2] = qload(zA + 2, s2);
-        if (has3) {
-          (void)tiled::mbar_try_wait(&bars[s3], par3);
-          q[s3] = qload(zA + 3, s3);
+        (void)tiled::mbar_try_wait(&bars[sqa], para);
+        q[sqa] = qload(zA + H, sqa);
+        if (hasqb) {
+          (void)tiled::mbar_try_wait(&bars[sqb], parb);
+          q[sqb] = qload(zA + H + 1, sqb);
         }
         if (inner) {
           point(zA, pA, s0, q[s0], q[s1], q[sm1], q[s2], q[sm2], vA, loA, kA, edge_pt);
@@ -1027,13 +1036,13 @@ inline TileOrder tile_order(const Geom& g, int TX, int TY, int H, int zc) {
   return t;
 }
 
-extern int g_z2;  // 2SHOC with TMA staging: two planes per iteration (1) or one (0)
+extern int g_z2;  // TMA staging: two planes per iteration (1) or one (0)
 
-template <int STAGE>
+template <int METHOD, int STAGE>
 cudaError_t launch_inner_z2(const Geom& g, const Args& A, cudaStream_t st, const CUtensorMap& m0,
                             const CUtensorMap& m1) {
-  typedef WShape2 SH;
-  auto kern = wide3d_z2<STAGE>;
+  typedef WShape2<METHOD> SH;
+  auto kern = wide3d_z2<METHOD, STAGE>;
   static int occ = 0;
   if (!occ) {
     cudaError_t e =
@@ -1072,12 +1081,12 @@ cudaError_t launch_inner(const Geom& g, const Args& A, cudaStream_t st, const CU
 template <int METHOD, bool TMA>
 cudaError_t launch_inner_stage(const Geom& g, const Args& A, cudaStream_t st,
                                const CUtensorMap& m0, const CUtensorMap& m1) {
-  if (METHOD == 2 && TMA && g_z2) {
+  if (TMA && g_z2) {
     switch (A.stage) {
-      case 1: return launch_inner_z2<1>(g, A, st, m0, m1);
-      case 2: return launch_inner_z2<2>(g, A, st, m0, m1);
-      case 3: return launch_inner_z2<3>(g, A, st, m0, m1);
-      case 4: return launch_inner_z2<4>(g, A, st, m0, m1);
+      case 1: return launch_inner_z2<METHOD, 1>(g, A, st, m0, m1);
+      case 2: return launch_inner_z2<METHOD, 2>(g, A, st, m0, m1);
+      case 3: return launch_inner_z2<METHOD, 3>(g, A, st, m0, m1);
+      case 4: return launch_inner_z2<METHOD, 4>(g, A, st, m0, m1);
     }
   }
   switch (A.stage) {

@@ -1,7 +1,8 @@
-"""Mixed-precision 3D 2SHOC interior kernel, two planes per iteration: the
-same bits as the one-plane kernel (same per-point arithmetic), run after
-run, for every boundary condition, on grids and z chunks with odd and even
-plane counts (the last iteration of a chunk may hold a single plane)."""
+"""Mixed-precision 3D interior kernel, two planes per iteration: the same
+bits as the one-plane kernel (same per-point arithmetic), run after run, for
+both methods and every boundary condition, on grids and z chunks with odd
+and even plane counts (the last iteration of a chunk may hold a single
+plane)."""
 import numpy as np
 import pytest
 
@@ -11,7 +12,7 @@ CASES = [((19, 17, 20), 0), ((21, 12, 34), 0), ((40, 40, 40), 0), ((3, 3, 4), 0)
          ((70, 45, 100), 0), ((37, 33, 66), 5), ((37, 33, 66), 7), ((50, 24, 32), 16)]
 
 
-def _run(shape, BC, z2, zc, steps=3):
+def _run(shape, BC, z2, zc, steps=3, method=2):
     import nlsemagic_gb300 as ng
     from nlsemagic_gb300 import autotune
     z, y, x = np.meshgrid(*[np.linspace(0.0, 1.0, n) for n in shape], indexing="ij")
@@ -22,7 +23,7 @@ def _run(shape, BC, z2, zc, steps=3):
     try:
         autotune.set_knob("wide.z2", z2)
         autotune.set_knob("wide.zc", zc)
-        with ng.Solver(shape, method=2, precision=ng.PREC_MIXED, BC=BC, s=-1.0, a=1.0,
+        with ng.Solver(shape, method=method, precision=ng.PREC_MIXED, BC=BC, s=-1.0, a=1.0,
                        h2=0.09, k=0.004) as sv:
             sv.upload(U, V)
             sv.run(steps)
@@ -32,12 +33,13 @@ def _run(shape, BC, z2, zc, steps=3):
             autotune.set_knob(k, v)
 
 
+@pytest.mark.parametrize("method", [1, 2])
 @pytest.mark.parametrize("BC", [1, 2, 3])
 @pytest.mark.parametrize("shape,zc", CASES)
-def test_two_planes_match_one(gpu_lib, shape, zc, BC):
-    one = _run(shape, BC, 0, zc)
+def test_two_planes_match_one(gpu_lib, shape, zc, BC, method):
+    one = _run(shape, BC, 0, zc, method=method)
     assert np.all(np.isfinite(one))
     for _ in range(2):
-        two = _run(shape, BC, 1, zc)
+        two = _run(shape, BC, 1, zc, method=method)
         assert np.array_equal(two.view(np.float64), one.view(np.float64)), \
             "max |diff| %g" % np.max(np.abs(two - one))
