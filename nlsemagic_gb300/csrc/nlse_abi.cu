@@ -59,6 +59,7 @@ extern int g_pdl;
 extern int g_face_bps;
 extern int g_tile_order;
 extern int g_z2;
+extern int g_wide2d;
 }
 }  // namespace nlse
 static int g_default_graph_steps = 8;
@@ -73,6 +74,11 @@ extern "C" int nlse_tune_set(const char* key, long long value) {
   if (!strcmp(key, "wide.zc")) {
     if (value < 0 || value > (1 << 20)) return fail(NLSE_ERR_ARG, "wide.zc out of range");
     nlse::wide::g_zc_override = (int)value;
+    return NLSE_OK;
+  }
+  if (!strcmp(key, "wide2d")) {
+    if (value != 0 && value != 1) return fail(NLSE_ERR_ARG, "wide2d must be 0 or 1");
+    nlse::wide::g_wide2d = (int)value;
     return NLSE_OK;
   }
   if (!strcmp(key, "wide.z2")) {
@@ -112,6 +118,10 @@ extern "C" int nlse_tune_get(const char* key, long long* value) {
   if (!key || !value) return fail(NLSE_ERR_ARG, "NULL argument");
   if (!strcmp(key, "wide.zc")) {
     *value = nlse::wide::g_zc_override;
+    return NLSE_OK;
+  }
+  if (!strcmp(key, "wide2d")) {
+    *value = nlse::wide::g_wide2d;
     return NLSE_OK;
   }
   if (!strcmp(key, "wide.z2")) {

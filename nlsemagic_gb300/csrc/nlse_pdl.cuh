@@ -11,7 +11,8 @@
 
 namespace nlse {
 namespace wide {
-extern int g_pdl;  // stage kernels launched with PDL (1) or in plain stream order (0)
+extern int g_pdl;     // stage kernels launched with PDL (1) or in plain stream order (0)
+extern int g_wide2d;  // 2D mixed grids: single-pass stage kernel (1) or gather form (0)
 }
 
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }

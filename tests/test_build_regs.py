@@ -1,7 +1,8 @@
 """The mixed-precision 3D interior kernel is compiled for 4 resident CTAs per
 SM (64 registers); a register spill there costs far more than it saves, so
 the build must report none (checked with ptxas, no GPU needed).  This
-covers both interior kernels: one plane per iteration and two."""
+covers both interior kernels (one plane per iteration and two) and the 2D
+single-pass stage kernel."""
 import os
 import re
 import shutil
@@ -25,11 +26,12 @@ def test_interior_kernel_does_not_spill(tmp_path):
     seen = 0
     for b in blocks[1:]:
         name = b.split("'", 1)[0]
-        if "wide6wide3d" not in name and "wide9wide3d_z2" not in name:
+        if "wide6wide3d" not in name and "wide9wide3d_z2" not in name and \
+                "wide2d7stage2d" not in name:
             continue
         seen += 1
         m = re.search(r"(\d+) bytes spill stores, (\d+) bytes spill loads", b)
         assert m and m.group(1) == "0" and m.group(2) == "0", (name, m.group(0) if m else b[:200])
-    # 2 methods x 4 stages x TMA / plain loads, and the two-plane form's
-    # 2 methods x 4 stages
-    assert seen == 24
+    # 2 methods x 4 stages x TMA / plain loads, the two-plane form's
+    # 2 methods x 4 stages, and the 2D kernel's 2 methods x 3 codes x 4 stages
+    assert seen == 48
