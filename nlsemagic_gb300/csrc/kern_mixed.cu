@@ -20,6 +20,9 @@ int g_z2 = 1;
 // 2D grids (BC 1-3): one single-pass stage kernel per stage (kern_wide2d.cuh)
 int g_wide2d = 1;
 }
+namespace wide2d {
+int g_ty = 0;
+}
 
 template <int DIM, int METHOD, int BC>
 static cudaError_t launch_one(const Geom& g, const Consts<float>& c, const MixedStageArgs& a,

@@ -1,6 +1,6 @@
 // Mixed-precision 2D stage kernel: one launch per RK4 stage, no scratch.
 //
-// A CTA owns a 32 x 32 tile and stages it with a 2-cell halo (hi and E) in
+// A CTA owns a 32 x TY tile and stages it with a 2-cell halo (hi and E) in
 // shared memory with coalesced row loads.  Interior points take the 2SHOC
 // wide form a/(12 h^2) (16 sum_f (Y_f - Y_0) - sum_2 (Y_2 - Y_0)) (or the CD
 // five-point form) from shared memory, so D is never formed.  Next to a face
@@ -10,15 +10,22 @@
 // identity in 2D).  Unlike the streaming 3D kernel a 2D tile is staged once,
 // so the face work costs each edge tile one extra pass and no per-plane
 // wait:
-//   1. stage the tile (cells outside the grid are zero);
+//   1. stage the tile (cells outside the grid are zero); the V values of
+//      the ghosts (at b and q) and, on short tiles, the point-local inputs
+//      of the update (V, lo, K) are loaded in the same round trip;
 //   2. edge tiles: the ghost beyond every face-interior face point of the
 //      tile, written into the halo cell it replaces;
 //   3. every interior point: F, stage update (F next to a face kept in
 //      shared memory for the MSD formula);
 //   4. edge tiles: every face point, from its MSD neighbour (same tile).
-// Tiles start at (32 bx - sx, 32 by - sy), sx, sy in {0, 1}, chosen so that
-// no tile starts at x = M-1 or y = N-1: a face point and its MSD neighbour
-// (coordinates clamped into [1, n-2]) then lie in the same tile.
+// Tiles start at (32 bx - sx, TY by - sy), sx, sy in {0, 1}, chosen so that
+// no tile starts at x = M-1 or y = N-1 (nor, as tiles are at least 3 cells
+// high, at 1): a face point and its MSD neighbour (coordinates clamped into
+// [1, n-2]) then lie in the same tile, and so do an interior point next to
+// a face and the face point whose ghost it reads.
+// TY (32, 16 or 8 rows; 4, 2 or 1 per thread) trades the halo's share of
+// the staged cells against the number of CTAs: short tiles keep every SM
+// busy on small grids.
 // The arithmetic is that of the mixed class (nlse_mixed.cuh): explicit
 // rounding, difference-form sums.
 #pragma once
@@ -29,27 +36,51 @@
 namespace nlse {
 namespace wide2d {
 
-constexpr int T = 32, HALO = 2, S = T + 2 * HALO;  // tile, staged side
-constexpr int BX = 32, BY = 8, NT = BX * BY;        // threads; 4 rows each
+extern int g_ty;  // tile height: 0 = by grid size, else 8, 16 or 32
+
+constexpr int TX = 32, HALO = 2, SX = TX + 2 * HALO;  // tile width, staged width
+constexpr int BX = 32, BY = 8, NT = BX * BY;           // threads
+
+// Launch shape per tile height.  Short tiles (small grids, latency-bound):
+// the point-local inputs are loaded with the tile, one round trip.  Taller
+// tiles (large grids, HBM-bound): loaded at their use, and the register
+// budget set for 8 resident CTAs per SM (32 registers; 6 CTAs and 40 for
+// MSD 2SHOC, whose ghost arithmetic spills at 32) so that more loads are in
+// flight.
+template <int TY>
+struct Shape {
+  static constexpr bool prefetch = TY == 8;
+};
+template <int METHOD, int BC, int TY>
+constexpr int min_blocks() {
+  return TY == 8 || (METHOD == 2 && BC == 2) ? 6 : 8;
+}
 
 struct Args {
   MixedStageArgs a;
   Consts<float> c;
 };
 
-template <int METHOD, int BC, int STAGE>
-__global__ void __launch_bounds__(NT) stage2d(Geom g, Args A, int sx, int sy) {
-  __shared__ float2 sh[S][S], se[S][S];
-  __shared__ float2 fq[T][T];  // F at the points next to a face (MSD)
+template <int METHOD, int BC, int STAGE, int TY>
+__global__ void __launch_bounds__(NT, min_blocks<METHOD, BC, TY>())
+    stage2d(Geom g, Args A, int sx, int sy) {
+  constexpr int SY = TY + 2 * HALO, R = TY / BY;
+  constexpr bool PF = Shape<TY>::prefetch;
+  constexpr int NG = 2 * TY + 2 * TX;  // face points of a tile: x faces, then y faces
+  __shared__ float2 sh[SY][SX], se[SY][SX];
+  __shared__ float2 fq[TY][TX];  // F at the points next to a face (MSD)
   typedef mixed::HE HE;
   pdl_trigger();  // the next kernel may launch; it waits for this one
   pdl_wait();     // the previous kernel's output
   const int M = g.M, N = g.N;
-  const int x0 = (int)blockIdx.x * T - sx, y0 = (int)blockIdx.y * T - sy;
-  const int tid = threadIdx.y * BX + threadIdx.x;
+  const int x0 = (int)blockIdx.x * TX - sx, y0 = (int)blockIdx.y * TY - sy;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * BX + tx;
   const float2* Ein = STAGE == 1 ? A.a.lo_in : A.a.e_in;
-  for (int i = tid; i < S * S; i += NT) {
-    const int cy = i / S, cx = i - cy * S, gx = x0 - HALO + cx, gy = y0 - HALO + cy;
+  const bool edge = x0 <= 0 || x0 + TX > M - 1 || y0 <= 0 || y0 + TY > N - 1;
+
+  // 1. staged tile (and the point-local inputs with it on short tiles)
+  for (int i = tid; i < SY * SX; i += NT) {
+    const int cy = i / SX, cx = i - cy * SX, gy = y0 - HALO + cy, gx = x0 - HALO + cx;
     float2 h = make_float2(0.f, 0.f), e = h;
     if (gx >= 0 && gx < M && gy >= 0 && gy < N) {
       const unsigned p = (unsigned)gy * M + gx;
@@ -59,6 +90,46 @@ __global__ void __launch_bounds__(NT) stage2d(Geom g, Args A, int sx, int sy) {
     sh[cy][cx] = h;
     se[cy][cx] = e;
   }
+  float vr[R];
+  float2 lor[R], kr[R];
+  // point-local inputs of row r (the loads are placed here, or at the use)
+  auto local = [&](int r) {
+    const int x = x0 + tx, y = y0 + ty + BY * r;
+    vr[r] = 0.f;
+    lor[r] = kr[r] = make_float2(0.f, 0.f);
+    if (x >= 0 && x < M && y >= 0 && y < N) {
+      const unsigned p = (unsigned)y * M + x;
+      vr[r] = A.a.V[p];
+      if (STAGE != 1) lor[r] = __ldcg(A.a.lo_in + p);
+      if (STAGE == 4) kr[r] = __ldcg(A.a.K + p);
+    }
+  };
+  if (PF) {
+#pragma unroll
+    for (int r = 0; r < R; ++r) local(r);
+  }
+  // ghost task of this thread (METHOD 2, edge tiles): face point b, inward
+  // neighbour q, inward step (dx, dy)
+  bool gt = false;
+  int bx = 0, by = 0, dx = 0, dy = 0;
+  float vb = 0.f, vq = 0.f;
+  if (METHOD == 2 && edge && tid < NG) {
+    if (tid < 2 * TY) {
+      const int side = tid / TY;
+      bx = side == 0 ? 0 : M - 1;
+      by = y0 + (tid - side * TY);
+      dx = side == 0 ? 1 : -1;
+      gt = bx >= x0 && bx < x0 + TX && by >= 1 && by <= N - 2;
+    } else {
+      const int side = (tid - 2 * TY) / TX;
+      by = side == 0 ? 0 : N - 1;
+      bx = x0 + (tid - 2 * TY - side * TX);
+      dy = side == 0 ? 1 : -1;
+      gt = by >= y0 && by < y0 + TY && bx >= 1 && bx <= M - 2;
+    }
+    if (gt && BC != 3) vb = A.a.V[(unsigned)by * M + bx];
+    if (gt && BC == 2) vq = A.a.V[(unsigned)(by + dy) * M + bx + dx];
+  }
   __syncthreads();
   auto at = [&](int x, int y) -> HE {  // grid coordinates inside the staged tile
     HE r;
@@ -66,23 +137,10 @@ __global__ void __launch_bounds__(NT) stage2d(Geom g, Args A, int sx, int sy) {
     r.e = se[y - y0 + HALO][x - x0 + HALO];
     return r;
   };
-  const bool edge = x0 <= 0 || x0 + T > M - 1 || y0 <= 0 || y0 + T > N - 1;
+
+  // 2. ghosts beyond the face points of an edge tile
   if (METHOD == 2 && edge) {
-    // ghosts: side 0 x = 0, 1 x = M-1, 2 y = 0, 3 y = N-1; 32 face points each
-    for (int t = tid; t < 4 * T; t += NT) {
-      const int side = t / T, k = t - side * T;
-      int bx, by, dx = 0, dy = 0;
-      if (side < 2) {
-        bx = side == 0 ? 0 : M - 1;
-        by = y0 + k;
-        dx = side == 0 ? 1 : -1;
-        if (bx < x0 || bx >= x0 + T || by < 1 || by > N - 2) continue;
-      } else {
-        by = side == 2 ? 0 : N - 1;
-        bx = x0 + k;
-        dy = side == 2 ? 1 : -1;
-        if (by < y0 || by >= y0 + T || bx < 1 || bx > M - 2) continue;
-      }
+    if (gt) {
       const int qx = bx + dx, qy = by + dy;
       const HE ub = at(bx, by), uq = at(qx, qy);
       float2 dq = make_float2(0.f, 0.f);
@@ -90,8 +148,7 @@ __global__ void __launch_bounds__(NT) stage2d(Geom g, Args A, int sx, int sy) {
         const HE nq[4] = {at(qx, qy + 1), at(qx, qy - 1), at(qx + 1, qy), at(qx - 1, qy)};
         dq = mixed::d_interior<2>(A.c, uq, nq);
       }
-      const unsigned pb = (unsigned)by * M + bx, pq = (unsigned)qy * M + qx;
-      const float2 dbc = mixed::d_boundary<BC>(A.c, ub, A.a.V[pb], uq, A.a.V[pq], dq, nullptr);
+      const float2 dbc = mixed::d_boundary<BC>(A.c, ub, vb, uq, vq, dq, nullptr);
       const HE tn[2] = {at(bx + dy, by + dx), at(bx - dy, by - dx)};  // along the face
       const float2 st = mixed::lapsum<2>(ub, tn);
       const float2 sq = mixed::lapsum<1>(ub, &uq);
@@ -103,60 +160,96 @@ __global__ void __launch_bounds__(NT) stage2d(Geom g, Args A, int sx, int sy) {
     }
     __syncthreads();
   }
-  // interior points: 4 rows per thread
+
+  // stage update of point p from F and the point's own inputs
+  auto upd = [&](unsigned p, float2 Tv, const HE& u, float2 lo, float2 kv) {
+    const float2 lo_ = STAGE == 1 ? u.e : lo;  // stage 1: E = lo
+    float2 eo, ko, ho, l2;
+    mixed::stage_update(A.c, STAGE, Tv, u.h, lo_, u.e, kv, eo, ko, ho, l2);
+    if (STAGE == 2) A.a.K[p] = ko;
+    if (STAGE < 4) {
+      A.a.e_out[p] = eo;
+    } else {
+      A.a.hi_out[p] = ho;
+      A.a.lo_out[p] = l2;
+    }
+  };
+
+  // 3. interior points
 #pragma unroll
-  for (int r = 0; r < T / BY; ++r) {
-    const int lx = threadIdx.x, ly = threadIdx.y + BY * r, x = x0 + lx, y = y0 + ly;
+  for (int r = 0; r < R; ++r) {
+    const int ly = ty + BY * r, x = x0 + tx, y = y0 + ly;
     if (x < 1 || x > M - 2 || y < 1 || y > N - 2) continue;
-    const unsigned p = (unsigned)y * M + x;
+    if (!PF) local(r);
     const HE u0 = at(x, y);
     const HE fn[4] = {at(x, y + 1), at(x, y - 1), at(x + 1, y), at(x - 1, y)};
-    const float v = A.a.V[p];
     float2 Tv;
     if (METHOD == 1) {
-      Tv = mixed::f_interior_cd<2>(A.c, u0, v, fn);
+      Tv = mixed::f_interior_cd<2>(A.c, u0, vr[r], fn);
     } else {
       const HE f2n[4] = {at(x, y + 2), at(x, y - 2), at(x + 2, y), at(x - 2, y)};
-      Tv = mixed::f_wide_2shoc<2>(A.c, u0, v, fn, f2n);
+      Tv = mixed::f_wide_2shoc<2>(A.c, u0, vr[r], fn, f2n);
     }
-    if (BC == 2 && edge && (x == 1 || x == M - 2 || y == 1 || y == N - 2)) fq[ly][lx] = Tv;
-    mixed::update(A.c, STAGE, p, Tv, A.a.hi_in, A.a.lo_in, A.a.e_in, A.a.K, A.a.e_out,
-                  A.a.hi_out, A.a.lo_out);
+    if (BC == 2 && edge && (x == 1 || x == M - 2 || y == 1 || y == N - 2)) fq[ly][tx] = Tv;
+    upd((unsigned)y * M + x, Tv, u0, lor[r], kr[r]);
   }
   if (!edge) return;
-  __syncthreads();  // F next to the faces (fq)
-  // face points of the tile, from their MSD neighbour (same tile)
+  if (BC == 2) __syncthreads();  // F next to the faces (fq)
+
+  // 4. face points of the tile, from their MSD neighbour (same tile)
 #pragma unroll
-  for (int r = 0; r < T / BY; ++r) {
-    const int lx = threadIdx.x, ly = threadIdx.y + BY * r, x = x0 + lx, y = y0 + ly;
+  for (int r = 0; r < R; ++r) {
+    const int ly = ty + BY * r, x = x0 + tx, y = y0 + ly;
     if (x < 0 || x >= M || y < 0 || y >= N) continue;
     if (x >= 1 && x <= M - 2 && y >= 1 && y <= N - 2) continue;
+    if (!PF) local(r);
     const int qx = x < 1 ? 1 : (x > M - 2 ? M - 2 : x);
     const int qy = y < 1 ? 1 : (y > N - 2 ? N - 2 : y);
-    const unsigned p = (unsigned)y * M + x;
     const HE ub = at(x, y), uq = at(qx, qy);
     const float2 fqv = BC == 2 ? fq[qy - y0][qx - x0] : make_float2(0.f, 0.f);
-    const float2 Tv = mixed::f_boundary<METHOD, BC>(A.c, ub, A.a.V[p], uq, fqv, nullptr);
-    mixed::update(A.c, STAGE, p, Tv, A.a.hi_in, A.a.lo_in, A.a.e_in, A.a.K, A.a.e_out,
-                  A.a.hi_out, A.a.lo_out);
+    const float2 Tv = mixed::f_boundary<METHOD, BC>(A.c, ub, vr[r], uq, fqv, nullptr);
+    upd((unsigned)y * M + x, Tv, ub, lor[r], kr[r]);
   }
 }
 
-inline int shift(int n) { return (n - 1) % T == 0 ? 1 : 0; }
+inline int shift(int n, int t) { return (n - 1) % t == 0 ? 1 : 0; }
+
+inline int tiles(const Geom& g, int ty) {
+  return ((g.M + shift(g.M, TX) + TX - 1) / TX) * ((g.N + shift(g.N, ty) + ty - 1) / ty);
+}
+
+// Tile height by grid size (152 SMs): 32 rows from 32 tiles per SM (4096^2
+// and up), 16 rows from 8 tiles per SM, else 8 rows.
+inline int pick_ty(const Geom& g) {
+  if (g_ty) return g_ty;
+  if (tiles(g, 32) >= 32 * 152) return 32;
+  if (tiles(g, 16) >= 8 * 152) return 16;
+  return 8;
+}
+
+template <int METHOD, int BC, int TY>
+cudaError_t launch_ty(const Geom& g, const MixedStageArgs& a, const Consts<float>& c, int stage,
+                      cudaStream_t st, bool pdl) {
+  const int sx = shift(g.M, TX), sy = shift(g.N, TY);
+  const dim3 grid((g.M + sx + TX - 1) / TX, (g.N + sy + TY - 1) / TY), block(BX, BY);
+  const Args A{a, c};
+  switch (stage) {
+    case 1: return launch_k(stage2d<METHOD, BC, 1, TY>, grid, block, 0, st, pdl, g, A, sx, sy);
+    case 2: return launch_k(stage2d<METHOD, BC, 2, TY>, grid, block, 0, st, pdl, g, A, sx, sy);
+    case 3: return launch_k(stage2d<METHOD, BC, 3, TY>, grid, block, 0, st, pdl, g, A, sx, sy);
+    case 4: return launch_k(stage2d<METHOD, BC, 4, TY>, grid, block, 0, st, pdl, g, A, sx, sy);
+  }
+  return cudaErrorInvalidValue;
+}
 
 template <int METHOD, int BC>
 cudaError_t launch(const Geom& g, const MixedStageArgs& a, const Consts<float>& c, int stage,
                    cudaStream_t st, bool pdl) {
-  const int sx = shift(g.M), sy = shift(g.N);
-  const dim3 grid((g.M + sx + T - 1) / T, (g.N + sy + T - 1) / T);
-  const Args A{a, c};
-  switch (stage) {
-    case 1: return launch_k(stage2d<METHOD, BC, 1>, grid, dim3(BX, BY), 0, st, pdl, g, A, sx, sy);
-    case 2: return launch_k(stage2d<METHOD, BC, 2>, grid, dim3(BX, BY), 0, st, pdl, g, A, sx, sy);
-    case 3: return launch_k(stage2d<METHOD, BC, 3>, grid, dim3(BX, BY), 0, st, pdl, g, A, sx, sy);
-    case 4: return launch_k(stage2d<METHOD, BC, 4>, grid, dim3(BX, BY), 0, st, pdl, g, A, sx, sy);
+  switch (pick_ty(g)) {
+    case 32: return launch_ty<METHOD, BC, 32>(g, a, c, stage, st, pdl);
+    case 16: return launch_ty<METHOD, BC, 16>(g, a, c, stage, st, pdl);
+    default: return launch_ty<METHOD, BC, 8>(g, a, c, stage, st, pdl);
   }
-  return cudaErrorInvalidValue;
 }
 
 }  // namespace wide2d

@@ -61,6 +61,9 @@ extern int g_tile_order;
 extern int g_z2;
 extern int g_wide2d;
 }
+namespace wide2d {
+extern int g_ty;
+}
 }  // namespace nlse
 static int g_default_graph_steps = 8;
 // FP32 and mixed 1D solves of at most this many points run each chunk in
@@ -79,6 +82,12 @@ extern "C" int nlse_tune_set(const char* key, long long value) {
   if (!strcmp(key, "wide2d")) {
     if (value != 0 && value != 1) return fail(NLSE_ERR_ARG, "wide2d must be 0 or 1");
     nlse::wide::g_wide2d = (int)value;
+    return NLSE_OK;
+  }
+  if (!strcmp(key, "wide2d.ty")) {
+    if (value != 0 && value != 8 && value != 16 && value != 32)
+      return fail(NLSE_ERR_ARG, "wide2d.ty must be 0, 8, 16 or 32");
+    nlse::wide2d::g_ty = (int)value;
     return NLSE_OK;
   }
   if (!strcmp(key, "wide.z2")) {
@@ -122,6 +131,10 @@ extern "C" int nlse_tune_get(const char* key, long long* value) {
   }
   if (!strcmp(key, "wide2d")) {
     *value = nlse::wide::g_wide2d;
+    return NLSE_OK;
+  }
+  if (!strcmp(key, "wide2d.ty")) {
+    *value = nlse::wide2d::g_ty;
     return NLSE_OK;
   }
   if (!strcmp(key, "wide.z2")) {

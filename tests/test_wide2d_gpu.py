@@ -3,8 +3,8 @@
 launch).  Against the FP64 oracle within the mixed tolerance on grids whose
 sides fall on every residue the tiling treats differently (n = 32 m + 1,
 which shifts the tiles by one cell; n = 32 m; thin and tiny grids), for
-both methods and every boundary code; the same bits run after run; and
-within the tolerance of the gather form it replaces."""
+both methods, every boundary code and every tile height; the same bits run
+after run; and within the tolerance of the gather form it replaces."""
 import numpy as np
 import pytest
 
@@ -29,18 +29,20 @@ def _field(shape):
     return U, V, h
 
 
-def _gpu(U, V, h, BC, method, steps, k, wide2d=1, gather=False):
+def _gpu(U, V, h, BC, method, steps, k, wide2d=1, gather=False, ty=0):
     import nlsemagic_gb300 as ng
     from nlsemagic_gb300 import autotune
-    old = autotune.get_knob("wide2d")
+    old = {key: autotune.get_knob(key) for key in ("wide2d", "wide2d.ty")}
     try:
         autotune.set_knob("wide2d", wide2d)
+        autotune.set_knob("wide2d.ty", ty)
         flags = ng.FLAG_MSD_GUARD | (ng.FLAG_GATHER if gather else 0)
         return np.ascontiguousarray(
             ng.take_steps(U, V, -1.0, 1.0, h * h, BC, steps, k, method=method,
                           precision=ng.PREC_MIXED, flags=flags))
     finally:
-        autotune.set_knob("wide2d", old)
+        for key, v in old.items():
+            autotune.set_knob(key, v)
 
 
 @pytest.mark.parametrize("shape", SHAPES)
@@ -52,21 +54,23 @@ def test_wide2d_against_oracle(gpu_lib, shape, method, BC):
     steps = 12
     want = oracle.take_steps(U, V, -1.0, 1.0, h * h, BC, steps, k, method=method, precision=2,
                              flags=oracle.MSD_GUARD)
-    got = _gpu(U, V, h, BC, method, steps, k)
-    assert np.all(np.isfinite(got))
-    assert W.rel_l2(got, want) <= MIXED_TOL
+    for ty in (0, 8, 16, 32):  # by grid size, then each tile height
+        got = _gpu(U, V, h, BC, method, steps, k, ty=ty)
+        assert np.all(np.isfinite(got))
+        assert W.rel_l2(got, want) <= MIXED_TOL, ty
     # the gather form it replaces: same tolerance against the oracle
     assert W.rel_l2(_gpu(U, V, h, BC, method, steps, k, wide2d=0), want) <= MIXED_TOL
 
 
+@pytest.mark.parametrize("ty", [8, 16, 32])
 @pytest.mark.parametrize("method", [1, 2])
 @pytest.mark.parametrize("BC", [1, 2, 3])
-def test_wide2d_deterministic(gpu_lib, method, BC):
+def test_wide2d_deterministic(gpu_lib, method, BC, ty):
     U, V, h = _field((161, 96))
     k = 0.5 * W.linear_stability_k(2, method, h, 1.0)
-    first = _gpu(U, V, h, BC, method, 40, k)
+    first = _gpu(U, V, h, BC, method, 40, k, ty=ty)
     for _ in range(2):
-        again = _gpu(U, V, h, BC, method, 40, k)
+        again = _gpu(U, V, h, BC, method, 40, k, ty=ty)
         assert np.array_equal(again.view(np.float64), first.view(np.float64))
 
 
@@ -84,3 +88,5 @@ def test_wide2d_knob_range(gpu_lib):
     from nlsemagic_gb300 import autotune
     with pytest.raises(Exception):
         autotune.set_knob("wide2d", 2)
+    with pytest.raises(Exception):
+        autotune.set_knob("wide2d.ty", 4)
