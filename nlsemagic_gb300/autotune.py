@@ -9,7 +9,9 @@ knobs and keeps the fastest:
                    CTA streams through; trades queue-fill overhead against the
                    number of CTAs in flight),
 * ``graph.steps``  RK4 steps captured per CUDA graph (launch overhead against
-                   graph size; matters for small grids).
+                   graph size; matters for small grids),
+* ``wide2d.ty``    tile height of the mixed-precision 2D stage kernel (8, 16
+                   or 32 rows: CTAs in flight against halo re-reads).
 
 The library has one more knob, ``wide.pdl`` (1 by default: the 3D 2SHOC
 stage kernels overlap through programmatic dependent launch; 0: plain stream
@@ -33,7 +35,7 @@ import numpy as np
 from . import _lib
 from .api import Solver, grid_dims
 
-KNOBS = ("wide.zc", "graph.steps")
+KNOBS = ("wide.zc", "graph.steps", "wide2d.ty")
 
 
 def set_knob(key, value):
@@ -94,13 +96,16 @@ def _smooth_state(shape, h):
 def candidates(shape, precision):
     ndim, dims = grid_dims(shape)
     cands = []
-    zcs = [0]
+    zcs, tys = [0], [0]
     if ndim == 3 and precision == 3:
         L = dims[2]
         zcs = sorted({z for z in (16, 32, 48, 64, 96, 128, 192, L) if 4 <= z <= L})
+    if ndim == 2 and precision == 3:
+        tys = [8, 16, 32]
     for zc in zcs:
-        for gs in (4, 10, 25):
-            cands.append({"wide.zc": zc, "graph.steps": gs})
+        for ty in tys:
+            for gs in (4, 10, 25):
+                cands.append({"wide.zc": zc, "graph.steps": gs, "wide2d.ty": ty})
     return cands
 
 

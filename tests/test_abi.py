@@ -64,6 +64,23 @@ def test_tuning_knobs_roundtrip_and_validation(lib):
         autotune.set_knob("no.such.knob", 1)
     with pytest.raises(_lib.NLSEError):
         autotune.set_knob("graph.steps", -3)
+    for key, good, bad in (("wide2d", 0, 2), ("wide2d.ty", 16, 12)):
+        old = autotune.get_knob(key)
+        autotune.set_knob(key, good)
+        assert autotune.get_knob(key) == good
+        with pytest.raises(_lib.NLSEError):
+            autotune.set_knob(key, bad)
+        autotune.set_knob(key, old)
+
+
+def test_autotune_candidates_per_class():
+    from nlsemagic_gb300 import autotune
+    two = autotune.candidates((256, 256), 3)
+    assert {c["wide2d.ty"] for c in two} == {8, 16, 32}
+    assert all(c["wide.zc"] == 0 for c in two)
+    three = autotune.candidates((64, 64, 64), 3)
+    assert {c["wide2d.ty"] for c in three} == {0} and len({c["wide.zc"] for c in three}) > 1
+    assert all(set(c) == set(autotune.KNOBS) for c in two + three)
 
 
 def _call(lib, U, BC=2, method=1, precision=2, dims=None, h2=0.01, k=1e-3, chunk=1):
