@@ -1,7 +1,10 @@
 // Exact-precision (FP64 / FP32) stage launchers.  This translation unit is
 // compiled with -fmad=false: no multiply-add is contracted, so every
 // operation rounds exactly as in the reference C integrators.
+#include <type_traits>
+
 #include "kern_gather.cuh"
+#include "kern_tile2d.cuh"
 #include "kern_tiled.cuh"
 #include "nlse_launch.h"
 
@@ -12,6 +15,14 @@ static cudaError_t launch_one(const Geom& g, const Consts<R>& c, const ExactStag
                               int stage, cudaStream_t st, int kernel_kind) {
   if (kernel_kind == KERNEL_TILED && tiled_supported(g, DIM)) {
     return tiled::launch_exact<R, DIM, METHOD, BC>(g, c, a, stage, st);
+  }
+  // FP32 2SHOC on 2D grids: the single-pass tile kernel (1.4-1.5x the
+  // two-launch D-scratch form).  FP64 stays on the gather kernels, bound by
+  // FP64 issue, where the tile's D on the halo costs more than the D scratch;
+  // so does CD, a single gather launch already.
+  if constexpr (DIM == 2 && METHOD == 2 && std::is_same<R, float>::value) {
+    if (kernel_kind == KERNEL_TILED && BC != 4 && wide::g_wide2d)
+      return tile2d::launch<R, METHOD, BC == 4 ? 1 : BC>(g, c, a, stage, st, wide::g_pdl != 0);
   }
   long long blocks = (g.n + 255) / 256;
   if (blocks > 152LL * 32) blocks = 152LL * 32;
@@ -32,6 +43,13 @@ long long exact_dsc_entries(const Geom& g, int method, int BC, int kernel_kind) 
   if (method != 2) return 0;
   const bool tiled = kernel_kind == KERNEL_TILED && tiled_supported(g, g.ndim) && BC != 4;
   return tiled ? 0 : g.n;
+}
+
+int exact_stage_launches(const Geom& g, int method, int BC, int kernel_kind, bool single) {
+  if (g.ndim == 2 && method == 2 && single && kernel_kind == KERNEL_TILED && BC != 4 &&
+      wide::g_wide2d)
+    return 1;
+  return exact_dsc_entries(g, method, BC, kernel_kind) ? 2 : 1;  // (D,) F
 }
 
 template <typename R, int DIM, int METHOD>

@@ -31,12 +31,11 @@
 #pragma once
 
 #include "kern_gather.cuh"
+#include "nlse_launch.h"
 #include "nlse_pdl.cuh"
 
 namespace nlse {
 namespace wide2d {
-
-extern int g_ty;  // tile height: 0 = by grid size, else 8, 16 or 32
 
 constexpr int TX = 32, HALO = 2, SX = TX + 2 * HALO;  // tile width, staged width
 constexpr int BX = 32, BY = 8, NT = BX * BY;           // threads

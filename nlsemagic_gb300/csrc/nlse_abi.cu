@@ -684,7 +684,9 @@ extern "C" int nlse_solver_stream(nlse_solver* s, void** stream) {
 
 extern "C" int nlse_solver_launches_per_step(const nlse_solver* s) {
   if (!s) return 0;
-  if (s->prob.precision != NLSE_PREC_MIXED) return s->dsc ? 8 : 4;
+  if (s->prob.precision != NLSE_PREC_MIXED)
+    return 4 * exact_stage_launches(s->g, s->prob.method, s->prob.bc, s->kernel_kind,
+                                    s->prob.precision == NLSE_PREC_SINGLE);
   // mixed-precision 3D grids on the tiled path: deep-point kernel + shell kernel(s) per stage
   return 4 * mixed_stage_launches(s->g, s->prob.method, s->prob.bc, s->kernel_kind);
 }

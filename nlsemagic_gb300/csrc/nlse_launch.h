@@ -61,6 +61,7 @@ cudaError_t launch_small1d_mixed(const Geom& g, int method, int BC, const Consts
                                  long long nsteps, cudaStream_t st);
 
 int mixed_stage_launches(const Geom& g, int method, int BC, int kernel_kind);
+int exact_stage_launches(const Geom& g, int method, int BC, int kernel_kind, bool single);
 long long mixed_ghost_entries(const Geom& g, int method, int BC, int kernel_kind);
 long long mixed_fq_entries(const Geom& g, int method, int BC, int kernel_kind);
 // Points of D scratch (ExactStageArgs / MixedStageArgs ::dsc) a 2SHOC stage on
