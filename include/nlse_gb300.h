@@ -272,12 +272,13 @@ int nlse_take_steps_noalloc(const nlse_problem *p, const double *dUr, const doub
  *                  tiles: 1 (default) chunk by chunk (neighbouring tiles
  *                  share their halo through L2), 0 every face tile last.
  *                  Same bits either way.
- *   "wide2d"       1 (default): mixed-precision 2D grids (BC 1-3) take
- *                  the single-pass stage kernel (one launch per stage, wide
- *                  form, ghost cells in shared memory); 0: the gather
- *                  kernels (two launches per 2SHOC stage).  Results agree
- *                  within the mixed tolerance, not bit for bit.
- *   "wide2d.ty"    tile height of that kernel: 0 (default) by grid size,
+ *   "wide2d"       1 (default): 2D grids (BC 1-3) of the mixed class, and
+ *                  FP32 2SHOC, take the single-pass stage kernels (one
+ *                  launch per stage, the tile staged in shared memory);
+ *                  0: the gather kernels (two launches per 2SHOC stage).
+ *                  FP32: same bits; mixed: within the mixed tolerance, not
+ *                  bit for bit (the single-pass kernel takes the wide form).
+ *   "wide2d.ty"    tile height of those kernels: 0 (default) by grid size,
  *                  or 8, 16, 32.  Same bits.
  * ---------------------------------------------------------------------- */
 int nlse_tune_set(const char *key, long long value);
