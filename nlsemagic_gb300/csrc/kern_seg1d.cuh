@@ -1,0 +1,117 @@
+// Mixed-precision 1D stage on one segment of SEG points: the stage input
+// (hi, E) staged once with a 2-cell halo in shared memory and, for 2SHOC, D
+// formed there on the segment and a 1-cell halo, so a 2SHOC stage takes one
+// pass instead of D into scratch, a grid-wide wait and F.
+//
+// Segments start at SEG t - s, s = 1 when (n-1) is a multiple of SEG, else 0,
+// so that none starts at 1 or n-1: an end point and its MSD neighbour share a
+// segment, and the neighbour's F (which reads D on both sides of it) is
+// formed from the segment's own D.  Every value is the same per-point
+// function of the same operands as in the gather kernels (kern_gather.cuh:
+// mixed::d_at, f_int, f_at_d), so the results are the same bits.
+// Boundary code 4 (one-sided ends) is not handled here.
+#pragma once
+
+#include "kern_gather.cuh"
+
+namespace nlse {
+namespace seg1d {
+
+constexpr int SEG = 1024, HALO = 2, NT = 256;
+
+__host__ __device__ inline int shift(long long n) { return (n - 1) % SEG == 0 ? 1 : 0; }
+__host__ __device__ inline long long segments(long long n) {
+  return (n + shift(n) + SEG - 1) / SEG;
+}
+
+struct IO {
+  const float2 *hi_in, *lo_in, *e_in;  // e_in: this stage's E (lo in stage 1)
+  const float* V;
+  float2 *K, *e_out, *hi_out, *lo_out;
+};
+
+// Shared memory of one segment: the staged input (hi, E) and D on
+// [x0-1, x0+SEG].
+struct Smem {
+  float2 sh[SEG + 2 * HALO], se[SEG + 2 * HALO];
+  float2 sd[SEG + 2];
+};
+
+// Segment t of a stage, by the NT threads (one-dimensional block) of the
+// calling CTA, in the shared memory it provides.
+template <int METHOD, int BC>
+__device__ __forceinline__ void segment(const Geom& g, const Consts<float>& c, const IO& io,
+                                        int stage, long long t, Smem& sm) {
+  static_assert(BC >= 1 && BC <= 3, "one-sided ends take the gather kernels");
+  typedef mixed::HE HE;
+  float2* sh = sm.sh;
+  float2* se = sm.se;
+  float2* sd = sm.sd;
+  const int tid = (int)threadIdx.x;
+  const int n = (int)g.n, x0 = (int)t * SEG - shift(n);  // n < 2^31 (validated)
+  const float2* E = stage == 1 ? io.lo_in : io.e_in;
+  for (int i = tid; i < SEG + 2 * HALO; i += NT) {
+    const int x = x0 - HALO + i;
+    float2 h = make_float2(0.f, 0.f), e = h;
+    if (x >= 0 && x < n) {
+      h = io.hi_in[x];
+      e = E[x];
+    }
+    sh[i] = h;
+    se[i] = e;
+  }
+  __syncthreads();
+  auto Y = [&](int x) -> HE {
+    HE r;
+    r.h = sh[x - x0 + HALO];
+    r.e = se[x - x0 + HALO];
+    return r;
+  };
+  auto dint = [&](int x) {  // d_int<1>: (x+1, x-1)
+    const HE nb[2] = {Y(x + 1), Y(x - 1)};
+    return mixed::d_interior<1>(c, Y(x), nb);
+  };
+  if (METHOD == 2) {
+    for (int i = tid; i < SEG + 2; i += NT) {
+      const int x = x0 - 1 + i;
+      float2 d = make_float2(0.f, 0.f);
+      if (x >= 0 && x < n) {
+        if (x >= 1 && x <= n - 2) {
+          d = dint(x);
+        } else {
+          const int q = x == 0 ? 1 : n - 2;
+          const float2 dq = BC == 2 ? dint(q) : make_float2(0.f, 0.f);
+          d = mixed::d_boundary<BC>(c, Y(x), io.V[x], Y(q), io.V[q], dq, nullptr);
+        }
+      }
+      sd[i] = d;
+    }
+    __syncthreads();
+  }
+  auto D = [&](int x) { return sd[x - x0 + 1]; };
+  auto fint = [&](int x) {  // f_int<1, 1> / f_int_d<1>
+    if (METHOD == 1) {
+      const HE nb[2] = {Y(x + 1), Y(x - 1)};
+      return mixed::f_interior_cd<1>(c, Y(x), io.V[x], nb);
+    }
+    const float2 dn[2] = {D(x + 1), D(x - 1)};
+    return mixed::f_interior_2shoc<1>(c, Y(x), io.V[x], D(x), dn, nullptr);
+  };
+  for (int r = 0; r < SEG / NT; ++r) {
+    const int x = x0 + tid + NT * r;
+    if (x < 0 || x >= n) continue;
+    float2 T;
+    if (x >= 1 && x <= n - 2) {
+      T = fint(x);
+    } else {
+      const int q = x == 0 ? 1 : n - 2;
+      const float2 fq = BC == 2 ? fint(q) : make_float2(0.f, 0.f);
+      T = mixed::f_boundary<METHOD, BC>(c, Y(x), io.V[x], Y(q), fq, nullptr);
+    }
+    mixed::update(c, stage, x, T, io.hi_in, io.lo_in, io.e_in, io.K, io.e_out, io.hi_out,
+                  io.lo_out);
+  }
+}
+
+}  // namespace seg1d
+}  // namespace nlse

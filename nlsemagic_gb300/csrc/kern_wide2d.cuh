@@ -60,20 +60,30 @@ struct Args {
   Consts<float> c;
 };
 
+// Shared memory of one tile: the staged tile (hi, E) and F at the points
+// next to a face (MSD).
+template <int TY>
+struct Smem {
+  float2 sh[TY + 2 * HALO][SX], se[TY + 2 * HALO][SX];
+  float2 fq[TY][TX];
+};
+
+// One tile (bxi, byi) of a stage, by the NT threads of the calling CTA (the
+// stage kernel below, or the batched persistent kernel, nlse_batch.cu), in
+// the shared memory the caller provides.
 template <int METHOD, int BC, int STAGE, int TY>
-__global__ void __launch_bounds__(NT, min_blocks<METHOD, BC, TY>())
-    stage2d(Geom g, Args A, int sx, int sy) {
+__device__ __forceinline__ void tile(const Geom& g, const Args& A, int bxi, int byi, int sx,
+                                     int sy, Smem<TY>& sm) {
   constexpr int SY = TY + 2 * HALO, R = TY / BY;
   constexpr bool PF = Shape<TY>::prefetch;
   constexpr int NG = 2 * TY + 2 * TX;  // face points of a tile: x faces, then y faces
-  __shared__ float2 sh[SY][SX], se[SY][SX];
-  __shared__ float2 fq[TY][TX];  // F at the points next to a face (MSD)
+  auto& sh = sm.sh;
+  auto& se = sm.se;
+  auto& fq = sm.fq;
   typedef mixed::HE HE;
-  pdl_trigger();  // the next kernel may launch; it waits for this one
-  pdl_wait();     // the previous kernel's output
   const int M = g.M, N = g.N;
-  const int x0 = (int)blockIdx.x * TX - sx, y0 = (int)blockIdx.y * TY - sy;
-  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * BX + tx;
+  const int x0 = bxi * TX - sx, y0 = byi * TY - sy;
+  const int tid = (int)(threadIdx.y * blockDim.x + threadIdx.x), tx = tid % BX, ty = tid / BX;
   const float2* Ein = STAGE == 1 ? A.a.lo_in : A.a.e_in;
   const bool edge = x0 <= 0 || x0 + TX > M - 1 || y0 <= 0 || y0 + TY > N - 1;
 
@@ -211,9 +221,18 @@ __global__ void __launch_bounds__(NT, min_blocks<METHOD, BC, TY>())
   }
 }
 
-inline int shift(int n, int t) { return (n - 1) % t == 0 ? 1 : 0; }
+template <int METHOD, int BC, int STAGE, int TY>
+__global__ void __launch_bounds__(NT, min_blocks<METHOD, BC, TY>())
+    stage2d(Geom g, Args A, int sx, int sy) {
+  __shared__ Smem<TY> sm;
+  pdl_trigger();  // the next kernel may launch; it waits for this one
+  pdl_wait();     // the previous kernel's output
+  tile<METHOD, BC, STAGE, TY>(g, A, (int)blockIdx.x, (int)blockIdx.y, sx, sy, sm);
+}
 
-inline int tiles(const Geom& g, int ty) {
+__host__ __device__ inline int shift(int n, int t) { return (n - 1) % t == 0 ? 1 : 0; }
+
+__host__ __device__ inline int tiles(const Geom& g, int ty) {
   return ((g.M + shift(g.M, TX) + TX - 1) / TX) * ((g.N + shift(g.N, ty) + ty - 1) / ty);
 }
 

@@ -2,10 +2,15 @@
 // include/nlse_gb300.h).
 //
 // Device side: a cooperative persistent kernel.  All active solves are cut
-// into tiles of TILE consecutive grid points; per RK4 stage every CTA pulls
-// tiles from an atomic work-queue counter of that stage until the queue is
-// empty, evaluates the stage with the gather-form stencil (kern_gather.cuh)
-// for the tile's solve, and then waits at a grid barrier.  The barrier spins
+// into tiles; per RK4 stage every CTA pulls tiles from an atomic work-queue
+// counter of that stage until the queue is empty, evaluates the stage on the
+// tile, and then waits at a grid barrier.  Tiles by solve:
+//   - mixed 2D (BC 1-3): 32 x 16 rectangles, the single-pass 2D stage tile
+//     (kern_wide2d.cuh: same bits as the single-solve 2D kernel);
+//   - mixed 1D (BC 1-3): segments of 1024 points staged in shared memory,
+//     D formed there (kern_seg1d.cuh: same bits as the gather kernels);
+//   - everything else: TILE consecutive points in gather form
+//     (kern_gather.cuh), 2SHOC in two phases (below).  The barrier spins
 // with a bounded clock budget; if it runs out, the kernel records
 // NLSE_ERR_TIMEOUT in an error word and every CTA returns.  Solves that have
 // finished their step count skip their tiles, so solves of different
@@ -26,6 +31,8 @@
 
 #include "../../include/nlse_gb300.h"
 #include "kern_gather.cuh"
+#include "kern_seg1d.cuh"
+#include "kern_wide2d.cuh"
 #include "nlse_launch.h"
 
 using namespace nlse;
@@ -34,6 +41,16 @@ namespace {
 
 constexpr int TILE = 1024;
 constexpr int BT = 256;  // threads per CTA
+constexpr int W2_TY = 16;  // height of the 2D rectangles
+static_assert(BT == wide2d::NT && BT == seg1d::NT, "tile functions take 256 threads");
+
+// tile kinds
+enum { K_LINEAR = 0, K_SEG1D = 1, K_RECT2D = 2 };
+
+// shared memory of the mixed class's segment and rectangle tiles
+constexpr size_t SMEM_TILE = sizeof(seg1d::Smem) > sizeof(wide2d::Smem<W2_TY>)
+                                 ? sizeof(seg1d::Smem)
+                                 : sizeof(wide2d::Smem<W2_TY>);
 
 struct BSolve {
   Geom g;
@@ -48,9 +65,25 @@ struct BSolve {
 
 struct BTile {
   int solve;
-  int pad;
+  int kind;         // K_LINEAR: start = first point; K_SEG1D / K_RECT2D: start = tile index
   long long start;
 };
+
+// the kind of tile a solve is cut into
+static int tile_kind(const BSolve& d) {
+  if (d.prec != NLSE_PREC_MIXED || d.bc == 4) return K_LINEAR;
+  if (d.g.ndim == 1) return K_SEG1D;
+  if (d.g.ndim == 2) return K_RECT2D;
+  return K_LINEAR;
+}
+
+static long long tile_count(const BSolve& d) {
+  switch (tile_kind(d)) {
+    case K_SEG1D: return seg1d::segments(d.g.n);
+    case K_RECT2D: return wide2d::tiles(d.g, W2_TY);
+    default: return (d.g.n + TILE - 1) / TILE;
+  }
+}
 
 // ---------------------------------------------------------------- device --
 // Per RK4 stage a 2SHOC solve runs two phases: D at every point into dsc
@@ -153,6 +186,60 @@ __device__ __noinline__ void ftile_mixed(const BSolve& s, int stage, int par, lo
   }
 }
 
+// mixed 1D segment t (single pass)
+template <int METHOD, int BC>
+__device__ __noinline__ void seg_mixed(const BSolve& s, int stage, int par, long long t,
+                                       void* smem) {
+  const MixedIO io = mixed_io(s, stage, par);
+  const seg1d::IO sio{io.hi_in, io.lo_in, io.d_in, io.V, io.K, io.d_out, io.hi_out, io.lo_out};
+  seg1d::segment<METHOD, BC>(s.g, s.cf, sio, stage, t, *reinterpret_cast<seg1d::Smem*>(smem));
+}
+
+// mixed 2D rectangle t (single pass)
+template <int METHOD, int BC, int STAGE>
+__device__ __noinline__ void rect_mixed(const BSolve& s, int par, long long t, void* smem) {
+  const MixedIO io = mixed_io(s, STAGE, par);
+  wide2d::Args A;
+  A.a = MixedStageArgs{io.hi_in, io.lo_in, io.d_in, io.V,    io.K,   io.d_out,
+                       io.hi_out, io.lo_out, nullptr, nullptr, nullptr};
+  A.c = s.cf;
+  const int sx = wide2d::shift(s.g.M, wide2d::TX), sy = wide2d::shift(s.g.N, W2_TY);
+  const int nbx = (s.g.M + sx + wide2d::TX - 1) / wide2d::TX;
+  wide2d::tile<METHOD, BC, STAGE, W2_TY>(s.g, A, (int)(t % nbx), (int)(t / nbx), sx, sy,
+                                         *reinterpret_cast<wide2d::Smem<W2_TY>*>(smem));
+}
+
+template <int METHOD, int BC>
+__device__ __forceinline__ void rect_by_stage(const BSolve& s, int stage, int par, long long t,
+                                              void* smem) {
+  switch (stage) {
+    case 1: rect_mixed<METHOD, BC, 1>(s, par, t, smem); break;
+    case 2: rect_mixed<METHOD, BC, 2>(s, par, t, smem); break;
+    case 3: rect_mixed<METHOD, BC, 3>(s, par, t, smem); break;
+    default: rect_mixed<METHOD, BC, 4>(s, par, t, smem); break;
+  }
+}
+
+// segment / rectangle tiles of the mixed class (BC 1-3)
+template <int METHOD>
+__device__ void staged_tile(const BSolve& s, int kind, int stage, int par, long long t,
+                            void* smem) {
+  switch (s.bc) {
+    case 1:
+      if (kind == K_SEG1D) seg_mixed<METHOD, 1>(s, stage, par, t, smem);
+      else rect_by_stage<METHOD, 1>(s, stage, par, t, smem);
+      break;
+    case 2:
+      if (kind == K_SEG1D) seg_mixed<METHOD, 2>(s, stage, par, t, smem);
+      else rect_by_stage<METHOD, 2>(s, stage, par, t, smem);
+      break;
+    default:
+      if (kind == K_SEG1D) seg_mixed<METHOD, 3>(s, stage, par, t, smem);
+      else rect_by_stage<METHOD, 3>(s, stage, par, t, smem);
+      break;
+  }
+}
+
 // phase 0: D (2SHOC solves), phase 1: F + update
 template <int CLS, int DIM, int METHOD, int BC>
 __device__ __forceinline__ void tile_one(const BSolve& s, int ph, int stage, int par, long long p0,
@@ -243,6 +330,7 @@ __global__ void __launch_bounds__(BT, CLS == NLSE_PREC_MIXED ? 4 : 3) batch_kern
                                                       long long budget) {
   __shared__ BSolve s;
   __shared__ int s_t;
+  __shared__ __align__(16) unsigned char smem[CLS == NLSE_PREC_MIXED ? SMEM_TILE : 16];
   for (int step = 0; step < steps; ++step) {
     for (int stage = 1; stage <= 4; ++stage) {
       for (int ph = ntiles_d > 0 ? 0 : 1; ph < 2; ++ph) {
@@ -263,9 +351,18 @@ __global__ void __launch_bounds__(BT, CLS == NLSE_PREC_MIXED ? 4 : 3) batch_kern
           }
           __syncthreads();
           if (step < s.steps_left) {
+            const int par = s.cur ^ (step & 1);
+            if constexpr (CLS == NLSE_PREC_MIXED) {
+              if (tl.kind != K_LINEAR) {  // single pass: phase 1 only
+                if (s.method == 1) staged_tile<1>(s, tl.kind, stage, par, tl.start, smem);
+                else staged_tile<2>(s, tl.kind, stage, par, tl.start, smem);
+                __syncthreads();
+                continue;
+              }
+            }
             long long p1 = tl.start + TILE;
             if (p1 > s.g.n) p1 = s.g.n;
-            process_tile<CLS>(s, ph, stage, s.cur ^ (step & 1), tl.start, p1);
+            process_tile<CLS>(s, ph, stage, par, tl.start, p1);
           }
           __syncthreads();
         }
@@ -541,17 +638,19 @@ extern "C" int nlse_batch_run(nlse_batch* b, int max_steps) {
   int err = 0;
   BTRY(cudaMemcpy(&err, b->d_err, sizeof(int), cudaMemcpyDeviceToHost));
   if (err) return nlse::set_error(err, "a previous batch launch gave up waiting at a grid barrier");
-  // per class: the solves that still run, 2SHOC first; steps = longest advance
+  // per class: the solves that still run, those with a D phase (2SHOC in
+  // gather form) first; steps = longest advance
   std::vector<int> which[2];
   long long ntiles[2] = {0, 0}, ntiles_d[2] = {0, 0};
   int steps[2] = {0, 0};
-  for (int pass = 0; pass < 2; ++pass)  // 2SHOC solves, then CD solves
+  for (int pass = 0; pass < 2; ++pass)  // D-phase solves, then the others
     for (size_t t = 0; t < b->slots.size(); ++t) {
       Slot& S = b->slots[t];
-      if (!S.used || S.d.steps_left <= 0 || (S.d.method == 2) != (pass == 0)) continue;
+      const bool dphase = S.d.method == 2 && tile_kind(S.d) == K_LINEAR;
+      if (!S.used || S.d.steps_left <= 0 || dphase != (pass == 0)) continue;
       const int c = S.d.prec == NLSE_PREC_DOUBLE ? 0 : 1;
       which[c].push_back((int)t);
-      const long long nt = (S.d.g.n + TILE - 1) / TILE;
+      const long long nt = tile_count(S.d);
       ntiles[c] += nt;
       if (pass == 0) ntiles_d[c] += nt;
       long long adv = S.d.steps_left < max_steps ? S.d.steps_left : max_steps;
@@ -584,11 +683,12 @@ extern "C" int nlse_batch_run(nlse_batch* b, int max_steps) {
     for (int id : which[c]) {
       Slot& S = b->slots[id];
       b->h_solves[nsolves] = S.d;
-      const long long nt = (S.d.g.n + TILE - 1) / TILE;
+      const int kind = tile_kind(S.d);
+      const long long nt = tile_count(S.d);
       for (long long q = 0; q < nt; ++q) {
         b->h_tiles[tt].solve = nsolves;
-        b->h_tiles[tt].pad = 0;
-        b->h_tiles[tt].start = q * TILE;
+        b->h_tiles[tt].kind = kind;
+        b->h_tiles[tt].start = kind == K_LINEAR ? q * TILE : q;
         ++tt;
       }
       ++nsolves;

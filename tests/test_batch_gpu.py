@@ -156,10 +156,11 @@ def test_uneven_config4_sample(gpu_lib):
 
 
 def test_mixed_batch_equals_single_solver(gpu_lib, cases):
-    # 1D/2D: the batch's two-phase stage (D into scratch, then F) and the
-    # single-solve gather kernels evaluate the same expressions: same bits
-    # (the 2D single-pass kernel takes the wide form and is compared with
-    # the FP64 oracle instead)
+    # 1D/2D: the batch evaluates every point with the same per-point
+    # expressions as the single-solve path -- 1D segments and one-sided 1D
+    # ends as the gather kernels (D staged in shared memory, or in scratch),
+    # 2D rectangles as the single-pass 2D kernel (wide form with ghosts)
+    # -- so the results are the same bits
     import nlsemagic_gb300 as ng
     steps = 17
     b = ng.Batch(1 << 28)
@@ -169,7 +170,42 @@ def test_mixed_batch_equals_single_solver(gpu_lib, cases):
     b.run(steps)
     for c, sl in zip(picked, slots):
         one = ng.take_steps(c["U"], c["V"], c["s"], c["a"], c["h2"], c["BC"], steps, c["k"],
-                            method=c["method"], precision=ng.PREC_MIXED,
-                            flags=ng.FLAG_MSD_GUARD | ng.FLAG_GATHER)
+                            method=c["method"], precision=ng.PREC_MIXED)
         assert bits_equal(b.download(sl), one)
+        if c["U"].ndim == 1:  # the gather form too
+            gat = ng.take_steps(c["U"], c["V"], c["s"], c["a"], c["h2"], c["BC"], steps, c["k"],
+                                method=c["method"], precision=ng.PREC_MIXED,
+                                flags=ng.FLAG_MSD_GUARD | ng.FLAG_GATHER)
+            assert bits_equal(b.download(sl), gat)
+    b.close()
+
+
+@pytest.mark.parametrize("method", [1, 2])
+@pytest.mark.parametrize("BC", [1, 2, 3])
+def test_mixed_batch_tile_edges(gpu_lib, method, BC):
+    # sizes on every residue the batch's tiles treat differently: 1D
+    # segments of 1024 (n = 1024 m + 1 shifts them by one point, n = 1024 m),
+    # 2D rectangles of 32 x 16 (sides 32 m + 1, 16 m + 1, 32 m, thin grids);
+    # each result is the single solver's, bit for bit
+    import nlsemagic_gb300 as ng
+    shapes = [(1025,), (2048,), (2049,), (3,), (1023,), (33, 17), (64, 48), (3, 97), (97, 3),
+              (65, 49), (40, 33)]
+    b = ng.Batch(1 << 28)
+    picked, slots = [], []
+    for t, shape in enumerate(shapes):
+        c = smooth_case(len(shape), shape[0], method, BC, seed=500 + t)
+        if len(shape) == 2:  # a non-square grid
+            c2 = smooth_case(2, max(shape), method, BC, seed=600 + t)
+            c["U"] = np.ascontiguousarray(c2["U"][:shape[0], :shape[1]])
+            c["V"] = np.ascontiguousarray(c2["V"][:shape[0], :shape[1]])
+        picked.append(c)
+        slots.append(b.add(c["U"], c["V"], c["s"], c["a"], c["h2"], c["BC"], 9, c["k"],
+                           c["method"], ng.PREC_MIXED))
+    b.run(9)
+    for c, sl in zip(picked, slots):
+        one = ng.take_steps(c["U"], c["V"], c["s"], c["a"], c["h2"], c["BC"], 9, c["k"],
+                            method=c["method"], precision=ng.PREC_MIXED)
+        got = b.download(sl)
+        assert np.all(np.isfinite(got))
+        assert bits_equal(got, one), c["U"].shape
     b.close()
