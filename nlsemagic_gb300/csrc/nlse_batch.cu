@@ -41,7 +41,7 @@ namespace {
 
 constexpr int TILE = 1024;
 constexpr int BT = 256;  // threads per CTA
-constexpr int W2_TY = 16;  // height of the 2D rectangles
+constexpr int W2_TY = 32;  // height of the 2D rectangles
 static_assert(BT == wide2d::NT && BT == seg1d::NT, "tile functions take 256 threads");
 
 // tile kinds
@@ -321,49 +321,73 @@ __device__ bool grid_barrier(BarrierState* bar, int* err, long long budget) {
 }
 
 // One launch per precision class.  tiles[0, ntiles_d) are the tiles of the
-// 2SHOC solves (phase 0 runs over them), tiles[0, ntiles) all tiles.
-template <int CLS>
-__global__ void __launch_bounds__(BT, CLS == NLSE_PREC_MIXED ? 4 : 3) batch_kernel(const BSolve* __restrict__ solves,
+// 2SHOC solves in gather form (phase 0 runs over them), tiles[0, ntiles) all
+// tiles.  STAGED: every tile is a segment or a rectangle (mixed class).
+// Resident CTAs per SM the kernels are compiled for: the general kernels
+// at 3 (FP64) and 4 (mixed: the gather paths fit 64 registers), and the
+// mixed kernel for runs whose solves all take segment or rectangle tiles at
+// 6 (40 registers; latency of the per-tile barriers hidden by more CTAs:
+// 20.5 against 15.7 Gpt-steps/s on the uneven 512-solve batch).
+template <int CLS, bool STAGED>
+constexpr int batch_min_blocks() {
+  return CLS == NLSE_PREC_MIXED ? (STAGED ? 6 : 4) : 3;
+}
+
+template <int CLS, bool STAGED>
+__global__ void __launch_bounds__(BT, batch_min_blocks<CLS, STAGED>()) batch_kernel(const BSolve* __restrict__ solves,
                                                       const BTile* __restrict__ tiles, int ntiles,
                                                       int ntiles_d, int steps, unsigned* qctr,
                                                       BarrierState* bar, int* err,
                                                       long long budget) {
   __shared__ BSolve s;
-  __shared__ int s_t;
+  __shared__ int s_solve;      // the solve whose descriptor s holds (-1: none)
+  __shared__ BTile s_tile[2];  // this tile and the next one claimed (solve -1: queue empty)
   __shared__ __align__(16) unsigned char smem[CLS == NLSE_PREC_MIXED ? SMEM_TILE : 16];
+  if (threadIdx.x == 0) s_solve = -1;
   for (int step = 0; step < steps; ++step) {
     for (int stage = 1; stage <= 4; ++stage) {
       for (int ph = ntiles_d > 0 ? 0 : 1; ph < 2; ++ph) {
         const int pass = (step * 4 + stage - 1) * 2 + ph;
         const int nt = ph == 0 ? ntiles_d : ntiles;
-        while (true) {
-          if (threadIdx.x == 0) s_t = (int)atomicAdd(&qctr[pass], 1u);
-          __syncthreads();
-          const int t = s_t;
-          if (t >= nt) break;
-          const BTile tl = tiles[t];
-          // cooperative copy of the solve descriptor into shared memory
-          {
+        if (threadIdx.x == 0) {
+          const int t = (int)atomicAdd(&qctr[pass], 1u);
+          s_tile[0] = t < nt ? tiles[t] : BTile{-1, 0, 0};
+        }
+        __syncthreads();
+        for (int it = 0;; ++it) {
+          const BTile tl = s_tile[it & 1];
+          if (tl.solve < 0) break;
+          // claim the next tile now; its record is stored when this one is done
+          unsigned nx = 0;
+          if (threadIdx.x == 0) nx = atomicAdd(&qctr[pass], 1u);
+          if (tl.solve != s_solve) {
+            __syncthreads();  // every thread has compared s_solve
             const int* src = reinterpret_cast<const int*>(&solves[tl.solve]);
             int* dst = reinterpret_cast<int*>(&s);
             for (int w = threadIdx.x; w < (int)(sizeof(BSolve) / sizeof(int)); w += blockDim.x)
               dst[w] = src[w];
+            if (threadIdx.x == 0) s_solve = tl.solve;
+            __syncthreads();
           }
-          __syncthreads();
           if (step < s.steps_left) {
             const int par = s.cur ^ (step & 1);
+            bool done = false;
             if constexpr (CLS == NLSE_PREC_MIXED) {
               if (tl.kind != K_LINEAR) {  // single pass: phase 1 only
                 if (s.method == 1) staged_tile<1>(s, tl.kind, stage, par, tl.start, smem);
                 else staged_tile<2>(s, tl.kind, stage, par, tl.start, smem);
-                __syncthreads();
-                continue;
+                done = true;
               }
             }
-            long long p1 = tl.start + TILE;
-            if (p1 > s.g.n) p1 = s.g.n;
-            process_tile<CLS>(s, ph, stage, par, tl.start, p1);
+            if constexpr (!STAGED) {
+              if (!done) {
+                long long p1 = tl.start + TILE;
+                if (p1 > s.g.n) p1 = s.g.n;
+                process_tile<CLS>(s, ph, stage, par, tl.start, p1);
+              }
+            }
           }
+          if (threadIdx.x == 0) s_tile[(it + 1) & 1] = (int)nx < nt ? tiles[nx] : BTile{-1, 0, 0};
           __syncthreads();
         }
         if (!grid_barrier(bar, err, budget)) return;
@@ -422,7 +446,7 @@ struct nlse_batch {
   // staging for transfers (planar doubles)
   double* stage = nullptr;
   size_t stage_cap = 0;
-  int max_blocks[2] = {0, 0};  // per class: FP64, mixed
+  int max_blocks[3] = {0, 0, 0};  // FP64, mixed, mixed with staged tiles only
   int last_launches = 0;
 };
 
@@ -529,14 +553,19 @@ extern "C" int nlse_batch_create(long long pool_bytes, int max_solves, nlse_batc
   }
   cudaMemsetAsync(b->d_bar, 0, sizeof(BarrierState), b->stream);
   cudaMemsetAsync(b->d_err, 0, sizeof(int), b->stream);
-  int sms = 0, per64 = 0, permx = 0;
+  int sms = 0, per64 = 0, permx = 0, perst = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per64, batch_kernel<NLSE_PREC_DOUBLE>, BT, 0);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&permx, batch_kernel<NLSE_PREC_MIXED>, BT, 0);
-  if (per64 < 1 || permx < 1)
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per64, batch_kernel<NLSE_PREC_DOUBLE, false>,
+                                                BT, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&permx, batch_kernel<NLSE_PREC_MIXED, false>,
+                                                BT, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perst, batch_kernel<NLSE_PREC_MIXED, true>,
+                                                BT, 0);
+  if (per64 < 1 || permx < 1 || perst < 1)
     return cleanup(nlse::set_error(NLSE_ERR_CUDA, "batch kernel cannot be resident"));
   b->max_blocks[0] = sms * per64;
   b->max_blocks[1] = sms * permx;
+  b->max_blocks[2] = sms * perst;
   (void)rc;
   *out = b;
   return NLSE_OK;
@@ -707,14 +736,17 @@ extern "C" int nlse_batch_run(nlse_batch* b, int max_steps) {
     const size_t np = (size_t)steps[c] * 8;
     BTRY(cudaMemsetAsync(b->d_qctr, 0, sizeof(unsigned) * np, b->stream));
     BTRY(cudaMemsetAsync(b->d_bar, 0, sizeof(BarrierState), b->stream));
-    int blocks = b->max_blocks[c];
+    bool staged = c == 1;  // every solve of the class in segment / rectangle tiles
+    for (int id : which[c]) staged = staged && tile_kind(b->slots[id].d) != K_LINEAR;
+    int blocks = b->max_blocks[staged ? 2 : c];
     if ((long long)blocks > ntiles[c]) blocks = (int)ntiles[c];
     const BTile* tiles = b->d_tiles + first;
     int nt_i = (int)ntiles[c], ntd_i = (int)ntiles_d[c], st_i = steps[c];
     void* args[] = {(void*)&b->d_solves, (void*)&tiles, &nt_i, &ntd_i, &st_i,
                     (void*)&b->d_qctr, (void*)&b->d_bar, (void*)&b->d_err, &budget};
-    const void* kern = c == 0 ? (const void*)batch_kernel<NLSE_PREC_DOUBLE>
-                              : (const void*)batch_kernel<NLSE_PREC_MIXED>;
+    const void* kern = c == 0   ? (const void*)batch_kernel<NLSE_PREC_DOUBLE, false>
+                       : staged ? (const void*)batch_kernel<NLSE_PREC_MIXED, true>
+                                : (const void*)batch_kernel<NLSE_PREC_MIXED, false>;
     BTRY(cudaLaunchCooperativeKernel(kern, dim3(blocks), dim3(BT), args, 0, b->stream));
     ++b->last_launches;
     first += ntiles[c];
