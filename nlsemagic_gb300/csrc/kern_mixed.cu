@@ -2,6 +2,7 @@
 #include "kern_gather.cuh"
 #include "kern_tiled.cuh"
 #include "kern_wide.cuh"
+#include "kern_seg1d.cuh"
 #include "kern_wide2d.cuh"
 #include "nlse_launch.h"
 
@@ -19,6 +20,9 @@ int g_tile_order = 1;
 int g_z2 = 1;
 // 2D grids (BC 1-3): one single-pass stage kernel per stage (kern_wide2d.cuh)
 int g_wide2d = 1;
+// 1D grids (BC 1-3) above the single-block size: one staged-segment launch
+// per stage (kern_seg1d.cuh), same bits as the gather kernels
+int g_seg1d = 1;
 }
 namespace wide2d {
 int g_ty = 0;
@@ -29,6 +33,8 @@ static cudaError_t launch_one(const Geom& g, const Consts<float>& c, const Mixed
                               int stage, cudaStream_t st, int kernel_kind) {
   if (DIM == 2 && kernel_kind == KERNEL_TILED && BC != 4 && wide::g_wide2d)
     return wide2d::launch<METHOD, BC == 4 ? 1 : BC>(g, a, c, stage, st, wide::g_pdl != 0);
+  if (DIM == 1 && kernel_kind == KERNEL_TILED && BC != 4 && wide::g_seg1d)
+    return seg1d::launch<METHOD, BC == 4 ? 1 : BC>(g, a, c, stage, st, wide::g_pdl != 0);
   if (kernel_kind == KERNEL_TILED && tiled_supported(g, DIM) && DIM == 3 && BC != 4) {
     tiled::MixedPol::Args A{a, c, stage, tiled::error_word()};
     return wide::launch<METHOD, BC == 4 ? 1 : BC>(g, A, st);
@@ -70,6 +76,7 @@ static bool wide_path(const Geom& g, int BC, int kernel_kind) {
 
 int mixed_stage_launches(const Geom& g, int method, int BC, int kernel_kind) {
   if (g.ndim == 2 && kernel_kind == KERNEL_TILED && BC != 4 && wide::g_wide2d) return 1;
+  if (g.ndim == 1 && kernel_kind == KERNEL_TILED && BC != 4 && wide::g_seg1d) return 1;
   if (!wide_path(g, BC, kernel_kind)) return method == 2 ? 2 : 1;  // (D,) F
   return method == 2 ? 3 : 2;  // (ghosts,) interior, faces
 }

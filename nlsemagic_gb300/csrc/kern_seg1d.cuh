@@ -13,15 +13,21 @@
 #pragma once
 
 #include "kern_gather.cuh"
+#include "nlse_launch.h"
+#include "nlse_pdl.cuh"
 
 namespace nlse {
 namespace seg1d {
 
-constexpr int SEG = 1024, HALO = 2, NT = 256;
+constexpr int HALO = 2, NT = 256;
 
-__host__ __device__ inline int shift(long long n) { return (n - 1) % SEG == 0 ? 1 : 0; }
+template <int SEG>
+__host__ __device__ inline int shift(long long n) {
+  return (n - 1) % SEG == 0 ? 1 : 0;
+}
+template <int SEG>
 __host__ __device__ inline long long segments(long long n) {
-  return (n + shift(n) + SEG - 1) / SEG;
+  return (n + shift<SEG>(n) + SEG - 1) / SEG;
 }
 
 struct IO {
@@ -32,6 +38,7 @@ struct IO {
 
 // Shared memory of one segment: the staged input (hi, E) and D on
 // [x0-1, x0+SEG].
+template <int SEG>
 struct Smem {
   float2 sh[SEG + 2 * HALO], se[SEG + 2 * HALO];
   float2 sd[SEG + 2];
@@ -39,16 +46,17 @@ struct Smem {
 
 // Segment t of a stage, by the NT threads (one-dimensional block) of the
 // calling CTA, in the shared memory it provides.
-template <int METHOD, int BC>
+template <int METHOD, int BC, int SEG>
 __device__ __forceinline__ void segment(const Geom& g, const Consts<float>& c, const IO& io,
-                                        int stage, long long t, Smem& sm) {
+                                        int stage, long long t, Smem<SEG>& sm) {
+  static_assert(SEG % NT == 0, "whole points per thread");
   static_assert(BC >= 1 && BC <= 3, "one-sided ends take the gather kernels");
   typedef mixed::HE HE;
   float2* sh = sm.sh;
   float2* se = sm.se;
   float2* sd = sm.sd;
   const int tid = (int)threadIdx.x;
-  const int n = (int)g.n, x0 = (int)t * SEG - shift(n);  // n < 2^31 (validated)
+  const int n = (int)g.n, x0 = (int)t * SEG - shift<SEG>(n);  // n < 2^31 (validated)
   const float2* E = stage == 1 ? io.lo_in : io.e_in;
   for (int i = tid; i < SEG + 2 * HALO; i += NT) {
     const int x = x0 - HALO + i;
@@ -111,6 +119,26 @@ __device__ __forceinline__ void segment(const Geom& g, const Consts<float>& c, c
     mixed::update(c, stage, x, T, io.hi_in, io.lo_in, io.e_in, io.K, io.e_out, io.hi_out,
                   io.lo_out);
   }
+}
+
+// Single-solve stage kernel: one CTA per segment of 256 points (one point
+// per thread), launched with PDL like the other stage kernels.
+constexpr int SOLO_SEG = 256;
+
+template <int METHOD, int BC>
+__global__ void __launch_bounds__(NT) stage1d(Geom g, Consts<float> c, IO io, int stage) {
+  __shared__ Smem<SOLO_SEG> sm;
+  pdl_trigger();  // the next kernel may launch; it waits for this one
+  pdl_wait();     // the previous kernel's output
+  segment<METHOD, BC, SOLO_SEG>(g, c, io, stage, blockIdx.x, sm);
+}
+
+template <int METHOD, int BC>
+cudaError_t launch(const Geom& g, const MixedStageArgs& a, const Consts<float>& c, int stage,
+                   cudaStream_t st, bool pdl) {
+  const IO io{a.hi_in, a.lo_in, a.e_in, a.V, a.K, a.e_out, a.hi_out, a.lo_out};
+  return launch_k(stage1d<METHOD, BC>, dim3((unsigned)segments<SOLO_SEG>(g.n)), dim3(NT), 0, st,
+                  pdl, g, c, io, stage);
 }
 
 }  // namespace seg1d

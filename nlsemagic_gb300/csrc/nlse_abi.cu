@@ -60,6 +60,7 @@ extern int g_face_bps;
 extern int g_tile_order;
 extern int g_z2;
 extern int g_wide2d;
+extern int g_seg1d;
 }
 namespace wide2d {
 extern int g_ty;
@@ -82,6 +83,11 @@ extern "C" int nlse_tune_set(const char* key, long long value) {
   if (!strcmp(key, "wide2d")) {
     if (value != 0 && value != 1) return fail(NLSE_ERR_ARG, "wide2d must be 0 or 1");
     nlse::wide::g_wide2d = (int)value;
+    return NLSE_OK;
+  }
+  if (!strcmp(key, "seg1d")) {
+    if (value != 0 && value != 1) return fail(NLSE_ERR_ARG, "seg1d must be 0 or 1");
+    nlse::wide::g_seg1d = (int)value;
     return NLSE_OK;
   }
   if (!strcmp(key, "wide2d.ty")) {
@@ -135,6 +141,10 @@ extern "C" int nlse_tune_get(const char* key, long long* value) {
   }
   if (!strcmp(key, "wide2d.ty")) {
     *value = nlse::wide2d::g_ty;
+    return NLSE_OK;
+  }
+  if (!strcmp(key, "seg1d")) {
+    *value = nlse::wide::g_seg1d;
     return NLSE_OK;
   }
   if (!strcmp(key, "wide.z2")) {

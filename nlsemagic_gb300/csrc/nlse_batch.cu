@@ -48,8 +48,9 @@ static_assert(BT == wide2d::NT && BT == seg1d::NT, "tile functions take 256 thre
 enum { K_LINEAR = 0, K_SEG1D = 1, K_RECT2D = 2 };
 
 // shared memory of the mixed class's segment and rectangle tiles
-constexpr size_t SMEM_TILE = sizeof(seg1d::Smem) > sizeof(wide2d::Smem<W2_TY>)
-                                 ? sizeof(seg1d::Smem)
+constexpr int SEG1 = 1024;  // points of a 1D segment
+constexpr size_t SMEM_TILE = sizeof(seg1d::Smem<SEG1>) > sizeof(wide2d::Smem<W2_TY>)
+                                 ? sizeof(seg1d::Smem<SEG1>)
                                  : sizeof(wide2d::Smem<W2_TY>);
 
 struct BSolve {
@@ -79,7 +80,7 @@ static int tile_kind(const BSolve& d) {
 
 static long long tile_count(const BSolve& d) {
   switch (tile_kind(d)) {
-    case K_SEG1D: return seg1d::segments(d.g.n);
+    case K_SEG1D: return seg1d::segments<SEG1>(d.g.n);
     case K_RECT2D: return wide2d::tiles(d.g, W2_TY);
     default: return (d.g.n + TILE - 1) / TILE;
   }
@@ -192,7 +193,8 @@ __device__ __noinline__ void seg_mixed(const BSolve& s, int stage, int par, long
                                        void* smem) {
   const MixedIO io = mixed_io(s, stage, par);
   const seg1d::IO sio{io.hi_in, io.lo_in, io.d_in, io.V, io.K, io.d_out, io.hi_out, io.lo_out};
-  seg1d::segment<METHOD, BC>(s.g, s.cf, sio, stage, t, *reinterpret_cast<seg1d::Smem*>(smem));
+  seg1d::segment<METHOD, BC, SEG1>(s.g, s.cf, sio, stage, t,
+                                   *reinterpret_cast<seg1d::Smem<SEG1>*>(smem));
 }
 
 // mixed 2D rectangle t (single pass)

@@ -13,6 +13,7 @@ namespace nlse {
 namespace wide {
 extern int g_pdl;     // stage kernels launched with PDL (1) or in plain stream order (0)
 extern int g_wide2d;  // 2D grids: single-pass stage kernels (1) or gather form (0)
+extern int g_seg1d;   // mixed 1D grids: staged-segment stage kernel (1) or gather form (0)
 }
 namespace wide2d {
 extern int g_ty;  // 2D stage kernels' tile height: 0 = by grid size, else 8, 16 or 32
