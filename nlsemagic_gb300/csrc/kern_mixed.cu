@@ -33,7 +33,11 @@ static cudaError_t launch_one(const Geom& g, const Consts<float>& c, const Mixed
                               int stage, cudaStream_t st, int kernel_kind) {
   if (DIM == 2 && kernel_kind == KERNEL_TILED && BC != 4 && wide::g_wide2d)
     return wide2d::launch<METHOD, BC == 4 ? 1 : BC>(g, a, c, stage, st, wide::g_pdl != 0);
-  if (DIM == 1 && kernel_kind == KERNEL_TILED && BC != 4 && wide::g_seg1d)
+  // 1D: 2SHOC always (one launch instead of D then F: 1.2-1.7x); CD, one
+  // gather launch already, below 2^22 points (1.1x at 2^20 points, 0.8x at
+  // 2^24 where the gather kernel keeps more loads in flight)
+  if (DIM == 1 && kernel_kind == KERNEL_TILED && BC != 4 && wide::g_seg1d &&
+      (METHOD == 2 || g.n < (1LL << 22)))
     return seg1d::launch<METHOD, BC == 4 ? 1 : BC>(g, a, c, stage, st, wide::g_pdl != 0);
   if (kernel_kind == KERNEL_TILED && tiled_supported(g, DIM) && DIM == 3 && BC != 4) {
     tiled::MixedPol::Args A{a, c, stage, tiled::error_word()};

@@ -135,7 +135,10 @@ def vortex_rings_3d(seed=1002, n=320, h=0.3, omega=0.02, nrings=4, steps=500, me
 
 def sech_or_tanh(x, s):
     """Bright soliton sech(x) for s = +1, dark soliton tanh(x) for s = -1."""
-    return 1.0 / np.cosh(x) if s > 0 else np.tanh(x)
+    if s > 0:
+        with np.errstate(over="ignore"):  # cosh overflows far out: sech -> 0 there
+            return 1.0 / np.cosh(x)
+    return np.tanh(x)
 
 
 @dataclass
