@@ -500,6 +500,44 @@ def run_batched(args):
             "speedup": v_batch / v_seq}
 
 
+def run_configs(args):
+    """The reference's CPU-runnable case and its 2D case, through resident
+    solvers (graph-captured chunks), in every precision class: configuration
+    1 (1D CD grey soliton, 1024 points, 1000 steps) and configuration 2 (2D
+    2SHOC dark vortices, 512^2 unless --grid2d, 2000 steps unless
+    --config2-steps).  Gpt-steps/s per class, timed after a warm-up run that
+    captures the graphs, and the FP32 / mixed results' relative L2 distance
+    to the FP64 result."""
+    import nlsemagic_gb300 as ng
+    from nlsemagic_gb300 import workloads as W
+    w1 = W.grey_soliton_1d()
+    w2 = W.dark_vortices_2d(n=args.grid2d, steps=args.config2_steps)
+    out = {}
+    for name, w, steps in (("config1", w1, w1.steps), ("config2", w2, args.config2_steps)):
+        res = {"workload": w.name, "rk4_steps": steps}
+        final = {}
+        for prec, label in ((ng.PREC_DOUBLE, "fp64"), (ng.PREC_MIXED, "mixed"),
+                            (ng.PREC_SINGLE, "fp32")):
+            with ng.Solver(w.U.shape, method=w.method, precision=prec, BC=w.BC, s=w.s, a=w.a,
+                           h2=w.h2, k=w.k) as sv:
+                sv.upload(w.U, w.V)
+                sv.run(min(steps, 16))  # captures the chunk graphs
+                sv.sync()
+                sv.upload(w.U, w.V)
+                t0 = time.perf_counter()
+                sv.run(steps)
+                sv.sync()
+                t = time.perf_counter() - t0
+                final[label] = sv.download()
+                res[label] = {"value": w.U.size * steps / t / 1e9, "unit": UNIT,
+                              "launches_per_step": sv.launches_per_step}
+        for label in ("mixed", "fp32"):
+            res[label]["rel_l2_vs_fp64"] = W.rel_l2(final[label], final["fp64"])
+        out[name] = res
+        log("%s: %s" % (name, json.dumps(res)))
+    return out
+
+
 def fifo_latencies(arrivals, service):
     """Latencies of a single first-come-first-served server with the given
     arrival times and per-request service times."""
@@ -585,8 +623,10 @@ def main():
     ap.add_argument("--pdl", type=int, default=1, choices=[0, 1],
                     help="3D 2SHOC stage kernels: 1 overlap through programmatic dependent "
                          "launch, 0 plain stream order (same bits)")
-    ap.add_argument("--only", choices=["batched", "serving"], default=None,
+    ap.add_argument("--only", choices=["batched", "serving", "configs"], default=None,
                     help="run one auxiliary section alone and print its JSON (for profiling)")
+    ap.add_argument("--grid2d", type=int, default=512, help="side of configuration 2")
+    ap.add_argument("--config2-steps", type=int, default=2000)
     args = ap.parse_args()
     if args.impl == "ours":
         from nlsemagic_gb300 import autotune
@@ -594,7 +634,8 @@ def main():
     if args.only:
         import nlsemagic_gb300 as ng
         ng.load()
-        out = run_batched(args) if args.only == "batched" else run_serving(args)
+        out = {"batched": run_batched, "serving": run_serving,
+               "configs": run_configs}[args.only](args)
         print(json.dumps({"section": args.only, **out}), flush=True)
         return
     from nlsemagic_gb300 import workloads as W
