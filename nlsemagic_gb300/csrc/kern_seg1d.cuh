@@ -13,6 +13,7 @@
 #pragma once
 
 #include "kern_gather.cuh"
+#include "nlse_cpasync.cuh"
 #include "nlse_launch.h"
 #include "nlse_pdl.cuh"
 
@@ -60,14 +61,11 @@ __device__ __forceinline__ void segment(const Geom& g, const Consts<float>& c, c
   const float2* E = stage == 1 ? io.lo_in : io.e_in;
   for (int i = tid; i < SEG + 2 * HALO; i += NT) {
     const int x = x0 - HALO + i;
-    float2 h = make_float2(0.f, 0.f), e = h;
-    if (x >= 0 && x < n) {
-      h = io.hi_in[x];
-      e = E[x];
-    }
-    sh[i] = h;
-    se[i] = e;
+    const bool in = x >= 0 && x < n;
+    cp_async<8>(&sh[i], io.hi_in + (in ? x : 0), in);
+    cp_async<8>(&se[i], E + (in ? x : 0), in);
   }
+  cp_async_wait_all();
   __syncthreads();
   auto Y = [&](int x) -> HE {
     HE r;

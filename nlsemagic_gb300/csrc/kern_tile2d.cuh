@@ -21,6 +21,7 @@
 
 #include "kern_gather.cuh"
 #include "kern_wide2d.cuh"
+#include "nlse_cpasync.cuh"
 #include "nlse_launch.h"
 #include "nlse_pdl.cuh"
 
@@ -40,8 +41,8 @@ __global__ void __launch_bounds__(NT)
   constexpr int H = METHOD == 2 ? 2 : 1;  // staged halo
   constexpr int SX = TX + 2 * H, SY = TY + 2 * H;
   constexpr int DX = METHOD == 2 ? TX + 2 : 1, DY = METHOD == 2 ? TY + 2 : 1;
-  __shared__ C2<R> su[SY][SX];
-  __shared__ C2<R> sd[DY][DX];  // 2SHOC: D on the tile and a 1-cell halo
+  __shared__ __align__(16) C2<R> su[SY][SX];  // cp.async destinations: 8/16-byte aligned
+  __shared__ C2<R> sd[DY][DX];                 // 2SHOC: D on the tile and a 1-cell halo
   pdl_trigger();  // the next kernel may launch; it waits for this one
   pdl_wait();     // the previous kernel's output
   const int M = g.M, N = g.N;
@@ -49,12 +50,20 @@ __global__ void __launch_bounds__(NT)
   const int tid = threadIdx.y * BX + threadIdx.x;
 
   // 1. stage Y
+  constexpr bool ASYNC = wide2d::async_staging<TY>();
   for (int i = tid; i < SY * SX; i += NT) {
     const int cy = i / SX, cx = i - cy * SX, gy = y0 - H + cy, gx = x0 - H + cx;
-    C2<R> u = {0, 0};
-    if (gx >= 0 && gx < M && gy >= 0 && gy < N) u = Yin[(unsigned)gy * M + gx];
-    su[cy][cx] = u;
+    const bool in = gx >= 0 && gx < M && gy >= 0 && gy < N;
+    const unsigned p = in ? (unsigned)gy * M + gx : 0u;
+    if (ASYNC) {
+      cp_async<sizeof(C2<R>)>(&su[cy][cx], Yin + p, in);
+    } else {
+      C2<R> u = {0, 0};
+      if (in) u = Yin[p];
+      su[cy][cx] = u;
+    }
   }
+  if (ASYNC) cp_async_wait_all();
   __syncthreads();
   auto U = [&](int x, int y) -> C2<R> { return su[y - y0 + H][x - x0 + H]; };
   auto Vat = [&](int x, int y) -> R { return V[(unsigned)y * M + x]; };

@@ -1,9 +1,9 @@
 // Mixed-precision 2D stage kernel: one launch per RK4 stage, no scratch.
 //
 // A CTA owns a 32 x TY tile and stages it with a 2-cell halo (hi and E) in
-// shared memory with coalesced row loads.  Interior points take the 2SHOC
-// wide form a/(12 h^2) (16 sum_f (Y_f - Y_0) - sum_2 (Y_2 - Y_0)) (or the CD
-// five-point form) from shared memory, so D is never formed.  Next to a face
+// shared memory.  Interior points take the 2SHOC wide form
+// a/(12 h^2) (16 sum_f (Y_f - Y_0) - sum_2 (Y_2 - Y_0)) (or the CD five-point
+// form) from shared memory, so D is never formed.  Next to a face
 // the wide form is exact once the cell beyond the face point b holds the
 // ghost value G = Y_b + h^2 D_bc(b) - (Y_q - Y_b) - sum_t (Y_t - Y_b) (q =
 // b's inward neighbour, t = b's two in-face neighbours; the 3D kernel's
@@ -25,12 +25,14 @@
 // a face and the face point whose ghost it reads.
 // TY (32, 16 or 8 rows; 4, 2 or 1 per thread) trades the halo's share of
 // the staged cells against the number of CTAs: short tiles keep every SM
-// busy on small grids.
+// busy on small grids.  The tile is staged with cp.async (every copy of a
+// thread in flight at once, no registers on the way).
 // The arithmetic is that of the mixed class (nlse_mixed.cuh): explicit
 // rounding, difference-form sums.
 #pragma once
 
 #include "kern_gather.cuh"
+#include "nlse_cpasync.cuh"
 #include "nlse_launch.h"
 #include "nlse_pdl.cuh"
 
@@ -71,7 +73,15 @@ struct Smem {
 // One tile (bxi, byi) of a stage, by the NT threads of the calling CTA (the
 // stage kernel below, or the batched persistent kernel, nlse_batch.cu), in
 // the shared memory the caller provides.
-template <int METHOD, int BC, int STAGE, int TY>
+// Tile staging by cp.async (ASYNC: 8- and 16-row tiles, the batched
+// launch's 32-row tiles) or through registers (the stage kernel's 32-row
+// tiles, 32 registers a thread: cp.async measured no faster there).
+template <int TY>
+__host__ __device__ constexpr bool async_staging() {
+  return TY <= 16;
+}
+
+template <int METHOD, int BC, int STAGE, int TY, bool ASYNC = async_staging<TY>()>
 __device__ __forceinline__ void tile(const Geom& g, const Args& A, int bxi, int byi, int sx,
                                      int sy, Smem<TY>& sm) {
   constexpr int SY = TY + 2 * HALO, R = TY / BY;
@@ -90,14 +100,20 @@ __device__ __forceinline__ void tile(const Geom& g, const Args& A, int bxi, int 
   // 1. staged tile (and the point-local inputs with it on short tiles)
   for (int i = tid; i < SY * SX; i += NT) {
     const int cy = i / SX, cx = i - cy * SX, gy = y0 - HALO + cy, gx = x0 - HALO + cx;
-    float2 h = make_float2(0.f, 0.f), e = h;
-    if (gx >= 0 && gx < M && gy >= 0 && gy < N) {
-      const unsigned p = (unsigned)gy * M + gx;
-      h = A.a.hi_in[p];
-      e = Ein[p];
+    const bool in = gx >= 0 && gx < M && gy >= 0 && gy < N;
+    const unsigned p = in ? (unsigned)gy * M + gx : 0u;
+    if (ASYNC) {
+      cp_async<8>(&sh[cy][cx], A.a.hi_in + p, in);
+      cp_async<8>(&se[cy][cx], Ein + p, in);
+    } else {
+      float2 h = make_float2(0.f, 0.f), e = h;
+      if (in) {
+        h = A.a.hi_in[p];
+        e = Ein[p];
+      }
+      sh[cy][cx] = h;
+      se[cy][cx] = e;
     }
-    sh[cy][cx] = h;
-    se[cy][cx] = e;
   }
   float vr[R];
   float2 lor[R], kr[R];
@@ -139,6 +155,7 @@ __device__ __forceinline__ void tile(const Geom& g, const Args& A, int bxi, int 
     if (gt && BC != 3) vb = A.a.V[(unsigned)by * M + bx];
     if (gt && BC == 2) vq = A.a.V[(unsigned)(by + dy) * M + bx + dx];
   }
+  if (ASYNC) cp_async_wait_all();
   __syncthreads();
   auto at = [&](int x, int y) -> HE {  // grid coordinates inside the staged tile
     HE r;
@@ -236,11 +253,12 @@ __host__ __device__ inline int tiles(const Geom& g, int ty) {
   return ((g.M + shift(g.M, TX) + TX - 1) / TX) * ((g.N + shift(g.N, ty) + ty - 1) / ty);
 }
 
-// Tile height by grid size (152 SMs): 32 rows from 32 tiles per SM (4096^2
-// and up), 16 rows from 8 tiles per SM, else 8 rows.
+// Tile height by grid size (152 SMs): 16 rows from 8 tiles per SM, else 8
+// rows.  (32-row tiles, staged through registers, measured slower at every
+// size once the 16-row tiles were staged by cp.async: 26.2 against 32.6
+// Gpt-steps/s for 2SHOC at 4096^2; the knob still selects them.)
 inline int pick_ty(const Geom& g) {
   if (g_ty) return g_ty;
-  if (tiles(g, 32) >= 32 * 152) return 32;
   if (tiles(g, 16) >= 8 * 152) return 16;
   return 8;
 }

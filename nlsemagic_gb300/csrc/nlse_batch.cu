@@ -207,8 +207,8 @@ __device__ __noinline__ void rect_mixed(const BSolve& s, int par, long long t, v
   A.c = s.cf;
   const int sx = wide2d::shift(s.g.M, wide2d::TX), sy = wide2d::shift(s.g.N, W2_TY);
   const int nbx = (s.g.M + sx + wide2d::TX - 1) / wide2d::TX;
-  wide2d::tile<METHOD, BC, STAGE, W2_TY>(s.g, A, (int)(t % nbx), (int)(t / nbx), sx, sy,
-                                         *reinterpret_cast<wide2d::Smem<W2_TY>*>(smem));
+  wide2d::tile<METHOD, BC, STAGE, W2_TY, true>(s.g, A, (int)(t % nbx), (int)(t / nbx), sx, sy,
+                                               *reinterpret_cast<wide2d::Smem<W2_TY>*>(smem));
 }
 
 template <int METHOD, int BC>
