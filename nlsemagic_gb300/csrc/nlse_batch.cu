@@ -41,6 +41,9 @@ namespace {
 
 constexpr int TILE = 1024;
 constexpr int BT = 256;  // threads per CTA
+// Tile sizes: 32 x 32 rectangles and 1024-point segments (on the uneven
+// 512-solve batch 23.6 Gpt-steps/s, against 19.4 with 32 x 16 rectangles
+// and 19.5 with those and 512-point segments).
 constexpr int W2_TY = 32;  // height of the 2D rectangles
 static_assert(BT == wide2d::NT && BT == seg1d::NT, "tile functions take 256 threads");
 
