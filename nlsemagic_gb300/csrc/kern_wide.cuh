@@ -495,7 +495,6 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
   const int x = x0 + tx, y = y0 + ty;
   const bool inner = x >= 1 && x <= M - 2 && y >= 1 && y <= N - 2;
   const bool edge = METHOD == 2 && (x0 == 0 || x0 + TX > M - 2 || y0 == 0 || y0 + TY > N - 2);
-  const float2* Ein = STAGE == 1 ? A.a.lo_in : A.a.e_in;
   const float4* GH = A.a.gh;
 
   if ((su32(smem) & 127u) != 0) {  // TMA destinations must be 128-byte aligned

@@ -946,7 +946,7 @@ thread_local VortCache t_vort;
 extern "C" int nlse_vorticity3d(const double* Ur, const double* Ui, const long long* dims,
                                 double lh2, double veps, double* wx, double* wy, double* wz,
                                 double* W) {
-  int M, N, L;
+  int M = 0, N = 0, L = 0;
   int rc = vort_dims(dims, &M, &N, &L);
   if (rc) return rc;
   if (!Ur || !wx || !wy || !wz || !W) return fail(NLSE_ERR_ARG, "NULL array argument");

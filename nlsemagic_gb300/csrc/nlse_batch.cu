@@ -534,7 +534,6 @@ extern "C" int nlse_batch_create(long long pool_bytes, int max_solves, nlse_batc
     return nlse::set_error(NLSE_ERR_ARG, "pool_bytes and max_solves must be > 0");
   *out = nullptr;
   nlse_batch* b = new nlse_batch();
-  int rc = NLSE_OK;
   auto cleanup = [&](int code) {
     nlse_batch_destroy(b);
     return code;
@@ -571,7 +570,6 @@ extern "C" int nlse_batch_create(long long pool_bytes, int max_solves, nlse_batc
   b->max_blocks[0] = sms * per64;
   b->max_blocks[1] = sms * permx;
   b->max_blocks[2] = sms * perst;
-  (void)rc;
   *out = b;
   return NLSE_OK;
 }
