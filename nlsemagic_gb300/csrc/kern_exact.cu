@@ -39,17 +39,24 @@ static cudaError_t launch_one(const Geom& g, const Consts<R>& c, const ExactStag
                   st, wide::g_pdl != 0, g, c, (const C2<R>*)a.Yin, a.Psi, a.V, a.K, a.Yout, stage);
 }
 
-long long exact_dsc_entries(const Geom& g, int method, int BC, int kernel_kind) {
-  if (method != 2) return 0;
-  const bool tiled = kernel_kind == KERNEL_TILED && tiled_supported(g, g.ndim) && BC != 4;
-  return tiled ? 0 : g.n;
+static bool tile2d_path(const Geom& g, int method, int BC, int kernel_kind, bool single) {
+  return g.ndim == 2 && method == 2 && single && kernel_kind == KERNEL_TILED && BC != 4 &&
+         wide::g_wide2d;
 }
 
-int exact_stage_launches(const Geom& g, int method, int BC, int kernel_kind, bool single) {
-  if (g.ndim == 2 && method == 2 && single && kernel_kind == KERNEL_TILED && BC != 4 &&
-      wide::g_wide2d)
-    return 1;
-  return exact_dsc_entries(g, method, BC, kernel_kind) ? 2 : 1;  // (D,) F
+// D scratch: 2SHOC in gather form.  FP32 2D grids on the tile kernel take
+// none; should the knob turn it off later, the gather kernel recomputes D.
+long long exact_dsc_entries(const Geom& g, int method, int BC, int kernel_kind, bool single) {
+  if (method != 2) return 0;
+  const bool tiled = kernel_kind == KERNEL_TILED && tiled_supported(g, g.ndim) && BC != 4;
+  return tiled || tile2d_path(g, method, BC, kernel_kind, single) ? 0 : g.n;
+}
+
+int exact_stage_launches(const Geom& g, int method, int BC, int kernel_kind, bool single,
+                         bool has_dsc) {
+  if (tile2d_path(g, method, BC, kernel_kind, single)) return 1;
+  if (kernel_kind == KERNEL_TILED && tiled_supported(g, g.ndim) && BC != 4) return 1;
+  return method == 2 && has_dsc ? 2 : 1;  // (D,) F
 }
 
 template <typename R, int DIM, int METHOD>

@@ -78,15 +78,20 @@ static bool wide_path(const Geom& g, int BC, int kernel_kind) {
   return kernel_kind == KERNEL_TILED && g.ndim == 3 && tiled_supported(g, 3) && BC != 4;
 }
 
-int mixed_stage_launches(const Geom& g, int method, int BC, int kernel_kind) {
+int mixed_stage_launches(const Geom& g, int method, int BC, int kernel_kind, bool has_dsc) {
   if (g.ndim == 2 && kernel_kind == KERNEL_TILED && BC != 4 && wide::g_wide2d) return 1;
   if (g.ndim == 1 && kernel_kind == KERNEL_TILED && BC != 4 && wide::g_seg1d) return 1;
-  if (!wide_path(g, BC, kernel_kind)) return method == 2 ? 2 : 1;  // (D,) F
+  if (!wide_path(g, BC, kernel_kind)) return method == 2 && has_dsc ? 2 : 1;  // (D,) F
   return method == 2 ? 3 : 2;  // (ghosts,) interior, faces
 }
 
+// D scratch: 2SHOC in gather form (two launches per stage, or the small 1D
+// path).  2D grids on the single-pass kernel take none; should the knob turn
+// that kernel off later, the gather kernel recomputes D instead.
 long long mixed_dsc_entries(const Geom& g, int method, int BC, int kernel_kind) {
-  return method == 2 && !wide_path(g, BC, kernel_kind) ? g.n : 0;
+  if (method != 2 || wide_path(g, BC, kernel_kind)) return 0;
+  if (g.ndim == 2 && kernel_kind == KERNEL_TILED && BC != 4 && wide::g_wide2d) return 0;
+  return g.n;
 }
 
 long long mixed_ghost_entries(const Geom& g, int method, int BC, int kernel_kind) {

@@ -423,7 +423,8 @@ extern "C" int nlse_solver_create(const nlse_problem* p, nlse_solver** out) {
     if (!r) r = dalloc(s, &s->ya, 2 * es * n);
     if (!r) r = dalloc(s, &s->yb, 2 * es * n);
     if (!r) r = dalloc(s, &s->V, es * n);
-    const long long nd = exact_dsc_entries(s->g, p->method, p->bc, s->kernel_kind);
+    const long long nd = exact_dsc_entries(s->g, p->method, p->bc, s->kernel_kind,
+                                           p->precision == NLSE_PREC_SINGLE);
     if (!r && nd) r = dalloc(s, &s->dsc, 2 * es * nd);
   } else {
     for (int t = 0; t < 2 && !r; ++t) {
@@ -649,7 +650,7 @@ extern "C" int nlse_solver_run(nlse_solver* s, long long nsteps) {
   if (nsteps < 0) return fail(NLSE_ERR_ARG, "nsteps must be >= 0");
   CUDA_TRY(cudaSetDevice(s->device));
   if (s->g.ndim == 1 && s->g.n <= g_small1d_max && s->prob.precision != NLSE_PREC_DOUBLE &&
-      nsteps > 0)
+      (s->prob.method == 1 || s->dsc) && nsteps > 0)
     return run_small1d(s, nsteps);
   const int G = s->graph_steps;
   if (G > 0 && nsteps >= G) {
@@ -696,9 +697,10 @@ extern "C" int nlse_solver_launches_per_step(const nlse_solver* s) {
   if (!s) return 0;
   if (s->prob.precision != NLSE_PREC_MIXED)
     return 4 * exact_stage_launches(s->g, s->prob.method, s->prob.bc, s->kernel_kind,
-                                    s->prob.precision == NLSE_PREC_SINGLE);
+                                    s->prob.precision == NLSE_PREC_SINGLE, s->dsc != nullptr);
   // mixed-precision 3D grids on the tiled path: deep-point kernel + shell kernel(s) per stage
-  return 4 * mixed_stage_launches(s->g, s->prob.method, s->prob.bc, s->kernel_kind);
+  return 4 * mixed_stage_launches(s->g, s->prob.method, s->prob.bc, s->kernel_kind,
+                                  s->dsc != nullptr);
 }
 
 extern "C" long long nlse_solver_bytes_for(const nlse_problem* p) {
@@ -709,7 +711,8 @@ extern "C" long long nlse_solver_bytes_for(const nlse_problem* p) {
   long long b = 0;
   if (p->precision == NLSE_PREC_DOUBLE || p->precision == NLSE_PREC_SINGLE) {
     const long long es = p->precision == NLSE_PREC_DOUBLE ? 8 : 4;
-    b = 4 * 2 * es * n + es * n + 2 * es * exact_dsc_entries(g, p->method, p->bc, kind);
+    b = 4 * 2 * es * n + es * n +
+        2 * es * exact_dsc_entries(g, p->method, p->bc, kind, p->precision == NLSE_PREC_SINGLE);
   } else {
     b = 8 * 8 * n + 4 * n + 16 * mixed_ghost_entries(g, p->method, p->bc, kind) +
         8 * mixed_fq_entries(g, p->method, p->bc, kind) +

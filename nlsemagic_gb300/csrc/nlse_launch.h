@@ -60,13 +60,14 @@ cudaError_t launch_small1d_mixed(const Geom& g, int method, int BC, const Consts
                                  float2* db, float2* dc, const float* V, float2* D, int cur,
                                  long long nsteps, cudaStream_t st);
 
-int mixed_stage_launches(const Geom& g, int method, int BC, int kernel_kind);
-int exact_stage_launches(const Geom& g, int method, int BC, int kernel_kind, bool single);
+int mixed_stage_launches(const Geom& g, int method, int BC, int kernel_kind, bool has_dsc);
+int exact_stage_launches(const Geom& g, int method, int BC, int kernel_kind, bool single,
+                         bool has_dsc);
 long long mixed_ghost_entries(const Geom& g, int method, int BC, int kernel_kind);
 long long mixed_fq_entries(const Geom& g, int method, int BC, int kernel_kind);
 // Points of D scratch (ExactStageArgs / MixedStageArgs ::dsc) a 2SHOC stage on
 // the gather path uses (two launches per stage), else 0.
-long long exact_dsc_entries(const Geom& g, int method, int BC, int kernel_kind);
+long long exact_dsc_entries(const Geom& g, int method, int BC, int kernel_kind, bool single);
 long long mixed_dsc_entries(const Geom& g, int method, int BC, int kernel_kind);
 
 // Layout conversions and reductions (kern_util.cu).

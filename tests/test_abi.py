@@ -73,6 +73,27 @@ def test_tuning_knobs_roundtrip_and_validation(lib):
         autotune.set_knob(key, old)
 
 
+def test_single_pass_2d_needs_no_d_scratch(lib):
+    # 2D 2SHOC on the single-pass kernels (mixed, FP32) allocates no D
+    # scratch: 8 bytes a point less than with the gather kernels
+    from nlsemagic_gb300 import autotune
+    shape, n = (300, 200), 300 * 200
+    old = autotune.get_knob("wide2d")
+    try:
+        for prec in (ng.PREC_MIXED, ng.PREC_SINGLE):
+            autotune.set_knob("wide2d", 1)
+            on = ng.Solver.bytes_for(shape, method=2, precision=prec, BC=1)
+            autotune.set_knob("wide2d", 0)
+            off = ng.Solver.bytes_for(shape, method=2, precision=prec, BC=1)
+            assert off - on == 8 * n, (prec, on, off)
+        autotune.set_knob("wide2d", 1)  # FP64 keeps the two-launch form and its scratch
+        a = ng.Solver.bytes_for(shape, method=2, precision=ng.PREC_DOUBLE, BC=1)
+        autotune.set_knob("wide2d", 0)
+        assert ng.Solver.bytes_for(shape, method=2, precision=ng.PREC_DOUBLE, BC=1) == a
+    finally:
+        autotune.set_knob("wide2d", old)
+
+
 def test_autotune_candidates_per_class():
     from nlsemagic_gb300 import autotune
     two = autotune.candidates((256, 256), 3)
