@@ -37,7 +37,7 @@ template <typename R, int METHOD, int BC, int TY>
 __global__ void __launch_bounds__(NT)
     exact2d(Geom g, Consts<R> c, const C2<R>* __restrict__ Yin, C2<R>* Psi,
             const R* __restrict__ V, C2<R>* __restrict__ K, C2<R>* __restrict__ Yout, int stage,
-            int sx, int sy) {
+            int sx, int sy, int nbx) {
   constexpr int H = METHOD == 2 ? 2 : 1;  // staged halo
   constexpr int SX = TX + 2 * H, SY = TY + 2 * H;
   constexpr int DX = METHOD == 2 ? TX + 2 : 1, DY = METHOD == 2 ? TY + 2 : 1;
@@ -46,7 +46,8 @@ __global__ void __launch_bounds__(NT)
   pdl_trigger();  // the next kernel may launch; it waits for this one
   pdl_wait();     // the previous kernel's output
   const int M = g.M, N = g.N;
-  const int x0 = (int)blockIdx.x * TX - sx, y0 = (int)blockIdx.y * TY - sy;
+  // one CTA per tile, tiles numbered x-fastest in a one-dimensional grid
+  const int x0 = (int)(blockIdx.x % nbx) * TX - sx, y0 = (int)(blockIdx.x / nbx) * TY - sy;
   const int tid = threadIdx.y * BX + threadIdx.x;
 
   // 1. stage Y
@@ -132,9 +133,10 @@ template <typename R, int METHOD, int BC, int TY>
 cudaError_t launch_ty(const Geom& g, const Consts<R>& c, const ExactStageArgs<R>& a, int stage,
                       cudaStream_t st, bool pdl) {
   const int sx = wide2d::shift(g.M, TX), sy = wide2d::shift(g.N, TY);
-  const dim3 grid((g.M + sx + TX - 1) / TX, (g.N + sy + TY - 1) / TY), block(BX, BY);
+  const int nbx = (g.M + sx + TX - 1) / TX;
+  const dim3 grid((unsigned)wide2d::tiles(g, TY)), block(BX, BY);
   return launch_k(exact2d<R, METHOD, BC, TY>, grid, block, 0, st, pdl, g, c, a.Yin, a.Psi, a.V,
-                  a.K, a.Yout, stage, sx, sy);
+                  a.K, a.Yout, stage, sx, sy, nbx);
 }
 
 template <typename R, int METHOD, int BC>

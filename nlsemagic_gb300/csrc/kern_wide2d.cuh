@@ -238,13 +238,16 @@ __device__ __forceinline__ void tile(const Geom& g, const Args& A, int bxi, int 
   }
 }
 
+// One CTA per tile, tiles numbered x-fastest in a one-dimensional grid (a
+// tall grid has more tile rows than gridDim.y allows).
 template <int METHOD, int BC, int STAGE, int TY>
 __global__ void __launch_bounds__(NT, min_blocks<METHOD, BC, TY>())
-    stage2d(Geom g, Args A, int sx, int sy) {
+    stage2d(Geom g, Args A, int sx, int sy, int nbx) {
   __shared__ Smem<TY> sm;
   pdl_trigger();  // the next kernel may launch; it waits for this one
   pdl_wait();     // the previous kernel's output
-  tile<METHOD, BC, STAGE, TY>(g, A, (int)blockIdx.x, (int)blockIdx.y, sx, sy, sm);
+  const int t = (int)blockIdx.x;
+  tile<METHOD, BC, STAGE, TY>(g, A, t % nbx, t / nbx, sx, sy, sm);
 }
 
 __host__ __device__ inline int shift(int n, int t) { return (n - 1) % t == 0 ? 1 : 0; }
@@ -267,13 +270,14 @@ template <int METHOD, int BC, int TY>
 cudaError_t launch_ty(const Geom& g, const MixedStageArgs& a, const Consts<float>& c, int stage,
                       cudaStream_t st, bool pdl) {
   const int sx = shift(g.M, TX), sy = shift(g.N, TY);
-  const dim3 grid((g.M + sx + TX - 1) / TX, (g.N + sy + TY - 1) / TY), block(BX, BY);
+  const int nbx = (g.M + sx + TX - 1) / TX;
+  const dim3 grid((unsigned)tiles(g, TY)), block(BX, BY);
   const Args A{a, c};
   switch (stage) {
-    case 1: return launch_k(stage2d<METHOD, BC, 1, TY>, grid, block, 0, st, pdl, g, A, sx, sy);
-    case 2: return launch_k(stage2d<METHOD, BC, 2, TY>, grid, block, 0, st, pdl, g, A, sx, sy);
-    case 3: return launch_k(stage2d<METHOD, BC, 3, TY>, grid, block, 0, st, pdl, g, A, sx, sy);
-    case 4: return launch_k(stage2d<METHOD, BC, 4, TY>, grid, block, 0, st, pdl, g, A, sx, sy);
+    case 1: return launch_k(stage2d<METHOD, BC, 1, TY>, grid, block, 0, st, pdl, g, A, sx, sy, nbx);
+    case 2: return launch_k(stage2d<METHOD, BC, 2, TY>, grid, block, 0, st, pdl, g, A, sx, sy, nbx);
+    case 3: return launch_k(stage2d<METHOD, BC, 3, TY>, grid, block, 0, st, pdl, g, A, sx, sy, nbx);
+    case 4: return launch_k(stage2d<METHOD, BC, 4, TY>, grid, block, 0, st, pdl, g, A, sx, sy, nbx);
   }
   return cudaErrorInvalidValue;
 }

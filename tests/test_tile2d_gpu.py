@@ -73,3 +73,12 @@ def test_tile2d_launches_per_step(gpu_lib):
         with ng.Solver((64, 48), method=2, precision=prec, BC=1, s=-1.0, a=1.0, h2=0.09,
                        k=0.002) as sv:
             assert sv.launches_per_step == want
+
+
+@pytest.mark.parametrize("shape", [(3, 700000), (700000, 3)])
+def test_tile2d_tall_grid(gpu_lib, shape):
+    # more tile rows than a launch's gridDim.y allows: bit-exact all the same
+    U, V = _case(shape, 77)
+    want = oracle.take_steps(U, V, -1.0, 0.9, 0.09, 1, 2, 0.002, method=2, precision=1,
+                             flags=oracle.MSD_GUARD)
+    assert bits_equal(_gpu(U, V, 1, 2, 1, 2, ty=8), want)

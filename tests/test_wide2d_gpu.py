@@ -90,3 +90,16 @@ def test_wide2d_knob_range(gpu_lib):
         autotune.set_knob("wide2d", 2)
     with pytest.raises(Exception):
         autotune.set_knob("wide2d.ty", 4)
+
+
+@pytest.mark.parametrize("shape", [(3, 700000), (700000, 3)])
+def test_wide2d_tall_grid(gpu_lib, shape):
+    # more tile rows than a launch's gridDim.y allows (65535): tiles are
+    # numbered in a one-dimensional grid
+    U, V, h = _field(shape)
+    k = 0.5 * W.linear_stability_k(2, 2, h, 1.0)
+    want = oracle.take_steps(U, V, -1.0, 1.0, h * h, 2, 3, k, method=2, precision=2,
+                             flags=oracle.MSD_GUARD)
+    for ty in (0, 8):
+        got = _gpu(U, V, h, 2, 2, 3, k, ty=ty)
+        assert W.rel_l2(got, want) <= MIXED_TOL
