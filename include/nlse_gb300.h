@@ -280,10 +280,12 @@ int nlse_take_steps_noalloc(const nlse_problem *p, const double *dUr, const doub
  *                  bit for bit (the single-pass kernel takes the wide form).
  *   "wide2d.ty"    tile height of those kernels: 0 (default) by grid size,
  *                  or 8, 16, 32.  Same bits.
- *   "seg1d"        1 (default): mixed-precision 1D grids (BC 1-3) above
+ *   "seg1d"        1 (default): 1D grids (BC 1-3) above
  *                  "small1d.max_points" take the staged-segment stage
- *                  kernel (one launch per stage, 2SHOC's D in shared
- *                  memory); 0: the gather kernels.  Same bits.
+ *                  kernels (one launch per stage, 2SHOC's D in shared
+ *                  memory): 2SHOC in FP32 and mixed at every size, FP64
+ *                  and CD below 2^22 points; 0: the gather kernels.  Same
+ *                  bits.
  * ---------------------------------------------------------------------- */
 int nlse_tune_set(const char *key, long long value);
 int nlse_tune_get(const char *key, long long *value);

@@ -4,17 +4,30 @@
 #include <type_traits>
 
 #include "kern_gather.cuh"
+#include "kern_seg1d.cuh"
 #include "kern_tile2d.cuh"
 #include "kern_tiled.cuh"
 #include "nlse_launch.h"
 
 namespace nlse {
 
+static bool seg1d_exact_path(const Geom& g, int method, int BC, int kernel_kind, bool single) {
+  return g.ndim == 1 && kernel_kind == KERNEL_TILED && BC != 4 && wide::g_seg1d &&
+         ((method == 2 && single) || g.n < (1LL << 22));
+}
+
 template <typename R, int DIM, int METHOD, int BC>
 static cudaError_t launch_one(const Geom& g, const Consts<R>& c, const ExactStageArgs<R>& a,
                               int stage, cudaStream_t st, int kernel_kind) {
   if (kernel_kind == KERNEL_TILED && tiled_supported(g, DIM)) {
     return tiled::launch_exact<R, DIM, METHOD, BC>(g, c, a, stage, st);
+  }
+  // 1D grids: staged segments, one launch per stage.  FP32 2SHOC at every
+  // size (1.4-1.75x the D-scratch form), the rest below 2^22 points (FP64,
+  // bound by FP64 issue, and CD gain nothing on larger grids)
+  if constexpr (DIM == 1 && BC != 4) {
+    if (seg1d_exact_path(g, METHOD, BC, kernel_kind, sizeof(R) == 4))
+      return seg1d::launch_exact<R, METHOD, BC>(g, c, a, stage, st, wide::g_pdl != 0);
   }
   // FP32 2SHOC on 2D grids: the single-pass tile kernel (1.4-1.5x the
   // two-launch D-scratch form).  FP64 stays on the gather kernels, bound by
@@ -55,6 +68,7 @@ long long exact_dsc_entries(const Geom& g, int method, int BC, int kernel_kind, 
 int exact_stage_launches(const Geom& g, int method, int BC, int kernel_kind, bool single,
                          bool has_dsc) {
   if (tile2d_path(g, method, BC, kernel_kind, single)) return 1;
+  if (seg1d_exact_path(g, method, BC, kernel_kind, single)) return 1;
   if (kernel_kind == KERNEL_TILED && tiled_supported(g, g.ndim) && BC != 4) return 1;
   return method == 2 && has_dsc ? 2 : 1;  // (D,) F
 }

@@ -1,7 +1,7 @@
-// Mixed-precision 1D stage on one segment of SEG points: the stage input
-// (hi, E) staged once with a 2-cell halo in shared memory and, for 2SHOC, D
-// formed there on the segment and a 1-cell halo, so a 2SHOC stage takes one
-// pass instead of D into scratch, a grid-wide wait and F.
+// 1D stage on one segment of SEG points: the stage input (mixed: hi, E;
+// exact: Y) staged once with a 2-cell halo in shared memory and, for 2SHOC,
+// D formed there on the segment and a 1-cell halo, so a 2SHOC stage takes
+// one pass instead of D into scratch, a grid-wide wait and F.
 //
 // Segments start at SEG t - s, s = 1 when (n-1) is a multiple of SEG, else 0,
 // so that none starts at 1 or n-1: an end point and its MSD neighbour share a
@@ -119,7 +119,76 @@ __device__ __forceinline__ void segment(const Geom& g, const Consts<float>& c, c
   }
 }
 
-// Single-solve stage kernel: one CTA per segment of 256 points (one point
+// Exact precisions (FP64 / FP32): the same segment, stage input Y (C2<R>)
+// staged with a 2-cell halo, D formed on the segment and a 1-cell halo, by
+// the gather kernels' per-point functions (kern_gather.cuh: exact::d_at,
+// f_int, f_at_d) in the same order; the unit that instantiates it is
+// compiled with -fmad=false, so the results are the reference's bits.
+template <typename R, int SEG>
+struct SmemExact {
+  C2<R> su[SEG + 2 * HALO];
+  C2<R> sd[SEG + 2];
+};
+
+template <typename R, int METHOD, int BC, int SEG>
+__device__ __forceinline__ void segment_exact(const Geom& g, const Consts<R>& c,
+                                              const C2<R>* __restrict__ Yin, C2<R>* Psi,
+                                              const R* __restrict__ V, C2<R>* __restrict__ K,
+                                              C2<R>* __restrict__ Yout, int stage, long long t,
+                                              SmemExact<R, SEG>& sm) {
+  static_assert(BC >= 1 && BC <= 3, "one-sided ends take the gather kernels");
+  static_assert(SEG % NT == 0, "whole points per thread");
+  const int tid = (int)threadIdx.x;
+  const int n = (int)g.n, x0 = (int)t * SEG - shift<SEG>(n);  // n < 2^31 (validated)
+  for (int i = tid; i < SEG + 2 * HALO; i += NT) {
+    const int x = x0 - HALO + i;
+    const bool in = x >= 0 && x < n;
+    cp_async<sizeof(C2<R>)>(&sm.su[i], Yin + (in ? x : 0), in);
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  auto U = [&](int x) { return sm.su[x - x0 + HALO]; };
+  auto dint = [&](int x) { return exact::d_int_1d<R>(c, U(x + 1), U(x), U(x - 1)); };
+  if (METHOD == 2) {
+    for (int i = tid; i < SEG + 2; i += NT) {
+      const int x = x0 - 1 + i;
+      C2<R> d = {0, 0};
+      if (x >= 0 && x < n) {
+        if (x >= 1 && x <= n - 2) {
+          d = dint(x);
+        } else {
+          const int q = x == 0 ? 1 : n - 2;
+          C2<R> dq = {0, 0};
+          if (BC == 2) dq = dint(q);
+          d = exact::d_bnd<R, BC>(c, U(x), V[x], U(q), V[q], dq);
+        }
+      }
+      sm.sd[i] = d;
+    }
+    __syncthreads();
+  }
+  auto D = [&](int x) { return sm.sd[x - x0 + 1]; };
+  auto fint = [&](int x) {  // f_int<R, 1, 1> / f_int_d<R, 1>
+    if (METHOD == 1) return exact::f_cd_1d<R>(c, U(x), V[x], U(x + 1), U(x - 1));
+    return exact::f_2shoc_1d<R>(c, U(x), V[x], D(x), D(x + 1), D(x - 1));
+  };
+  for (int r = 0; r < SEG / NT; ++r) {
+    const int x = x0 + tid + NT * r;
+    if (x < 0 || x >= n) continue;
+    C2<R> T;
+    if (x >= 1 && x <= n - 2) {
+      T = fint(x);
+    } else {
+      const int q = x == 0 ? 1 : n - 2;
+      C2<R> fq = {0, 0};
+      if (BC == 2) fq = fint(q);
+      T = exact::f_bnd<R, BC>(c, U(x), V[x], U(q), fq);
+    }
+    exact::update<R>(c, stage, x, T, Psi, K, Yout);
+  }
+}
+
+// Single-solve stage kernels: one CTA per segment of 256 points (one point
 // per thread), launched with PDL like the other stage kernels.
 constexpr int SOLO_SEG = 256;
 
@@ -137,6 +206,24 @@ cudaError_t launch(const Geom& g, const MixedStageArgs& a, const Consts<float>& 
   const IO io{a.hi_in, a.lo_in, a.e_in, a.V, a.K, a.e_out, a.hi_out, a.lo_out};
   return launch_k(stage1d<METHOD, BC>, dim3((unsigned)segments<SOLO_SEG>(g.n)), dim3(NT), 0, st,
                   pdl, g, c, io, stage);
+}
+
+template <typename R, int METHOD, int BC>
+__global__ void __launch_bounds__(NT)
+    stage1d_exact(Geom g, Consts<R> c, const C2<R>* __restrict__ Yin, C2<R>* Psi,
+                  const R* __restrict__ V, C2<R>* __restrict__ K, C2<R>* __restrict__ Yout,
+                  int stage) {
+  __shared__ __align__(16) SmemExact<R, SOLO_SEG> sm;  // cp.async destinations
+  pdl_trigger();  // the next kernel may launch; it waits for this one
+  pdl_wait();     // the previous kernel's output
+  segment_exact<R, METHOD, BC, SOLO_SEG>(g, c, Yin, Psi, V, K, Yout, stage, blockIdx.x, sm);
+}
+
+template <typename R, int METHOD, int BC>
+cudaError_t launch_exact(const Geom& g, const Consts<R>& c, const ExactStageArgs<R>& a,
+                         int stage, cudaStream_t st, bool pdl) {
+  return launch_k(stage1d_exact<R, METHOD, BC>, dim3((unsigned)segments<SOLO_SEG>(g.n)),
+                  dim3(NT), 0, st, pdl, g, c, a.Yin, a.Psi, a.V, a.K, a.Yout, stage);
 }
 
 }  // namespace seg1d
