@@ -272,8 +272,8 @@ int nlse_take_steps_noalloc(const nlse_problem *p, const double *dUr, const doub
  *                  tiles: 1 (default) chunk by chunk (neighbouring tiles
  *                  share their halo through L2), 0 every face tile last.
  *                  Same bits either way.
- *   "wide2d"       1 (default): 2D grids (BC 1-3) of the mixed class, and
- *                  FP32 2SHOC, take the single-pass stage kernels (one
+ *   "wide2d"       1 (default): 2D grids (BC 1-3) of the mixed and FP32
+ *                  classes take the single-pass stage kernels (one
  *                  launch per stage, the tile staged in shared memory);
  *                  0: the gather kernels (two launches per 2SHOC stage).
  *                  FP32: same bits; mixed: within the mixed tolerance, not

@@ -29,11 +29,11 @@ static cudaError_t launch_one(const Geom& g, const Consts<R>& c, const ExactStag
     if (seg1d_exact_path(g, METHOD, BC, kernel_kind, sizeof(R) == 4))
       return seg1d::launch_exact<R, METHOD, BC>(g, c, a, stage, st, wide::g_pdl != 0);
   }
-  // FP32 2SHOC on 2D grids: the single-pass tile kernel (1.4-1.5x the
-  // two-launch D-scratch form).  FP64 stays on the gather kernels, bound by
-  // FP64 issue, where the tile's D on the halo costs more than the D scratch;
-  // so does CD, a single gather launch already.
-  if constexpr (DIM == 2 && METHOD == 2 && std::is_same<R, float>::value) {
+  // FP32 on 2D grids: the single-pass tile kernel (2SHOC 1.4-1.5x the
+  // two-launch D-scratch form; CD, staged by cp.async, 1.0-1.16x the gather
+  // launch).  FP64 stays on the gather kernels, bound by FP64 issue, where
+  // the tile's D on the halo costs more than the D scratch.
+  if constexpr (DIM == 2 && std::is_same<R, float>::value) {
     if (kernel_kind == KERNEL_TILED && BC != 4 && wide::g_wide2d)
       return tile2d::launch<R, METHOD, BC == 4 ? 1 : BC>(g, c, a, stage, st, wide::g_pdl != 0);
   }
@@ -53,8 +53,8 @@ static cudaError_t launch_one(const Geom& g, const Consts<R>& c, const ExactStag
 }
 
 static bool tile2d_path(const Geom& g, int method, int BC, int kernel_kind, bool single) {
-  return g.ndim == 2 && method == 2 && single && kernel_kind == KERNEL_TILED && BC != 4 &&
-         wide::g_wide2d;
+  (void)method;
+  return g.ndim == 2 && single && kernel_kind == KERNEL_TILED && BC != 4 && wide::g_wide2d;
 }
 
 // D scratch: 2SHOC in gather form.  FP32 2D grids on the tile kernel take

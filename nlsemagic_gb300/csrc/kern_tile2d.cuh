@@ -1,7 +1,7 @@
 // Exact-precision 2D stage kernel: one launch per RK4 stage, the stage input
 // staged once per tile in shared memory and, for 2SHOC, D formed there too
 // (no D scratch in HBM, no second launch).  Written for both exact
-// precisions and methods; dispatched for FP32 2SHOC (kern_exact.cu).
+// precisions and methods; dispatched for FP32 (kern_exact.cu).
 //
 // A CTA of 32 x 8 threads owns a 32 x TY tile (the tiling of the mixed 2D
 // kernel, kern_wide2d.cuh: tiles shifted so that none starts at 1 or n-1,

@@ -1,6 +1,6 @@
-"""Exact-precision 2D stage kernels.  FP32 2SHOC takes the single-pass tile
-kernel (the stage input staged per tile in shared memory, D formed there,
-one launch per stage); FP64 and CD keep the gather kernels.  Every
+"""Exact-precision 2D stage kernels.  FP32 takes the single-pass tile kernel
+(the stage input staged per tile in shared memory, 2SHOC's D formed there,
+one launch per stage); FP64 keeps the gather kernels.  Every
 combination is bit-identical to the oracle (the reference C integrators'
 arithmetic) for both precisions, both methods, every boundary code and
 every tile-height setting, on grids whose sides fall on every residue the
