@@ -3,8 +3,8 @@
 // A CTA owns a 32 x TY tile and stages it with a 2-cell halo (hi and E) in
 // shared memory.  Interior points take the 2SHOC wide form
 // a/(12 h^2) (16 sum_f (Y_f - Y_0) - sum_2 (Y_2 - Y_0)) (or the CD five-point
-// form) from shared memory, so D is never formed.  Next to a face
-// the wide form is exact once the cell beyond the face point b holds the
+// form) from shared memory, so D is never formed.  Next to a face the wide
+// form is exact once the cell beyond the face point b holds the
 // ghost value G = Y_b + h^2 D_bc(b) - (Y_q - Y_b) - sum_t (Y_t - Y_b) (q =
 // b's inward neighbour, t = b's two in-face neighbours; the 3D kernel's
 // identity in 2D).  Unlike the streaming 3D kernel a 2D tile is staged once,
@@ -25,8 +25,8 @@
 // a face and the face point whose ghost it reads.
 // TY (32, 16 or 8 rows; 4, 2 or 1 per thread) trades the halo's share of
 // the staged cells against the number of CTAs: short tiles keep every SM
-// busy on small grids.  The tile is staged with cp.async (every copy of a
-// thread in flight at once, no registers on the way).
+// busy on small grids.  8- and 16-row tiles are staged with cp.async (every
+// copy of a thread in flight at once, no registers on the way).
 // The arithmetic is that of the mixed class (nlse_mixed.cuh): explicit
 // rounding, difference-form sums.
 #pragma once
@@ -70,9 +70,6 @@ struct Smem {
   float2 fq[TY][TX];
 };
 
-// One tile (bxi, byi) of a stage, by the NT threads of the calling CTA (the
-// stage kernel below, or the batched persistent kernel, nlse_batch.cu), in
-// the shared memory the caller provides.
 // Tile staging by cp.async (ASYNC: 8- and 16-row tiles, the batched
 // launch's 32-row tiles) or through registers (the stage kernel's 32-row
 // tiles, 32 registers a thread: cp.async measured no faster there).
@@ -81,6 +78,9 @@ __host__ __device__ constexpr bool async_staging() {
   return TY <= 16;
 }
 
+// One tile (bxi, byi) of a stage, by the NT threads of the calling CTA (the
+// stage kernel below, or the batched persistent kernel, nlse_batch.cu), in
+// the shared memory the caller provides.
 template <int METHOD, int BC, int STAGE, int TY, bool ASYNC = async_staging<TY>()>
 __device__ __forceinline__ void tile(const Geom& g, const Args& A, int bxi, int byi, int sx,
                                      int sy, Smem<TY>& sm) {
