@@ -82,8 +82,9 @@ __host__ __device__ constexpr bool async_staging() {
 // stage kernel below, or the batched persistent kernel, nlse_batch.cu), in
 // the shared memory the caller provides.
 template <int METHOD, int BC, int STAGE, int TY, bool ASYNC = async_staging<TY>()>
-__device__ __forceinline__ void tile(const Geom& g, const Args& A, int bxi, int byi, int sx,
-                                     int sy, Smem<TY>& sm) {
+__device__ __forceinline__ void tile(const Geom& g, const MixedStageArgs& a,
+                                     const Consts<float>& c, int bxi, int byi, int sx, int sy,
+                                     Smem<TY>& sm) {
   constexpr int SY = TY + 2 * HALO, R = TY / BY;
   constexpr bool PF = Shape<TY>::prefetch;
   constexpr int NG = 2 * TY + 2 * TX;  // face points of a tile: x faces, then y faces
@@ -94,7 +95,7 @@ __device__ __forceinline__ void tile(const Geom& g, const Args& A, int bxi, int 
   const int M = g.M, N = g.N;
   const int x0 = bxi * TX - sx, y0 = byi * TY - sy;
   const int tid = (int)(threadIdx.y * blockDim.x + threadIdx.x), tx = tid % BX, ty = tid / BX;
-  const float2* Ein = STAGE == 1 ? A.a.lo_in : A.a.e_in;
+  const float2* Ein = STAGE == 1 ? a.lo_in : a.e_in;
   const bool edge = x0 <= 0 || x0 + TX > M - 1 || y0 <= 0 || y0 + TY > N - 1;
 
   // 1. staged tile (and the point-local inputs with it on short tiles)
@@ -103,12 +104,12 @@ __device__ __forceinline__ void tile(const Geom& g, const Args& A, int bxi, int 
     const bool in = gx >= 0 && gx < M && gy >= 0 && gy < N;
     const unsigned p = in ? (unsigned)gy * M + gx : 0u;
     if (ASYNC) {
-      cp_async<8>(&sh[cy][cx], A.a.hi_in + p, in);
+      cp_async<8>(&sh[cy][cx], a.hi_in + p, in);
       cp_async<8>(&se[cy][cx], Ein + p, in);
     } else {
       float2 h = make_float2(0.f, 0.f), e = h;
       if (in) {
-        h = A.a.hi_in[p];
+        h = a.hi_in[p];
         e = Ein[p];
       }
       sh[cy][cx] = h;
@@ -124,9 +125,9 @@ __device__ __forceinline__ void tile(const Geom& g, const Args& A, int bxi, int 
     lor[r] = kr[r] = make_float2(0.f, 0.f);
     if (x >= 0 && x < M && y >= 0 && y < N) {
       const unsigned p = (unsigned)y * M + x;
-      vr[r] = A.a.V[p];
-      if (STAGE != 1) lor[r] = __ldcg(A.a.lo_in + p);
-      if (STAGE == 4) kr[r] = __ldcg(A.a.K + p);
+      vr[r] = a.V[p];
+      if (STAGE != 1) lor[r] = __ldcg(a.lo_in + p);
+      if (STAGE == 4) kr[r] = __ldcg(a.K + p);
     }
   };
   if (PF) {
@@ -152,8 +153,8 @@ __device__ __forceinline__ void tile(const Geom& g, const Args& A, int bxi, int 
       dy = side == 0 ? 1 : -1;
       gt = by >= y0 && by < y0 + TY && bx >= 1 && bx <= M - 2;
     }
-    if (gt && BC != 3) vb = A.a.V[(unsigned)by * M + bx];
-    if (gt && BC == 2) vq = A.a.V[(unsigned)(by + dy) * M + bx + dx];
+    if (gt && BC != 3) vb = a.V[(unsigned)by * M + bx];
+    if (gt && BC == 2) vq = a.V[(unsigned)(by + dy) * M + bx + dx];
   }
   if (ASYNC) cp_async_wait_all();
   __syncthreads();
@@ -172,14 +173,14 @@ __device__ __forceinline__ void tile(const Geom& g, const Args& A, int bxi, int 
       float2 dq = make_float2(0.f, 0.f);
       if (BC == 2) {
         const HE nq[4] = {at(qx, qy + 1), at(qx, qy - 1), at(qx + 1, qy), at(qx - 1, qy)};
-        dq = mixed::d_interior<2>(A.c, uq, nq);
+        dq = mixed::d_interior<2>(c, uq, nq);
       }
-      const float2 dbc = mixed::d_boundary<BC>(A.c, ub, vb, uq, vq, dq, nullptr);
+      const float2 dbc = mixed::d_boundary<BC>(c, ub, vb, uq, vq, dq, nullptr);
       const HE tn[2] = {at(bx + dy, by + dx), at(bx - dy, by - dx)};  // along the face
       const float2 st = mixed::lapsum<2>(ub, tn);
       const float2 sq = mixed::lapsum<1>(ub, &uq);
       const float2 delta =
-          mixed::psub(mixed::pmul(mixed::P2(A.c.h2), dbc), mixed::padd(sq, st));
+          mixed::psub(mixed::pmul(mixed::P2(c.h2), dbc), mixed::padd(sq, st));
       const int gx = bx - dx - x0 + HALO, gy = by - dy - y0 + HALO;  // the cell beyond b
       sh[gy][gx] = ub.h;
       se[gy][gx] = mixed::padd(ub.e, delta);
@@ -191,13 +192,13 @@ __device__ __forceinline__ void tile(const Geom& g, const Args& A, int bxi, int 
   auto upd = [&](unsigned p, float2 Tv, const HE& u, float2 lo, float2 kv) {
     const float2 lo_ = STAGE == 1 ? u.e : lo;  // stage 1: E = lo
     float2 eo, ko, ho, l2;
-    mixed::stage_update(A.c, STAGE, Tv, u.h, lo_, u.e, kv, eo, ko, ho, l2);
-    if (STAGE == 2) A.a.K[p] = ko;
+    mixed::stage_update(c, STAGE, Tv, u.h, lo_, u.e, kv, eo, ko, ho, l2);
+    if (STAGE == 2) a.K[p] = ko;
     if (STAGE < 4) {
-      A.a.e_out[p] = eo;
+      a.e_out[p] = eo;
     } else {
-      A.a.hi_out[p] = ho;
-      A.a.lo_out[p] = l2;
+      a.hi_out[p] = ho;
+      a.lo_out[p] = l2;
     }
   };
 
@@ -211,10 +212,10 @@ __device__ __forceinline__ void tile(const Geom& g, const Args& A, int bxi, int 
     const HE fn[4] = {at(x, y + 1), at(x, y - 1), at(x + 1, y), at(x - 1, y)};
     float2 Tv;
     if (METHOD == 1) {
-      Tv = mixed::f_interior_cd<2>(A.c, u0, vr[r], fn);
+      Tv = mixed::f_interior_cd<2>(c, u0, vr[r], fn);
     } else {
       const HE f2n[4] = {at(x, y + 2), at(x, y - 2), at(x + 2, y), at(x - 2, y)};
-      Tv = mixed::f_wide_2shoc<2>(A.c, u0, vr[r], fn, f2n);
+      Tv = mixed::f_wide_2shoc<2>(c, u0, vr[r], fn, f2n);
     }
     if (BC == 2 && edge && (x == 1 || x == M - 2 || y == 1 || y == N - 2)) fq[ly][tx] = Tv;
     upd((unsigned)y * M + x, Tv, u0, lor[r], kr[r]);
@@ -233,7 +234,7 @@ __device__ __forceinline__ void tile(const Geom& g, const Args& A, int bxi, int 
     const int qy = y < 1 ? 1 : (y > N - 2 ? N - 2 : y);
     const HE ub = at(x, y), uq = at(qx, qy);
     const float2 fqv = BC == 2 ? fq[qy - y0][qx - x0] : make_float2(0.f, 0.f);
-    const float2 Tv = mixed::f_boundary<METHOD, BC>(A.c, ub, vr[r], uq, fqv, nullptr);
+    const float2 Tv = mixed::f_boundary<METHOD, BC>(c, ub, vr[r], uq, fqv, nullptr);
     upd((unsigned)y * M + x, Tv, ub, lor[r], kr[r]);
   }
 }
@@ -247,7 +248,7 @@ __global__ void __launch_bounds__(NT, min_blocks<METHOD, BC, TY>())
   pdl_trigger();  // the next kernel may launch; it waits for this one
   pdl_wait();     // the previous kernel's output
   const int t = (int)blockIdx.x;
-  tile<METHOD, BC, STAGE, TY>(g, A, t % nbx, t / nbx, sx, sy, sm);
+  tile<METHOD, BC, STAGE, TY>(g, A.a, A.c, t % nbx, t / nbx, sx, sy, sm);
 }
 
 __host__ __device__ inline int shift(int n, int t) { return (n - 1) % t == 0 ? 1 : 0; }

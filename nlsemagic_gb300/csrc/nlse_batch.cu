@@ -204,14 +204,13 @@ __device__ __noinline__ void seg_mixed(const BSolve& s, int stage, int par, long
 template <int METHOD, int BC, int STAGE>
 __device__ __noinline__ void rect_mixed(const BSolve& s, int par, long long t, void* smem) {
   const MixedIO io = mixed_io(s, STAGE, par);
-  wide2d::Args A;
-  A.a = MixedStageArgs{io.hi_in, io.lo_in, io.d_in, io.V,    io.K,   io.d_out,
-                       io.hi_out, io.lo_out, nullptr, nullptr, nullptr};
-  A.c = s.cf;
+  const MixedStageArgs a{io.hi_in, io.lo_in, io.d_in, io.V,    io.K,   io.d_out,
+                         io.hi_out, io.lo_out, nullptr, nullptr, nullptr};
   const int sx = wide2d::shift(s.g.M, wide2d::TX), sy = wide2d::shift(s.g.N, W2_TY);
   const int nbx = (s.g.M + sx + wide2d::TX - 1) / wide2d::TX;
-  wide2d::tile<METHOD, BC, STAGE, W2_TY, true>(s.g, A, (int)(t % nbx), (int)(t / nbx), sx, sy,
-                                               *reinterpret_cast<wide2d::Smem<W2_TY>*>(smem));
+  // constants read from the descriptor in shared memory
+  wide2d::tile<METHOD, BC, STAGE, W2_TY, true>(s.g, a, s.cf, (int)(t % nbx), (int)(t / nbx), sx,
+                                               sy, *reinterpret_cast<wide2d::Smem<W2_TY>*>(smem));
 }
 
 template <int METHOD, int BC>
