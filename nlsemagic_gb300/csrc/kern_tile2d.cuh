@@ -46,8 +46,11 @@ __global__ void __launch_bounds__(NT)
   pdl_trigger();  // the next kernel may launch; it waits for this one
   pdl_wait();     // the previous kernel's output
   const int M = g.M, N = g.N;
-  // one CTA per tile, tiles numbered x-fastest in a one-dimensional grid
-  const int x0 = (int)(blockIdx.x % nbx) * TX - sx, y0 = (int)(blockIdx.x / nbx) * TY - sy;
+  // one CTA per tile: a two-dimensional grid, or (nbx > 0: more tile rows
+  // than gridDim.y allows) tiles numbered x-fastest in a one-dimensional one
+  const int bxi = nbx ? (int)(blockIdx.x % nbx) : (int)blockIdx.x;
+  const int byi = nbx ? (int)(blockIdx.x / nbx) : (int)blockIdx.y;
+  const int x0 = bxi * TX - sx, y0 = byi * TY - sy;
   const int tid = threadIdx.y * BX + threadIdx.x;
 
   // 1. stage Y
@@ -133,10 +136,12 @@ template <typename R, int METHOD, int BC, int TY>
 cudaError_t launch_ty(const Geom& g, const Consts<R>& c, const ExactStageArgs<R>& a, int stage,
                       cudaStream_t st, bool pdl) {
   const int sx = wide2d::shift(g.M, TX), sy = wide2d::shift(g.N, TY);
-  const int nbx = (g.M + sx + TX - 1) / TX;
-  const dim3 grid((unsigned)wide2d::tiles(g, TY)), block(BX, BY);
+  const int nbx = (g.M + sx + TX - 1) / TX, nby = (g.N + sy + TY - 1) / TY;
+  const bool flat = nby > 65535;
+  const dim3 grid(flat ? (unsigned)wide2d::tiles(g, TY) : (unsigned)nbx, flat ? 1u : (unsigned)nby);
+  const dim3 block(BX, BY);
   return launch_k(exact2d<R, METHOD, BC, TY>, grid, block, 0, st, pdl, g, c, a.Yin, a.Psi, a.V,
-                  a.K, a.Yout, stage, sx, sy, nbx);
+                  a.K, a.Yout, stage, sx, sy, flat ? nbx : 0);
 }
 
 template <typename R, int METHOD, int BC>

@@ -239,8 +239,9 @@ __device__ __forceinline__ void tile(const Geom& g, const MixedStageArgs& a,
   }
 }
 
-// One CTA per tile, tiles numbered x-fastest in a one-dimensional grid (a
-// tall grid has more tile rows than gridDim.y allows).
+// One CTA per tile: a two-dimensional grid of tiles, or (nbx > 0: a tall
+// grid has more tile rows than gridDim.y allows) tiles numbered x-fastest
+// in a one-dimensional grid.
 template <int METHOD, int BC, int STAGE, int TY>
 __global__ void __launch_bounds__(NT, min_blocks<METHOD, BC, TY>())
     stage2d(Geom g, Args A, int sx, int sy, int nbx) {
@@ -248,7 +249,8 @@ __global__ void __launch_bounds__(NT, min_blocks<METHOD, BC, TY>())
   pdl_trigger();  // the next kernel may launch; it waits for this one
   pdl_wait();     // the previous kernel's output
   const int t = (int)blockIdx.x;
-  tile<METHOD, BC, STAGE, TY>(g, A.a, A.c, t % nbx, t / nbx, sx, sy, sm);
+  const int bxi = nbx ? t % nbx : t, byi = nbx ? t / nbx : (int)blockIdx.y;
+  tile<METHOD, BC, STAGE, TY>(g, A.a, A.c, bxi, byi, sx, sy, sm);
 }
 
 __host__ __device__ inline int shift(int n, int t) { return (n - 1) % t == 0 ? 1 : 0; }
@@ -271,14 +273,19 @@ template <int METHOD, int BC, int TY>
 cudaError_t launch_ty(const Geom& g, const MixedStageArgs& a, const Consts<float>& c, int stage,
                       cudaStream_t st, bool pdl) {
   const int sx = shift(g.M, TX), sy = shift(g.N, TY);
-  const int nbx = (g.M + sx + TX - 1) / TX;
-  const dim3 grid((unsigned)tiles(g, TY)), block(BX, BY);
+  const int nbx = (g.M + sx + TX - 1) / TX, nby = (g.N + sy + TY - 1) / TY;
+  // a two-dimensional grid where it fits: the index arithmetic of the
+  // one-dimensional numbering measured 4-8% slower at 512^2
+  const bool flat = nby > 65535;
+  const dim3 grid(flat ? (unsigned)tiles(g, TY) : (unsigned)nbx, flat ? 1u : (unsigned)nby);
+  const dim3 block(BX, BY);
+  const int nbx_arg = flat ? nbx : 0;
   const Args A{a, c};
   switch (stage) {
-    case 1: return launch_k(stage2d<METHOD, BC, 1, TY>, grid, block, 0, st, pdl, g, A, sx, sy, nbx);
-    case 2: return launch_k(stage2d<METHOD, BC, 2, TY>, grid, block, 0, st, pdl, g, A, sx, sy, nbx);
-    case 3: return launch_k(stage2d<METHOD, BC, 3, TY>, grid, block, 0, st, pdl, g, A, sx, sy, nbx);
-    case 4: return launch_k(stage2d<METHOD, BC, 4, TY>, grid, block, 0, st, pdl, g, A, sx, sy, nbx);
+    case 1: return launch_k(stage2d<METHOD, BC, 1, TY>, grid, block, 0, st, pdl, g, A, sx, sy, nbx_arg);
+    case 2: return launch_k(stage2d<METHOD, BC, 2, TY>, grid, block, 0, st, pdl, g, A, sx, sy, nbx_arg);
+    case 3: return launch_k(stage2d<METHOD, BC, 3, TY>, grid, block, 0, st, pdl, g, A, sx, sy, nbx_arg);
+    case 4: return launch_k(stage2d<METHOD, BC, 4, TY>, grid, block, 0, st, pdl, g, A, sx, sy, nbx_arg);
   }
   return cudaErrorInvalidValue;
 }
