@@ -7,8 +7,8 @@
 // so that none starts at 1 or n-1: an end point and its MSD neighbour share a
 // segment, and the neighbour's F (which reads D on both sides of it) is
 // formed from the segment's own D.  Every value is the same per-point
-// function of the same operands as in the gather kernels (kern_gather.cuh:
-// mixed::d_at, f_int, f_at_d), so the results are the same bits.
+// function of the same operands as in the gather kernels of its class
+// (kern_gather.cuh: d_at, f_int, f_at_d), so the results are the same bits.
 // Boundary code 4 (one-sided ends) is not handled here.
 #pragma once
 
