@@ -280,6 +280,12 @@ int nlse_take_steps_noalloc(const nlse_problem *p, const double *dUr, const doub
  *                  bit for bit (the single-pass kernel takes the wide form).
  *   "wide2d.ty"    tile height of those kernels: 0 (default) by grid size,
  *                  or 8, 16, 32.  Same bits.
+ *   "io.zero_copy" 1 (default): host arrays in page-locked memory mapped
+ *                  into the device address space (cudaHostAlloc,
+ *                  cudaHostRegister) are read and written in place by the
+ *                  layout-conversion kernels of nlse_solver_upload /
+ *                  _download and the one-shot calls; 0: always staged
+ *                  through device copies.  Same bits.
  *   "seg1d"        1 (default): 1D grids (BC 1-3) above
  *                  "small1d.max_points" take the staged-segment stage
  *                  kernels (one launch per stage, 2SHOC's D in shared

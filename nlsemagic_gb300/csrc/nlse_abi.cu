@@ -67,6 +67,10 @@ extern int g_ty;
 }
 }  // namespace nlse
 static int g_default_graph_steps = 8;
+// Host arrays in page-locked (device-mapped) memory are read and written by
+// the layout-conversion kernels in place, over the host link, instead of
+// being copied into a device staging buffer first.
+static int g_zero_copy = 1;
 // FP32 and mixed 1D solves of at most this many points run each chunk in
 // single-block launches (0: never).  At the 1024-point configuration this
 // runs 2.0-2.6x faster than a launch per pass; FP64 does not gain (one SM's
@@ -83,6 +87,11 @@ extern "C" int nlse_tune_set(const char* key, long long value) {
   if (!strcmp(key, "wide2d")) {
     if (value != 0 && value != 1) return fail(NLSE_ERR_ARG, "wide2d must be 0 or 1");
     nlse::wide::g_wide2d = (int)value;
+    return NLSE_OK;
+  }
+  if (!strcmp(key, "io.zero_copy")) {
+    if (value != 0 && value != 1) return fail(NLSE_ERR_ARG, "io.zero_copy must be 0 or 1");
+    g_zero_copy = (int)value;
     return NLSE_OK;
   }
   if (!strcmp(key, "seg1d")) {
@@ -145,6 +154,10 @@ extern "C" int nlse_tune_get(const char* key, long long* value) {
   }
   if (!strcmp(key, "seg1d")) {
     *value = nlse::wide::g_seg1d;
+    return NLSE_OK;
+  }
+  if (!strcmp(key, "io.zero_copy")) {
+    *value = g_zero_copy;
     return NLSE_OK;
   }
   if (!strcmp(key, "wide.z2")) {
@@ -468,7 +481,7 @@ static int ingest(nlse_solver* s, const double* re, const double* im, const doub
   switch (s->prob.precision) {
     case NLSE_PREC_DOUBLE:
       CUDA_TRY(planar_to_c2d(re, im, (C2<double>*)s->psi, n, s->stream));
-      if (V) CUDA_TRY(cudaMemcpyAsync(s->V, V, sizeof(double) * n, cudaMemcpyDeviceToDevice, s->stream));
+      if (V) CUDA_TRY(cudaMemcpyAsync(s->V, V, sizeof(double) * n, cudaMemcpyDefault, s->stream));
       break;
     case NLSE_PREC_SINGLE:
       CUDA_TRY(planar_to_c2f(re, im, (C2<float>*)s->psi, n, s->stream));
@@ -489,10 +502,33 @@ extern "C" int nlse_solver_upload_device(nlse_solver* s, const double* dUr, cons
   return ingest(s, dUr, dUi, dV);
 }
 
+// Device view of a host array in page-locked memory mapped into the device
+// address space (cudaHostAlloc / cudaHostRegister), else null (pageable
+// memory: staged by copies).
+static const double* mapped_host(const double* p) {
+  if (!g_zero_copy || !p) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost && a.devicePointer ? (const double*)a.devicePointer
+                                                         : nullptr;
+}
+
 extern "C" int nlse_solver_upload(nlse_solver* s, const double* Ur, const double* Ui,
                                   const double* V) {
   if (!s || !Ur || !V) return fail(NLSE_ERR_ARG, "NULL argument");
   CUDA_TRY(cudaSetDevice(s->device));
+  {  // page-locked arrays: converted in place by the ingest kernels
+    const double *dr = mapped_host(Ur), *di = mapped_host(Ui), *dv = mapped_host(V);
+    if (dr && dv && (!Ui || di)) {
+      int r = ingest(s, dr, Ui ? di : nullptr, dv);
+      if (r) return r;
+      CUDA_TRY(cudaStreamSynchronize(s->stream));
+      return NLSE_OK;
+    }
+  }
   int r = ensure_stage(s);
   if (r) return r;
   const long long n = s->g.n;
@@ -533,6 +569,16 @@ extern "C" int nlse_solver_download_device(nlse_solver* s, double* dUr, double* 
 extern "C" int nlse_solver_download(nlse_solver* s, double* Ur, double* Ui) {
   if (!s || !Ur || !Ui) return fail(NLSE_ERR_ARG, "NULL argument");
   CUDA_TRY(cudaSetDevice(s->device));
+  {  // page-locked arrays: written in place by the emit kernels
+    double* dr = (double*)mapped_host(Ur);
+    double* di = (double*)mapped_host(Ui);
+    if (dr && di) {
+      int r = emit(s, dr, di);
+      if (r) return r;
+      CUDA_TRY(cudaStreamSynchronize(s->stream));
+      return device_error_check();
+    }
+  }
   int r = ensure_stage(s);
   if (r) return r;
   const long long n = s->g.n;

@@ -64,7 +64,8 @@ def test_tuning_knobs_roundtrip_and_validation(lib):
         autotune.set_knob("no.such.knob", 1)
     with pytest.raises(_lib.NLSEError):
         autotune.set_knob("graph.steps", -3)
-    for key, good, bad in (("wide2d", 0, 2), ("wide2d.ty", 16, 12), ("seg1d", 0, 2)):
+    for key, good, bad in (("wide2d", 0, 2), ("wide2d.ty", 16, 12), ("seg1d", 0, 2),
+                           ("io.zero_copy", 0, 3)):
         old = autotune.get_knob(key)
         autotune.set_knob(key, good)
         assert autotune.get_knob(key) == good
