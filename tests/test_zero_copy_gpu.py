@@ -56,7 +56,8 @@ def test_pinned_and_pageable_same_bits(gpu_lib, shape, method, BC, prec):
             got = (ore.numpy() + 1j * oim.numpy()).reshape(shape, order="F")
         finally:
             autotune.set_knob("io.zero_copy", old)
-        assert np.array_equal(got.view(np.float64), np.ascontiguousarray(want).view(np.float64))
+        assert np.array_equal(np.ascontiguousarray(got).view(np.float64),
+                              np.ascontiguousarray(want).view(np.float64))
 
 
 def test_pinned_real_input(gpu_lib):
