@@ -27,7 +27,7 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from ._lib import FLAG_MSD_GUARD, PREC_DOUBLE, PREC_MIXED, PREC_SINGLE, Problem, check, load
+from ._lib import FLAG_MSD_GUARD, PREC_DOUBLE, PREC_MIXED, Problem, check, load
 
 _dp = ctypes.POINTER(ctypes.c_double)
 

@@ -6,7 +6,6 @@ CPU (no GPU involved)."""
 import os
 import socket
 
-import pytest
 import torch.multiprocessing as mp
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
