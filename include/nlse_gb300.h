@@ -167,6 +167,11 @@ int nlse_solver_download_device(nlse_solver *s, double *dUr, double *dUi);
  * mass).  Returns NLSE_ERR_NONFINITE if the state holds NaN or Inf. */
 int nlse_solver_mass(nlse_solver *s, double *sum_abs2);
 int nlse_solver_sync(nlse_solver *s);
+/* Non-blocking: *idle = 1 when every step queued on the solver's stream has
+ * finished (then as nlse_solver_sync), 0 while work is in flight.  For
+ * request loops that keep several solves in flight (no reference
+ * counterpart). */
+int nlse_solver_query(nlse_solver *s, int *idle);
 /* The cudaStream_t the solver enqueues on. */
 int nlse_solver_stream(nlse_solver *s, void **stream);
 /* Steps per captured CUDA graph (default 8; 0 disables graphs). */
@@ -213,6 +218,9 @@ int nlse_batch_download(nlse_batch *b, int slot, double *Ur, double *Ui);
 /* Release a slot and its pool memory. */
 int nlse_batch_remove(nlse_batch *b, int slot);
 int nlse_batch_sync(nlse_batch *b);
+/* Non-blocking: *idle = 1 when the batch's queued launches have finished
+ * (then as nlse_batch_sync), 0 while they run. */
+int nlse_batch_query(nlse_batch *b, int *idle);
 /* Active solves, total grid points, and free pool bytes. */
 int nlse_batch_stats(nlse_batch *b, int *active, long long *points, long long *free_bytes);
 /* cudaStream_t of the batch. */
@@ -222,20 +230,24 @@ int nlse_batch_last_launches(nlse_batch *b);
 
 /* ------------------------------------------------------------------------
  * Allocation-free FP64 chunk.  No counterpart in the reference: an addition
- * for callers that must not allocate device memory -- work recorded while a
- * stream is captured into a CUDA graph, plug-ins whose host application owns
- * every device allocation (e.g. a MEX function on MATLAB gpuArray data), and
- * real-time loops that may not allocate after start-up.
+ * for callers that must not allocate device memory -- plug-ins whose host
+ * application owns every device allocation (e.g. a MEX function on MATLAB
+ * gpuArray data, or a framework with its own memory pool, where a library's
+ * private cudaMalloc would escape the host's accounting or fail against its
+ * reservation) and real-time loops that may not allocate after start-up.
  *
  * Same problem description as nlse_take_steps, but the arrays are DEVICE
  * pointers owned by the caller (planar doubles; dUi may be NULL) and the call
  * is asynchronous on `stream` (a cudaStream_t; NULL = legacy default stream).
- * precision must be NLSE_PREC_DOUBLE (results identical to nlse_take_steps).
+ * precision must be NLSE_PREC_DOUBLE; the results are bit-identical to
+ * nlse_take_steps in FP64 (both reproduce the reference C integrator).
  * The RK4 scratch is a fixed device array inside the library holding
  * NLSE_NOALLOC_MAX_POINTS grid points (16 MiB, held on every GPU that loads
  * the library until the process exits); larger grids return
- * NLSE_ERR_CAPACITY.  The first call on a device looks the array's address
- * up once (no allocation); make that first call before any stream capture.
+ * NLSE_ERR_CAPACITY.  The first call in a device's context looks the array's
+ * address up (no allocation) and caches it for that context; a call in a new
+ * context (after cudaDeviceReset, or under another context) looks it up
+ * again.  Make that first call before any stream capture.
  * All calls share the array and it keeps the last call's contents (nothing in
  * it must start at zero): calls that overlap on the GPU race and must be
  * serialised by the caller.
@@ -295,6 +307,13 @@ int nlse_take_steps_noalloc(const nlse_problem *p, const double *dUr, const doub
  * ---------------------------------------------------------------------- */
 int nlse_tune_set(const char *key, long long value);
 int nlse_tune_get(const char *key, long long *value);
+
+/* Measured FP64 rates of the current device: independent FMAs per second
+ * (2 flops each) and separate FP64 adds per second, from a timed kernel of
+ * independent dependency chains.  No reference counterpart: the compute
+ * roofline of the exact FP64 class, whose reference operation order rules
+ * out multiply-add contraction (so its bound is the add/multiply rate). */
+int nlse_device_fp64_rates(double *fma_per_s, double *add_per_s);
 
 /* Linear stability limit of the time step used by the NLSEmagic drivers:
  * h^2 / (ndim * sqrt(2) * a) for CD, 3/4 of that for 2SHOC
