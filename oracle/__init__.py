@@ -45,6 +45,17 @@ def _load_port():
     return _port
 
 
+def set_threads(n):
+    """OpenMP threads that one take_steps call spreads its grid sweeps over
+    (default 1, serial like the reference).  The result bits do not depend
+    on it: every sweep writes each point from values no other point of the
+    same sweep writes."""
+    f = _load_port().nlse_oracle_set_threads
+    f.restype = None
+    f.argtypes = [ctypes.c_int]
+    f(int(n))
+
+
 def _dims_of(U):
     """MATLAB dims of a MATLAB-shaped array: shape (M,), (M, N) or (M, N, L),
     first index fastest (Fortran order)."""

@@ -26,7 +26,11 @@ from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_OUT = os.path.join(HERE, "_ref")
-REFERENCE_ROOT = os.environ.get("NLSE_REFERENCE_ROOT", "/root/reference")
+# The reference checkout: $NLSE_REFERENCE_ROOT, else a sibling directory
+# named "reference" next to this checkout.
+REFERENCE_ROOT = os.environ.get(
+    "NLSE_REFERENCE_ROOT",
+    os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 
 # name -> path relative to the reference checkout
 REF_FILES = {
@@ -48,8 +52,10 @@ REF_FILES = {
 
 REF_CFLAGS = ["-std=gnu89", "-O3", "-funroll-loops", "-ffp-contract=off",
               "-fPIC", "-shared", "-w"]
-PORT_CFLAGS = ["-std=c99", "-O3", "-ffp-contract=off", "-fPIC", "-shared",
-               "-Wall", "-Wno-unused-function", "-pthread"]
+# -fopenmp: nlse_oracle_set_threads() spreads one solve's grid sweeps over
+# threads for the large parity runs (bit-identical; default one thread).
+PORT_CFLAGS = ["-std=c99", "-O3", "-funroll-loops", "-ffp-contract=off", "-fopenmp", "-fPIC",
+               "-shared", "-Wall", "-Wno-unused-function", "-pthread"]
 
 PORT_SRC = os.path.join(HERE, "nlse_oracle.c")
 PORT_LIB = os.path.join(HERE, "libnlse_oracle.so")
@@ -70,7 +76,7 @@ def _stale(out, srcs):
 
 def build_port(force: bool = False) -> str:
     """Compile this project's C restatement into oracle/libnlse_oracle.so."""
-    srcs = [PORT_SRC, os.path.join(HERE, "nlse_oracle_impl.h")]
+    srcs = [PORT_SRC, os.path.join(HERE, "nlse_oracle_impl.h"), os.path.abspath(__file__)]
     if force or _stale(PORT_LIB, srcs):
         tmp = PORT_LIB + ".tmp%d" % os.getpid()
         _run(["gcc"] + PORT_CFLAGS + [PORT_SRC, "-o", tmp, "-lm"])

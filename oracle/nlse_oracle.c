@@ -53,6 +53,14 @@
 #undef REAL
 #undef SUFFIX
 
+/* OpenMP threads of the grid sweeps of nlse_oracle_take_steps (default 1:
+ * serial, as the reference).  Every sweep writes each point from values that
+ * no other point of the same sweep writes, so the result bits do not depend
+ * on the thread count. */
+static int g_threads = 1;
+
+void nlse_oracle_set_threads(int n) { g_threads = n < 1 ? 1 : n; }
+
 static int check_args(int ndim, int method, const long long *dims, int BC, int chunk) {
     int d;
     if (ndim < 1 || ndim > 3) return -1;
@@ -83,6 +91,7 @@ int nlse_oracle_take_steps(int ndim, int method, int precision, const long long 
         c.ndim = ndim; c.method = method; c.BC = BC;
         c.guard = flags & NLSE_ORACLE_MSD_GUARD;
         c.quirk = 0;
+        c.nthreads = g_threads;
         c.M = M; c.N = N; c.L = L;
         c.s = s; c.a = a; c.V = V;
         c.ah2 = a / h2;
@@ -121,6 +130,7 @@ int nlse_oracle_take_steps(int ndim, int method, int precision, const long long 
         c.ndim = ndim; c.method = method; c.BC = BC;
         c.guard = flags & NLSE_ORACLE_MSD_GUARD;
         c.quirk = (flags & NLSE_ORACLE_REF_QUIRKS) && ndim == 3 && method == 2;
+        c.nthreads = g_threads;
         c.M = M; c.N = N; c.L = L;
         c.s = fs; c.a = fa; c.V = fv;
         c.ah2 = fa / fh2;

@@ -26,6 +26,7 @@
 
 typedef struct {
     int ndim, method, BC, guard, quirk;
+    int nthreads; /* OpenMP threads of the grid sweeps (1 = serial) */
     long M, N, L; /* L = N = 1 in 1D, L = 1 in 2D */
     REAL s, a;
     /* method 1 (CD) */
@@ -39,8 +40,9 @@ typedef struct {
 
 /* A = B + c*C on both planes (vec_add / add_matrix / add_cube). */
 static void FN(axpy)(REAL *Ar, REAL *Ai, const REAL *Br, const REAL *Bi,
-                     const REAL *Cr, const REAL *Ci, REAL c, long n) {
+                     const REAL *Cr, const REAL *Ci, REAL c, long n, int nthreads) {
     long p;
+#pragma omp parallel for if (nthreads > 1) num_threads(nthreads) schedule(static)
     for (p = 0; p < n; ++p) {
         Ar[p] = Br[p] + c * Cr[p];
         Ai[p] = Bi[p] + c * Ci[p];
@@ -106,6 +108,7 @@ static void FN(boundary_f)(const FN(ctx_t) *c, REAL *Fr, REAL *Fi, const REAL *U
                            const REAL *Ui, int bc) {
     long i, j, k;
     const long L = c->L, N = c->N, M = c->M;
+#pragma omp parallel for if (c->nthreads > 1) num_threads(c->nthreads) private(j, k) schedule(static)
     for (i = 0; i < L; ++i)
         for (j = 0; j < N; ++j)
             for (k = 0; k < M; ++k) {
@@ -141,6 +144,7 @@ static void FN(boundary_f)(const FN(ctx_t) *c, REAL *Fr, REAL *Fi, const REAL *U
 static void FN(boundary_d)(const FN(ctx_t) *c, const REAL *Ur, const REAL *Ui, int bc) {
     long i, j, k;
     const long L = c->L, N = c->N, M = c->M;
+#pragma omp parallel for if (c->nthreads > 1) num_threads(c->nthreads) private(j, k) schedule(static)
     for (i = 0; i < L; ++i)
         for (j = 0; j < N; ++j)
             for (k = 0; k < M; ++k) {
@@ -180,6 +184,7 @@ static void FN(f1d_cd)(const FN(ctx_t) *c, REAL *Fr, REAL *Fi, const REAL *Ur, c
     const REAL s = c->s, ah2 = c->ah2;
     const REAL *V = c->V;
     long i;
+#pragma omp parallel for if (c->nthreads > 1) num_threads(c->nthreads) schedule(static)
     for (i = 1; i < N - 1; ++i) {
         Fr[i] = -ah2 * (Ui[i + 1] - 2 * Ui[i] + Ui[i - 1]) -
                 (s * (Ur[i] * Ur[i] + Ui[i] * Ui[i]) - V[i]) * Ui[i];
@@ -207,6 +212,7 @@ static void FN(f1d_2shoc)(const FN(ctx_t) *c, REAL *Fr, REAL *Fi, const REAL *Ur
     const REAL *V = c->V;
     REAL *Dr = c->Dr, *Di = c->Di;
     long i;
+#pragma omp parallel for if (c->nthreads > 1) num_threads(c->nthreads) schedule(static)
     for (i = 1; i < N - 1; ++i) {
         Dr[i] = (Ur[i + 1] - 2 * Ur[i] + Ur[i - 1]) * lh2;
         Di[i] = (Ui[i + 1] - 2 * Ui[i] + Ui[i - 1]) * lh2;
@@ -220,6 +226,7 @@ static void FN(f1d_2shoc)(const FN(ctx_t) *c, REAL *Fr, REAL *Fi, const REAL *Ur
     } else {
         FN(boundary_d)(c, Ur, Ui, c->BC);
     }
+#pragma omp parallel for if (c->nthreads > 1) num_threads(c->nthreads) schedule(static)
     for (i = 1; i < N - 1; ++i) {
         Fr[i] = a112 * (Di[i + 1] + Di[i - 1]) - a76 * Di[i] -
                 (s * (Ur[i] * Ur[i] + Ui[i] * Ui[i]) - V[i]) * Ui[i];
@@ -249,6 +256,7 @@ static void FN(f2d_cd)(const FN(ctx_t) *c, REAL *Fr, REAL *Fi, const REAL *Ur, c
     const REAL s = c->s, ah2 = c->ah2;
     const REAL *V = c->V;
     long i, j;
+#pragma omp parallel for if (c->nthreads > 1) num_threads(c->nthreads) private(j) schedule(static)
     for (i = 1; i < N - 1; ++i)
         for (j = 1; j < M - 1; ++j) {
             const long p = i * M + j;
@@ -266,6 +274,7 @@ static void FN(f2d_2shoc)(const FN(ctx_t) *c, REAL *Fr, REAL *Fi, const REAL *Ur
     const REAL *V = c->V;
     REAL *Dr = c->Dr, *Di = c->Di;
     long i, j;
+#pragma omp parallel for if (c->nthreads > 1) num_threads(c->nthreads) private(j) schedule(static)
     for (i = 1; i < N - 1; ++i)
         for (j = 1; j < M - 1; ++j) {
             const long p = i * M + j;
@@ -273,6 +282,7 @@ static void FN(f2d_2shoc)(const FN(ctx_t) *c, REAL *Fr, REAL *Fi, const REAL *Ur
             Dr[p] = (Ur[p + M] + Ur[p - M] - 4 * Ur[p] + Ur[p + 1] + Ur[p - 1]) * lh2;
         }
     FN(boundary_d)(c, Ur, Ui, c->BC);
+#pragma omp parallel for if (c->nthreads > 1) num_threads(c->nthreads) private(j) schedule(static)
     for (i = 1; i < N - 1; ++i)
         for (j = 1; j < M - 1; ++j) {
             const long p = i * M + j;
@@ -293,6 +303,7 @@ static void FN(f3d_cd)(const FN(ctx_t) *c, REAL *Fr, REAL *Fi, const REAL *Ur, c
     const REAL s = c->s, ah2 = c->ah2;
     const REAL *V = c->V;
     long i, j, k;
+#pragma omp parallel for if (c->nthreads > 1) num_threads(c->nthreads) private(j, k) schedule(static)
     for (i = 1; i < L - 1; ++i)
         for (j = 1; j < N - 1; ++j)
             for (k = 1; k < M - 1; ++k) {
@@ -313,6 +324,7 @@ static void FN(f3d_2shoc)(const FN(ctx_t) *c, REAL *Fr, REAL *Fi, const REAL *Ur
     const REAL *V = c->V;
     REAL *Dr = c->Dr, *Di = c->Di;
     long i, j, k;
+#pragma omp parallel for if (c->nthreads > 1) num_threads(c->nthreads) private(j, k) schedule(static)
     for (i = 1; i < L - 1; ++i)
         for (j = 1; j < N - 1; ++j)
             for (k = 1; k < M - 1; ++k) {
@@ -323,6 +335,7 @@ static void FN(f3d_2shoc)(const FN(ctx_t) *c, REAL *Fr, REAL *Fi, const REAL *Ur
                                6 * Ui[p]);
             }
     FN(boundary_d)(c, Ur, Ui, c->BC);
+#pragma omp parallel for if (c->nthreads > 1) num_threads(c->nthreads) private(j, k) schedule(static)
     for (i = 1; i < L - 1; ++i)
         for (j = 1; j < N - 1; ++j)
             for (k = 1; k < M - 1; ++k) {
@@ -381,16 +394,16 @@ static void FN(rk4_chunk)(FN(ctx_t) *c, REAL *Ur, REAL *Ui, REAL *scratch, int c
     k6 = k / (REAL)6.0;
     for (step = 0; step < chunk; ++step) {
         FN(eval_f)(c, Kr, Ki, Ur, Ui);
-        FN(axpy)(Yr, Yi, Ur, Ui, Kr, Ki, k2, n);
+        FN(axpy)(Yr, Yi, Ur, Ui, Kr, Ki, k2, n, c->nthreads);
         FN(eval_f)(c, Tr, Ti, Yr, Yi);
-        FN(axpy)(Kr, Ki, Kr, Ki, Tr, Ti, (REAL)2.0, n);
-        FN(axpy)(Yr, Yi, Ur, Ui, Tr, Ti, k2, n);
+        FN(axpy)(Kr, Ki, Kr, Ki, Tr, Ti, (REAL)2.0, n, c->nthreads);
+        FN(axpy)(Yr, Yi, Ur, Ui, Tr, Ti, k2, n, c->nthreads);
         FN(eval_f)(c, Tr, Ti, Yr, Yi);
-        FN(axpy)(Kr, Ki, Kr, Ki, Tr, Ti, (REAL)2.0, n);
-        FN(axpy)(Yr, Yi, Ur, Ui, Tr, Ti, k, n);
+        FN(axpy)(Kr, Ki, Kr, Ki, Tr, Ti, (REAL)2.0, n, c->nthreads);
+        FN(axpy)(Yr, Yi, Ur, Ui, Tr, Ti, k, n, c->nthreads);
         FN(eval_f)(c, Tr, Ti, Yr, Yi);
-        FN(axpy)(Kr, Ki, Kr, Ki, Tr, Ti, (REAL)1.0, n);
-        FN(axpy)(Ur, Ui, Ur, Ui, Kr, Ki, k6, n);
+        FN(axpy)(Kr, Ki, Kr, Ki, Tr, Ti, (REAL)1.0, n, c->nthreads);
+        FN(axpy)(Ur, Ui, Ur, Ui, Kr, Ki, k6, n, c->nthreads);
     }
 }
 

@@ -89,6 +89,26 @@ def test_oracle_matches_live_reference(ndim, method, prec, BC):
     assert bits_equal(got, ref)
 
 
+@pytest.mark.parametrize("ndim,method,prec", list(itertools.product([1, 2, 3], [1, 2], [2, 1])))
+def test_oracle_thread_count_does_not_change_bits(ndim, method, prec):
+    # The large parity runs spread one solve over threads; each grid sweep
+    # writes every point from values no other point of that sweep writes.
+    shape = {1: (301,), 2: (41, 37), 3: (19, 17, 23)}[ndim]
+    rng = np.random.default_rng(31 + 10 * ndim + method + prec)
+    U = (1 + 0.2 * rng.standard_normal(shape)) + 0.2j * rng.standard_normal(shape)
+    V = 0.1 * rng.random(shape)
+    for BC in (1, 2, 3):
+        args = (U, V, -1.0, 1.0, 0.1, BC, 4, 0.002)
+        try:
+            oracle.set_threads(1)
+            one = oracle.take_steps(*args, method=method, precision=prec)
+            oracle.set_threads(4)
+            many = oracle.take_steps(*args, method=method, precision=prec)
+        finally:
+            oracle.set_threads(1)
+        assert bits_equal(one, many), BC
+
+
 def test_oracle_rejects_bad_arguments():
     U = np.ones(8, dtype=complex)
     with pytest.raises(ValueError):
