@@ -280,6 +280,9 @@ int nlse_take_steps_noalloc(const nlse_problem *p, const double *dUr, const doub
  *                  staging, both methods) advances two z planes per
  *                  iteration (one barrier and plane wait per two points);
  *                  0: one plane.  Same bits.
+ *   "wide.ty"      tile height of that two-plane kernel: 8 (default; 32 x 8
+ *                  tiles, 4 CTAs per SM), 4 (6 CTAs per SM) or 16 (2 CTAs
+ *                  per SM): halo re-reads against CTAs in flight.  Same bits.
  *   "wide.tile_order"  order of the mixed-precision 3D interior kernel's
  *                  tiles: 1 (default) chunk by chunk (neighbouring tiles
  *                  share their halo through L2), 0 every face tile last.

@@ -88,6 +88,7 @@ SIGNATURES = {
     "nlse_solver_download_device": (_i, [_vp, _vp, _vp]),
     "nlse_solver_mass": (_i, [_vp, _dp]),
     "nlse_solver_sync": (_i, [_vp]),
+    "nlse_solver_query": (_i, [_vp, ctypes.POINTER(_i)]),
     "nlse_solver_stream": (_i, [_vp, ctypes.POINTER(_vp)]),
     "nlse_solver_set_graph_steps": (_i, [_vp, _i]),
     "nlse_solver_launches_per_step": (_i, [_vp]),
@@ -111,11 +112,13 @@ SIGNATURES = {
     "nlse_batch_download": (_i, [_vp, _i, _dp, _dp]),
     "nlse_batch_remove": (_i, [_vp, _i]),
     "nlse_batch_sync": (_i, [_vp]),
+    "nlse_batch_query": (_i, [_vp, ctypes.POINTER(_i)]),
     "nlse_batch_stats": (_i, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_ll), ctypes.POINTER(_ll)]),
     "nlse_batch_stream": (_i, [_vp, ctypes.POINTER(_vp)]),
     "nlse_batch_last_launches": (_i, [_vp]),
     "nlse_take_steps_noalloc": (_i, [ctypes.POINTER(Problem), _vp, _vp, _vp, _vp, _vp, _i,
                                      _vp]),
+    "nlse_device_fp64_rates": (_i, [_dp, _dp]),
     "nlse_tune_set": (_i, [ctypes.c_char_p, _ll]),
     "nlse_tune_get": (_i, [ctypes.c_char_p, ctypes.POINTER(_ll)]),
 }

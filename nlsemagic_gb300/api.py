@@ -263,6 +263,12 @@ class Solver:
     def sync(self):
         check(self._lib.nlse_solver_sync(self._h))
 
+    def idle(self):
+        """True when the queued steps have finished (non-blocking)."""
+        out = ctypes.c_int()
+        check(self._lib.nlse_solver_query(self._h, ctypes.byref(out)))
+        return bool(out.value)
+
     def sum_abs2(self):
         """sum over points of |U|^2, accumulated in FP64 (multiply by h^d for
         the mass)."""
@@ -339,6 +345,12 @@ class Batch:
 
     def sync(self):
         check(self._lib.nlse_batch_sync(self._h))
+
+    def idle(self):
+        """True when the queued launches have finished (non-blocking)."""
+        out = ctypes.c_int()
+        check(self._lib.nlse_batch_query(self._h, ctypes.byref(out)))
+        return bool(out.value)
 
     def remaining(self, slot):
         out = ctypes.c_longlong()

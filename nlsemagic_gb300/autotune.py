@@ -7,7 +7,9 @@ knobs and keeps the fastest:
 
 * ``wide.zc``      z-chunk length of the mixed-precision 3D kernel (planes a
                    CTA streams through; trades queue-fill overhead against the
-                   number of CTAs in flight),
+                   number of CTAs in flight; 0: the library's choice),
+* ``wide.ty``      tile height of that kernel (4, 8 or 16 rows of 32 columns:
+                   halo re-reads against CTAs in flight),
 * ``graph.steps``  RK4 steps captured per CUDA graph (launch overhead against
                    graph size; matters for small grids),
 * ``wide2d.ty``    tile height of the mixed-precision 2D stage kernel (8, 16
@@ -35,7 +37,7 @@ import numpy as np
 from . import _lib
 from .api import Solver, grid_dims
 
-KNOBS = ("wide.zc", "graph.steps", "wide2d.ty")
+KNOBS = ("wide.zc", "wide.ty", "graph.steps", "wide2d.ty")
 
 
 def set_knob(key, value):
@@ -96,16 +98,19 @@ def _smooth_state(shape, h):
 def candidates(shape, precision):
     ndim, dims = grid_dims(shape)
     cands = []
-    zcs, tys = [0], [0]
+    zcs, wtys, tys = [0], [8], [0]
     if ndim == 3 and precision == 3:
         L = dims[2]
-        zcs = sorted({z for z in (16, 32, 48, 64, 96, 128, 192, L) if 4 <= z <= L})
+        zcs = [0] + sorted({z for z in (16, 32, 64) if 4 <= z <= L})
+        wtys = [4, 8, 16]
     if ndim == 2 and precision == 3:
         tys = [8, 16, 32]
     for zc in zcs:
-        for ty in tys:
-            for gs in (4, 10, 25):
-                cands.append({"wide.zc": zc, "graph.steps": gs, "wide2d.ty": ty})
+        for wty in wtys:
+            for ty in tys:
+                for gs in (4, 10, 25):
+                    cands.append({"wide.zc": zc, "wide.ty": wty, "graph.steps": gs,
+                                  "wide2d.ty": ty})
     return cands
 
 

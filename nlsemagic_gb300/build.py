@@ -38,6 +38,7 @@ UNITS = {
     "kern_cq.cu": ["-fmad=false"],
     "kern_small_exact.cu": ["-fmad=false"],
     "kern_small_mixed.cu": [],
+    "kern_probe.cu": [],
 }
 
 
@@ -101,6 +102,28 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     with open(stamp, "w") as f:
         f.write(" ".join(extra))
     return LIB
+
+
+HARNESS_SRC = os.path.join(HERE, "harness", "nlse_harness.c")
+HARNESS = os.path.join(HERE, "harness", "nlse_harness")
+
+
+def build_harness(force: bool = False) -> str:
+    """Compile the standalone C harness (nlsemagic_gb300/harness/nlse_harness)
+    against the library's C ABI with the host C compiler; it finds the
+    library next to itself at run time (rpath $ORIGIN/..)."""
+    lib = build()
+    if force or _stale(HARNESS, [HARNESS_SRC, lib, os.path.join(INCLUDE, "nlse_gb300.h")]):
+        cc = os.environ.get("CC", "gcc")
+        tmp = HARNESS + ".tmp%d" % os.getpid()
+        cmd = [cc, "-std=gnu11", "-O2", "-Wall", "-Wextra", "-ffp-contract=off", "-I", INCLUDE,
+               HARNESS_SRC, "-o", tmp, "-L", HERE, "-lnlse_gb300", "-Wl,-rpath,$ORIGIN/..",
+               "-lm"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("harness build failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
+        os.replace(tmp, HARNESS)
+    return HARNESS
 
 
 if __name__ == "__main__":

@@ -18,6 +18,8 @@ int g_tile_order = 1;
 // 3D 2SHOC interior kernel (TMA staging): two planes per iteration.  Same
 // bits as one plane; 23.6 Gpt-steps/s at 320^3 against 21.9.
 int g_z2 = 1;
+// tile height of the two-plane interior kernel (4, 8 or 16 rows of 32)
+int g_wide_ty = 8;
 // 2D grids (BC 1-3): one single-pass stage kernel per stage (kern_wide2d.cuh)
 int g_wide2d = 1;
 // 1D grids (BC 1-3) above the single-block size: one staged-segment launch

@@ -457,9 +457,9 @@ __global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3
 // the slots of planes zA-4, zA-3 -- last read at iteration j-2 (a plane is
 // last read at the iteration that advances it), so the barrier of iteration
 // j-1 orders the refill after every read -- with planes zA+4, zA+5.
-template <int METHOD>
+template <int METHOD, int TY_>
 struct WShape2 {
-  static constexpr int TX = 32, TY = NLSE_WIDE_TY, NT = TX * TY, H = METHOD == 2 ? 2 : 1, XO = 2;
+  static constexpr int TX = 32, TY = TY_, NT = TX * TY, H = METHOD == 2 ? 2 : 1, XO = 2;
   static constexpr int PX = TX + 4, PY = TY + 2 * H, NU = 8;
   static constexpr int PLANE = round_up(PX * PY * 8, 128);
   static constexpr int SLOT = 2 * PLANE;
@@ -468,13 +468,22 @@ struct WShape2 {
   static constexpr unsigned TX_BYTES = (unsigned)(2 * PX * PY * 8);
 };
 
-template <int METHOD, int STAGE>
-__global__ void __launch_bounds__(32 * NLSE_WIDE_TY, NLSE_WIDE_MIN_BLOCKS) wide3d_z2(
+// Tile heights of the two-plane kernel, chosen at run time (knob "wide.ty"),
+// with the CTAs per SM each is compiled for: 32 x 8 tiles 4 per SM and 32 x
+// 16 tiles 2 (64 registers a thread); 32 x 4 tiles 6 (80 registers; the
+// 8-slot ring of 37 KB allows no more in 228 KB).
+template <int TY>
+constexpr int z2_min_blocks() {
+  return TY == 4 ? 6 : (TY == 16 ? 2 : 4);
+}
+
+template <int METHOD, int STAGE, int TY>
+__global__ void __launch_bounds__(32 * TY, z2_min_blocks<TY>()) wide3d_z2(
     Geom g, Args A, int zc, TileOrder to, GhostLayout gl, const __grid_constant__ CUtensorMap tm0,
     const __grid_constant__ CUtensorMap tm1) {
-  typedef WShape2<METHOD> SH;
+  typedef WShape2<METHOD, TY> SH;
   typedef mixed::HE HE;
-  constexpr int TX = SH::TX, TY = SH::TY, H = SH::H, XO = SH::XO, PX = SH::PX, NU = SH::NU;
+  constexpr int TX = SH::TX, H = SH::H, XO = SH::XO, PX = SH::PX, NU = SH::NU;
 
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned long long* bars = reinterpret_cast<unsigned long long*>(smem + SH::B_OFF);
@@ -986,10 +995,9 @@ inline int sm_count() {
 // resident CTAs (measured at 320^3 with 4 CTAs per SM: chunks of 16-32
 // planes ran 12-14% faster than the 2-3 waves a load-balance model
 // prefers), and at least 16 planes so the 2H-plane queue fill stays small.
-inline int default_zc(const Geom& g, int H, int occ) {
+inline int default_zc(const Geom& g, int H, int occ, int ty) {
   (void)H;
-  const long long cols =
-      (long long)((g.M + 31) / 32) * ((g.N + NLSE_WIDE_TY - 1) / NLSE_WIDE_TY);
+  const long long cols = (long long)((g.M + 31) / 32) * ((g.N + ty - 1) / ty);
   const long long want = 8LL * sm_count() * (occ > 0 ? occ : 1);
   long long nbz = (want + cols - 1) / cols;
   if (nbz < 1) nbz = 1;
@@ -1037,11 +1045,11 @@ inline TileOrder tile_order(const Geom& g, int TX, int TY, int H, int zc) {
 
 extern int g_z2;  // TMA staging: two planes per iteration (1) or one (0)
 
-template <int METHOD, int STAGE>
+template <int METHOD, int STAGE, int TY>
 cudaError_t launch_inner_z2(const Geom& g, const Args& A, cudaStream_t st, const CUtensorMap& m0,
                             const CUtensorMap& m1) {
-  typedef WShape2<METHOD> SH;
-  auto kern = wide3d_z2<METHOD, STAGE>;
+  typedef WShape2<METHOD, TY> SH;
+  auto kern = wide3d_z2<METHOD, STAGE, TY>;
   static int occ = 0;
   if (!occ) {
     cudaError_t e =
@@ -1050,7 +1058,7 @@ cudaError_t launch_inner_z2(const Geom& g, const Args& A, cudaStream_t st, const
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, SH::NT, SH::SMEM);
     if (e != cudaSuccess || occ < 1) occ = 1;
   }
-  const int zc = g_zc_override > 0 ? g_zc_override : default_zc(g, SH::H, occ);
+  const int zc = g_zc_override > 0 ? g_zc_override : default_zc(g, SH::H, occ, SH::TY);
   const TileOrder to = tile_order(g, SH::TX, SH::TY, SH::H, zc);
   const unsigned nb = (unsigned)to.nbx * (unsigned)to.nby * (unsigned)to.nbz;
   return launch_k(kern, dim3(nb), dim3(SH::TX, SH::TY), SH::SMEM, st, g_pdl != 0, g, A, zc, to,
@@ -1070,23 +1078,42 @@ cudaError_t launch_inner(const Geom& g, const Args& A, cudaStream_t st, const CU
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, SH::NT, SH::SMEM);
     if (e != cudaSuccess || occ < 1) occ = 1;
   }
-  const int zc = g_zc_override > 0 ? g_zc_override : default_zc(g, SH::H, occ);
+  const int zc = g_zc_override > 0 ? g_zc_override : default_zc(g, SH::H, occ, SH::TY);
   const TileOrder to = tile_order(g, SH::TX, SH::TY, SH::H, zc);
   const unsigned nb = (unsigned)to.nbx * (unsigned)to.nby * (unsigned)to.nbz;
   return launch_k(kern, dim3(nb), dim3(SH::TX, SH::TY), SH::SMEM, st, METHOD == 2 && g_pdl, g, A,
                   zc, to, GhostLayout(g), m0, m1);
 }
 
+extern int g_wide_ty;  // tile height of the two-plane kernel: 4, 8 (default) or 16
+
+template <int METHOD, int TY>
+cudaError_t launch_z2_stage(const Geom& g, const Args& A, cudaStream_t st, const CUtensorMap& m0,
+                            const CUtensorMap& m1) {
+  switch (A.stage) {
+    case 1: return launch_inner_z2<METHOD, 1, TY>(g, A, st, m0, m1);
+    case 2: return launch_inner_z2<METHOD, 2, TY>(g, A, st, m0, m1);
+    case 3: return launch_inner_z2<METHOD, 3, TY>(g, A, st, m0, m1);
+    case 4: return launch_inner_z2<METHOD, 4, TY>(g, A, st, m0, m1);
+  }
+  return cudaErrorInvalidValue;
+}
+
+// Rows of the staged planes (tile height + 2 H) of the interior kernel the
+// launch below picks: the TMA boxes are built for it.
+template <int METHOD>
+inline int staged_rows() {
+  const int H = METHOD == 2 ? 2 : 1;
+  return (g_z2 ? g_wide_ty : NLSE_WIDE_TY) + 2 * H;
+}
+
 template <int METHOD, bool TMA>
 cudaError_t launch_inner_stage(const Geom& g, const Args& A, cudaStream_t st,
                                const CUtensorMap& m0, const CUtensorMap& m1) {
   if (TMA && g_z2) {
-    switch (A.stage) {
-      case 1: return launch_inner_z2<METHOD, 1>(g, A, st, m0, m1);
-      case 2: return launch_inner_z2<METHOD, 2>(g, A, st, m0, m1);
-      case 3: return launch_inner_z2<METHOD, 3>(g, A, st, m0, m1);
-      case 4: return launch_inner_z2<METHOD, 4>(g, A, st, m0, m1);
-    }
+    if (g_wide_ty == 4) return launch_z2_stage<METHOD, 4>(g, A, st, m0, m1);
+    if (g_wide_ty == 16) return launch_z2_stage<METHOD, 16>(g, A, st, m0, m1);
+    return launch_z2_stage<METHOD, 8>(g, A, st, m0, m1);
   }
   switch (A.stage) {
     case 1: return launch_inner<METHOD, 1, TMA>(g, A, st, m0, m1);
@@ -1124,8 +1151,9 @@ cudaError_t launch(const Geom& g, const Args& A, cudaStream_t st) {
     memset(&m0, 0, sizeof(m0));
     memset(&m1, 0, sizeof(m1));
     const void* ein = A.stage == 1 ? (const void*)A.a.lo_in : (const void*)A.a.e_in;
-    bool tma = tiled::make_map(&m0, A.a.hi_in, g, 1, SH::PX, SH::PY) &&
-               tiled::make_map(&m1, ein, g, 1, SH::PX, SH::PY);
+    const int py = staged_rows<METHOD>();
+    bool tma = tiled::make_map(&m0, A.a.hi_in, g, 1, SH::PX, py) &&
+               tiled::make_map(&m1, ein, g, 1, SH::PX, py);
     cudaError_t e = tma ? launch_inner_stage<METHOD, true>(g, A, st, m0, m1)
                         : launch_inner_stage<METHOD, false>(g, A, st, m0, m1);
     if (e != cudaSuccess) return e;

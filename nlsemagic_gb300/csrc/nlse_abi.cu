@@ -59,6 +59,7 @@ extern int g_pdl;
 extern int g_face_bps;
 extern int g_tile_order;
 extern int g_z2;
+extern int g_wide_ty;
 extern int g_wide2d;
 extern int g_seg1d;
 }
@@ -108,6 +109,12 @@ extern "C" int nlse_tune_set(const char* key, long long value) {
   if (!strcmp(key, "wide.z2")) {
     if (value != 0 && value != 1) return fail(NLSE_ERR_ARG, "wide.z2 must be 0 or 1");
     nlse::wide::g_z2 = (int)value;
+    return NLSE_OK;
+  }
+  if (!strcmp(key, "wide.ty")) {
+    if (value != 4 && value != 8 && value != 16)
+      return fail(NLSE_ERR_ARG, "wide.ty must be 4, 8 or 16");
+    nlse::wide::g_wide_ty = (int)value;
     return NLSE_OK;
   }
   if (!strcmp(key, "wide.tile_order")) {
@@ -162,6 +169,10 @@ extern "C" int nlse_tune_get(const char* key, long long* value) {
   }
   if (!strcmp(key, "wide.z2")) {
     *value = nlse::wide::g_z2;
+    return NLSE_OK;
+  }
+  if (!strcmp(key, "wide.ty")) {
+    *value = nlse::wide::g_wide_ty;
     return NLSE_OK;
   }
   if (!strcmp(key, "wide.tile_order")) {
@@ -258,8 +269,6 @@ static Consts<double> consts_double(const nlse_problem* p) {
   c.k = k;
   c.k2 = k / 2.0;
   c.k6 = k / 6.0;
-  c.kinv = 1.0 / k;
-  c.kinv2 = 2.0 / k;
   c.a12lh2 = a / (12.0 * h2);
   c.h2 = h2;
   c.msd_guard = (p->flags & NLSE_FLAG_MSD_GUARD) ? 1 : 0;
@@ -289,8 +298,6 @@ static Consts<float> consts_single(const nlse_problem* p) {
   c.k = k;
   c.k2 = k / 2.0f;
   c.k6 = k / 6.0f;
-  c.kinv = 1.0f / k;
-  c.kinv2 = 2.0f / k;
   c.h2 = h2;
   c.msd_guard = (p->flags & NLSE_FLAG_MSD_GUARD) ? 1 : 0;
   return c;
@@ -310,11 +317,13 @@ static Consts<float> consts_mixed(const nlse_problem* p) {
   c.a112 = (float)d.a112;
   c.a_6h2 = (float)d.a_6h2;
   c.a_12 = (float)d.a_12;
+  // k and k/2 as FP32 pairs hi + lo (the RK4 update of the mixed path
+  // multiplies by both parts)
   c.k = (float)d.k;
+  c.k_lo = (float)(d.k - (double)c.k);
   c.k2 = (float)d.k2;
+  c.k2_lo = (float)(d.k2 - (double)c.k2);
   c.k6 = (float)d.k6;
-  c.kinv = (float)d.kinv;
-  c.kinv2 = (float)d.kinv2;
   c.a12lh2 = (float)d.a12lh2;
   c.h2 = (float)d.h2;
   c.msd_guard = d.msd_guard;
@@ -730,6 +739,18 @@ extern "C" int nlse_solver_set_graph_steps(nlse_solver* s, int steps) {
 extern "C" int nlse_solver_sync(nlse_solver* s) {
   if (!s) return fail(NLSE_ERR_ARG, "solver is NULL");
   CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return device_error_check();
+}
+
+extern "C" int nlse_solver_query(nlse_solver* s, int* idle) {
+  if (!s || !idle) return fail(NLSE_ERR_ARG, "NULL argument");
+  cudaError_t e = cudaStreamQuery(s->stream);
+  if (e == cudaErrorNotReady) {
+    *idle = 0;
+    return NLSE_OK;
+  }
+  CUDA_TRY(e);
+  *idle = 1;
   return device_error_check();
 }
 

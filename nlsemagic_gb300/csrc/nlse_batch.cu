@@ -773,6 +773,17 @@ extern "C" int nlse_batch_sync(nlse_batch* b) {
   return NLSE_OK;
 }
 
+extern "C" int nlse_batch_query(nlse_batch* b, int* idle) {
+  if (!b || !idle) return nlse::set_error(NLSE_ERR_ARG, "NULL argument");
+  cudaError_t e = cudaStreamQuery(b->stream);
+  if (e == cudaErrorNotReady) {
+    *idle = 0;
+    return NLSE_OK;
+  }
+  *idle = 1;
+  return nlse_batch_sync(b);  // returns at once; reports a failed launch
+}
+
 extern "C" int nlse_batch_remaining(nlse_batch* b, int slot, long long* steps_left) {
   if (!b || !steps_left || slot < 0 || slot >= (int)b->slots.size() || !b->slots[slot].used)
     return nlse::set_error(NLSE_ERR_ARG, "bad slot");

@@ -33,7 +33,9 @@ struct Consts {
   R a76, a112;         // 1D 2SHOC: a*(7/6), a*(1/12)
   R a_6h2, a_12;       // 2D: a*(1/(6 h2)), a*(1/12); 3D: a/(6 h2), a/12
   R k, k2, k6;         // k, k/2, k/6
-  R kinv, kinv2;       // 1/k, 2/k (mixed path only)
+  // Mixed path: the low parts of k and k/2, so that both enter the RK4 update
+  // as FP32 pairs hi + lo (nlse_mixed.cuh).
+  R k_lo, k2_lo;
   R a12lh2;            // a/(12 h2) (mixed path, wide fourth-order form)
   R h2;                // h^2 (mixed path, 2SHOC ghost values)
   int msd_guard;       // MSD zero-neighbour guard
@@ -46,7 +48,7 @@ struct StageBufs {
   void* psi;      // C2<R>[n]   (mixed: hi part, float2)
   void* psi_lo;   // mixed only: low part, float2[n]
   const void* V;  // R[n] (mixed: float)
-  void* K;        // C2<R>[n]   RK4 accumulator (mixed: float2, holds K1+2K2)
+  void* K;        // C2<R>[n]   RK4 accumulator (mixed: float2, holds k (K1/2 + K2))
   void* ya;       // C2<R>[n]   stage state ping (mixed: stage delta d, float2)
   void* yb;       // C2<R>[n]   stage state pong
 };

@@ -225,30 +225,42 @@ __device__ __forceinline__ void comp_add(float& hi, float& lo, float inc) {
 }
 
 // ---- RK4 stage update of the mixed path -------------------------------------
-// Each stage stores the next E (= lo + d) rather than d itself, so the stencil
-// of every stage reads two planes (hi, E); d is recovered as E - lo.  K1 and
-// K3 are recovered from d_2 and d_4, so the only accumulator written is
-// K12 = K1 + 2 K2 (stage 2):
-//   1: E' = lo + k/2 T
-//   2: K = (E - lo)(2/k) + 2 T;   E' = lo + k/2 T
-//   3: E' = lo + k T
-//   4: psi_out = psi + k/6 (K + 2 (E - lo)(1/k) + T)   (compensated)
+// Each stage stores the next E (= lo + d, d the stage's state increment)
+// rather than d itself, so the stencil of every stage reads two planes
+// (hi, E); d is recovered as E - lo.  The update works in increment units:
+// the one accumulator written holds S = d_2 + k T_2 = k (K1/2 + K2), and no
+// value is scaled by 1/k and back.  The time step enters only as FP32 pairs
+// hi + lo (k, k/2 and 1/3): rounding these constants once to FP32
+// would change the effective time step by up to ~6e-8 relative, a bias that
+// repeats every step, so the phase error it causes grows linearly with time
+// (it was the largest error of this class on the benchmark solves).
+//   1: E' = lo + (k/2) T                     (d_2 = k/2 K1)
+//   2: S = (E - lo) + k T;  E' = lo + (k/2) T  (d_3 = k/2 K2)
+//   3: E' = lo + k T                         (d_4 = k K3)
+//   4: psi_out = psi + (S + (E - lo) + (k/2) T) / 3   (compensated)
+//              = psi + k/6 (K1 + 2 K2 + 2 K3 + K4)
 // e is E of this stage at the point (unused in stage 1), Kv the accumulator
 // (stage 4).  Writes eo (stages 1-3), Ko (stage 2) or (hio, loo) (stage 4).
+// (hi + lo) x + acc, the small product first
+__device__ __forceinline__ float2 pair_fma(float hi, float lo, float2 x, float2 acc) {
+  return pfma(P2(hi), x, pfma(P2(lo), x, acc));
+}
+
 __device__ __forceinline__ void stage_update(const Consts<float>& c, int stage, float2 T,
                                              float2 hi, float2 lo, float2 e, float2 Kv,
                                              float2& eo, float2& Ko, float2& hio, float2& loo) {
   if (stage == 1) {
-    eo = pfma(P2(c.k2), T, lo);
+    eo = pair_fma(c.k2, c.k2_lo, T, lo);
   } else if (stage == 2) {
-    Ko = pfma(psub(e, lo), P2(c.kinv2), pmul(P2(2.f), T));
-    eo = pfma(P2(c.k2), T, lo);
+    Ko = pair_fma(c.k, c.k_lo, T, psub(e, lo));
+    eo = pair_fma(c.k2, c.k2_lo, T, lo);
   } else if (stage == 3) {
-    eo = pfma(P2(c.k), T, lo);
+    eo = pair_fma(c.k, c.k_lo, T, lo);
   } else {
-    float2 d = psub(e, lo);
-    float2 kt = pfma(P2(2.f), pmul(d, P2(c.kinv)), padd(Kv, T));
-    float2 inc = pmul(P2(c.k6), kt);
+    // (S + d_4 + (k/2) T) / 3, the division as a multiplication by the FP32
+    // pair of 1/3 (0x1.555556p-2 - 0x1.555556p-27, 1/3 to 8.9e-16 relative)
+    const float2 y = pair_fma(c.k2, c.k2_lo, T, padd(Kv, psub(e, lo)));
+    const float2 inc = pfma(P2(0x1.555556p-2f), y, pmul(P2(-0x1.555556p-27f), y));
     hio = hi;
     loo = lo;
     comp_add(hio.x, loo.x, inc.x);

@@ -102,6 +102,8 @@ def test_autotune_candidates_per_class():
     assert all(c["wide.zc"] == 0 for c in two)
     three = autotune.candidates((64, 64, 64), 3)
     assert {c["wide2d.ty"] for c in three} == {0} and len({c["wide.zc"] for c in three}) > 1
+    assert {c["wide.ty"] for c in three} == {4, 8, 16}
+    assert {c["wide.ty"] for c in two} == {8}
     assert all(set(c) == set(autotune.KNOBS) for c in two + three)
 
 

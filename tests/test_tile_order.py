@@ -1,8 +1,8 @@
 """Tile order of the mixed-precision 3D interior kernel (host-side check, no
-GPU): the launch enumerates every tile exactly once, and the tiles it places
-first -- those that start without waiting for the face kernels before them
--- stage no face point and no ghost value (their tile, 2-cell halo and the
-chunk's planes +-2 all lie in [1, n-2]).  Compiled with nvcc as host code
+GPU), for each of its tile heights: the launch enumerates every tile exactly
+once, and the tiles it places first -- those that start without waiting for
+the face kernels before them -- stage no face point and no ghost value
+(their tile, 2-cell halo and the chunk's planes +-2 all lie in [1, n-2]).  Compiled with nvcc as host code
 from the kernel's own header."""
 import os
 import shutil
@@ -14,12 +14,12 @@ SRC = r'''
 #include "kern_wide.cuh"
 #include <cstdio>
 #include <vector>
-namespace nlse { namespace wide { int g_tile_order = 1; int g_pdl = 1; int g_face_bps = 8; int g_zc_override = 0; } }
+namespace nlse { namespace wide { int g_tile_order = 1; int g_pdl = 1; int g_face_bps = 8; int g_zc_override = 0; int g_z2 = 1; int g_wide_ty = 8; } }
 using namespace nlse;
 using namespace nlse::wide;
-int check(int M, int N, int L, int zc, int cm) {
+int check(int M, int N, int L, int zc, int cm, int TY) {
   Geom g; g.ndim = 3; g.M = M; g.N = N; g.L = L; g.n = (long long)M * N * L;
-  const int TX = 32, TY = NLSE_WIDE_TY, H = 2;
+  const int TX = 32, H = 2;
   TileOrder t = tile_order(g, TX, TY, H, zc);
   t.chunk_major = cm;
   const long long nb = (long long)t.nbx * t.nby * t.nbz;
@@ -47,11 +47,15 @@ int main() {
   for (int M : dims) for (int N : dims) for (int L : {3, 4, 5, 8, 9, 20, 37, 64, 320})
     for (int zc : zcs) {
       if (zc > L) continue;
-      for (int cm = 0; cm < 2; ++cm) {
-        int r = check(M, N, L, zc, cm);
-        if (r) { printf("FAIL %d %d %d %d order %d code %d\n", M, N, L, zc, cm, r); return 1; }
-        ++n;
-      }
+      for (int cm = 0; cm < 2; ++cm)
+        for (int ty : {4, 8, 16}) {  // the tile heights of the interior kernel
+          int r = check(M, N, L, zc, cm, ty);
+          if (r) {
+            printf("FAIL %d %d %d %d order %d ty %d code %d\n", M, N, L, zc, cm, ty, r);
+            return 1;
+          }
+          ++n;
+        }
     }
   printf("OK %lld\n", n);
   return 0;
