@@ -48,6 +48,23 @@ UNIT = "Gpt-steps/s"
 BYTES_MODEL_MIXED = 240.0
 BYTES_DESIGN_MIXED = 160.0
 BYTES_FP64 = 304.0
+# FP64 instructions per interior grid-point-step of the exact FP64 class,
+# counted from the reference expressions (each +, -, x one instruction; the
+# reference operation order forbids contraction): 3D 2SHOC per stage D 16,
+# F 57 (the |U|^2 term shared by both components), update 7 -> 80 x 4; 2D
+# 2SHOC D 12, F 35, update 7 -> 54 x 4 (src/NLSEmagic3D/NLSE3D_TAKE_STEPS_2SHOC.c:
+# 56-72, 233-262; src_old/NLSE2D_v1/NLSE2D_TAKE_STEPS_2SHOC.c:59-67, 169-187).
+FP64_OPS = {(3, 2): 320.0, (2, 2): 216.0}
+# The timed CPU arm is the C restatement of the reference integrator (the
+# reference's own build cannot travel to an aarch64 host).  Both were timed
+# side by side on one x86-64 core (320^3, one RK4 step of FP64 2SHOC MSD, the
+# reference built with its own -O3 -funroll-loops through the mex shim): the
+# restatement took 9.2-11.0 s, the reference 12.0-15.3 s, with identical
+# bits.  The restatement is the faster of the two, so the CPU figure is not
+# understated by the substitution.
+PORT_VS_REFERENCE = {"grid": "320^3", "rk4_steps": 1, "threads": 1, "host": "x86-64 Xeon 2.7 GHz",
+                     "port_s": [9.2, 11.0], "reference_s": [12.0, 15.3],
+                     "same_bits": True}
 
 
 def log(*a):
@@ -198,6 +215,28 @@ def cpu_sample(w, steps, threads, precision=2):
     return pts / wall / 1e9, wall
 
 
+def host_cpu():
+    """Model and core count of the host, from lscpu (else /proc/cpuinfo and
+    os.cpu_count())."""
+    info = {"cores": os.cpu_count(), "model": None, "arch": None}
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        kv = {}
+        for ln in out.splitlines():
+            if ":" in ln:
+                k, v = ln.split(":", 1)
+                kv[k.strip()] = v.strip()
+        info["model"] = kv.get("Model name") or kv.get("Vendor ID")
+        info["arch"] = kv.get("Architecture")
+        if kv.get("CPU(s)", "").isdigit():
+            info["cores"] = int(kv["CPU(s)"])
+        if kv.get("Socket(s)", "").isdigit() and kv.get("Core(s) per socket", "").isdigit():
+            info["physical_cores"] = int(kv["Socket(s)"]) * int(kv["Core(s) per socket"])
+    except Exception:
+        pass
+    return info
+
+
 def cpu_threads_for(w):
     n = os.cpu_count() or 1
     try:
@@ -209,6 +248,23 @@ def cpu_threads_for(w):
     if avail:
         n = max(1, min(n, int(0.6 * avail // per)))
     return min(n, 64)
+
+
+def tune_for(args, shape, method, precision, BC):
+    """Launch knobs for this problem class from the autotuner
+    (nlsemagic_gb300/autotune.py: tuned once per device and class, cached),
+    applied before the solvers are created; returns the knobs in force."""
+    from nlsemagic_gb300 import autotune
+    entry = None
+    if args.tune:
+        t0 = time.perf_counter()
+        entry = autotune.tune(shape, method=method, precision=precision, BC=BC, steps=20)
+        autotune.apply(shape, method=method, precision=precision, BC=BC)
+        log("autotune %s: %s (%.1f s)" % (list(shape), json.dumps(entry),
+                                          time.perf_counter() - t0))
+    knobs = {k: autotune.get_knob(k) for k in autotune.KNOBS + ("wide.pdl",)}
+    knobs["source"] = "autotuner" if entry else "library defaults"
+    return knobs
 
 
 def run_reference(args, w):
@@ -238,7 +294,8 @@ def run_reference(args, w):
                    "bc": "MSD", "rk4_steps_per_sample": steps_per_sample,
                    "precision": "fp64 (reference CPU integrator)"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": sample},
+                         "sample": sample, "host_cpu": host_cpu(),
+                         "port_vs_reference": PORT_VS_REFERENCE},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -266,9 +323,11 @@ def run_gpu(args, w):
     Ur = torch.from_numpy(np.ascontiguousarray(w.U.real.ravel(order="F"))).cuda()
     Ui = torch.from_numpy(np.ascontiguousarray(w.U.imag.ravel(order="F"))).cuda()
     Vd = torch.from_numpy(np.ascontiguousarray(w.V.ravel(order="F"))).cuda()
+    tuned = tune_for(args, w.U.shape, w.method, prec, w.BC)
     solver = ng.Solver(w.U.shape, method=w.method, precision=prec, BC=w.BC, s=w.s, a=w.a,
                        h2=w.h2, k=w.k)
-    solver.set_graph_steps(args.graph_steps)
+    if args.graph_steps > 0:
+        solver.set_graph_steps(args.graph_steps)
     stream = torch.cuda.ExternalStream(solver.stream)
 
     def job():
@@ -348,12 +407,13 @@ def run_gpu(args, w):
     if fp64_steps > 0 and rank == 0:
         s64 = ng.Solver(w.U.shape, method=w.method, precision=ng.PREC_DOUBLE, BC=w.BC, s=w.s,
                         a=w.a, h2=w.h2, k=w.k)
-        s64.set_graph_steps(args.graph_steps)
+        if args.graph_steps > 0:
+            s64.set_graph_steps(args.graph_steps)
         smx = ng.Solver(w.U.shape, method=w.method, precision=prec, BC=w.BC, s=w.s, a=w.a,
                         h2=w.h2, k=w.k)
         st64 = torch.cuda.ExternalStream(s64.stream)
         s64.upload_device(Ur.data_ptr(), Ui.data_ptr(), Vd.data_ptr())
-        s64.run(max(1, args.graph_steps))  # captures the graph outside the timed run
+        s64.run(max(1, args.graph_steps, 8))  # captures the graph outside the timed run
         s64.sync()
         s64.upload_device(Ur.data_ptr(), Ui.data_ptr(), Vd.data_ptr())
         e0 = torch.cuda.Event(enable_timing=True)
@@ -374,8 +434,19 @@ def run_gpu(args, w):
                 "roofline_frac_of_measured_hbm": float(n) * fp64_steps * BYTES_FP64 / t64 /
                 1e9 / peaks()[0],
                 "mass_rel_drift": abs(m64 - mass0) / mass0,
-                "mixed_rel_l2_vs_fp64": err,
-                "mixed_rel_l2_tolerance": 1e-6}
+                "mixed_rel_l2_vs_oracle_fp64": err,
+                "mixed_rel_l2_tolerance": 1e-6,
+                "fp64_bit_identical_to_oracle": "by test (tests/test_config_parity_gpu.py, "
+                                                "this grid, all 500 steps)"}
+        try:
+            rates = fp64_rates()
+            ops = FP64_OPS[(3, w.method)]
+            fp64["fp64_rates"] = rates
+            fp64["fp64_ops_per_point_step"] = ops
+            fp64["fp64_issue_frac_of_measured_add_rate"] = fp64["value"] * 1e9 * ops / \
+                rates["add_per_s"]
+        except Exception as e:  # the probe is a report, not the measurement
+            fp64["fp64_rates"] = {"error": str(e)}
         s64.close()
         smx.close()
 
@@ -409,7 +480,7 @@ def run_gpu(args, w):
                    "precision": "mixed (FP32 stages, compensated FP32 hi/lo state)",
                    "parallelism": "replicas x%d" % world,
                    "l2": "inputs (~1.9 GB working set) larger than L2; no flush",
-                   "graph_steps": args.graph_steps},
+                   "launch_knobs": tuned},
         "roofline": roof,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 3 * 8 * n,
                 "d2h_bytes_per_step": 2 * 8 * n,
@@ -433,7 +504,8 @@ def run_gpu(args, w):
             "value": v, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": "%d RK4 step(s) of the %s solve per thread (FP64 2SHOC), %d threads, C "
                       "oracle port of NLSE3D_TAKE_STEPS_2SHOC.c, %.1f s wall" % (
-                          args.cpu_sample_steps, w.name, threads, wall)}
+                          args.cpu_sample_steps, w.name, threads, wall),
+            "host_cpu": host_cpu(), "port_vs_reference": PORT_VS_REFERENCE}
     if rank == 0:
         print(json.dumps(result), flush=True)
     solver.close()
@@ -499,24 +571,107 @@ def run_batched(args):
             "speedup": v_batch / v_seq}
 
 
+def oracle_trajectory(w, marks, precision):
+    """The C oracle's state after each number of RK4 steps in marks (chained
+    calls, same bits as one call), the solve spread over the host's cores."""
+    import oracle
+    oracle.set_threads(os.cpu_count() or 1)
+    out, U, done = {}, w.U, 0
+    try:
+        for m in marks:
+            U = oracle.take_steps(U, w.V, w.s, w.a, w.h2, w.BC, m - done, w.k, method=w.method,
+                                  precision=precision, flags=oracle.MSD_GUARD)
+            done = m
+            out[m] = U
+    finally:
+        oracle.set_threads(1)
+    return out
+
+
+def fp64_rates():
+    """Measured FP64 issue rates of this GPU (nlse_device_fp64_rates)."""
+    import ctypes
+
+    import nlsemagic_gb300 as ng
+    fma, add = ctypes.c_double(), ctypes.c_double()
+    ng._lib.check(ng.load().nlse_device_fp64_rates(ctypes.byref(fma), ctypes.byref(add)))
+    return {"fma_per_s": fma.value, "add_per_s": add.value,
+            "fma_tflops": 2 * fma.value / 1e12,
+            "how": "timed kernel, 8 independent chains per thread, 16 blocks of 256 per SM"}
+
+
+def fp64_solve(w, steps, graph_steps=10):
+    """Gpt-steps/s of the exact FP64 class on workload w (resident solver,
+    graphs, CUDA events on the solver stream) and its final state."""
+    import torch
+
+    import nlsemagic_gb300 as ng
+    with ng.Solver(w.U.shape, method=w.method, precision=ng.PREC_DOUBLE, BC=w.BC, s=w.s, a=w.a,
+                   h2=w.h2, k=w.k) as sv:
+        sv.set_graph_steps(graph_steps)
+        sv.upload(w.U, w.V)
+        sv.run(max(1, min(steps, graph_steps)))  # captures the graph
+        sv.sync()
+        sv.upload(w.U, w.V)
+        st = torch.cuda.ExternalStream(sv.stream)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        sv.run(steps)
+        e1.record(st)
+        e1.synchronize()
+        t = e0.elapsed_time(e1) / 1000.0
+        return float(w.points) * steps / t / 1e9, sv.download()
+
+
+def run_fp64(args):
+    """The exact FP64 class against its compute bound: the vortex-ring solve
+    (--grid, --fp64-steps RK4 steps) and the dark-vortex solve (--grid2d,
+    200 steps), Gpt-steps/s and the fraction of the measured FP64 add rate
+    their instruction counts imply."""
+    from nlsemagic_gb300 import workloads as W
+    rates = fp64_rates()
+    out = {"fp64_rates": rates}
+    steps3 = args.fp64_steps if args.fp64_steps > 0 else 20
+    for name, w, steps in (("3d_2shoc", W.vortex_rings_3d(n=args.grid, method=2), steps3),
+                           ("2d_2shoc", W.dark_vortices_2d(n=args.grid2d), 200)):
+        v, _ = fp64_solve(w, steps)
+        ops = FP64_OPS[(w.ndim, w.method)]
+        out[name] = {"workload": w.name, "rk4_steps": steps, "value": v, "unit": UNIT,
+                     "fp64_ops_per_point_step": ops,
+                     "fp64_issue_frac_of_measured_add_rate": v * 1e9 * ops / rates["add_per_s"],
+                     "hbm_frac_of_measured": v * BYTES_FP64 / peaks()[0]}
+        log("%s: %s" % (name, json.dumps(out[name])))
+    return out
+
+
 def run_configs(args):
     """The reference's CPU-runnable case and its 2D case, through resident
     solvers (graph-captured chunks), in every precision class: configuration
     1 (1D CD grey soliton, 1024 points, 1000 steps) and configuration 2 (2D
     2SHOC dark vortices, 512^2 unless --grid2d, 2000 steps unless
     --config2-steps).  Gpt-steps/s per class, timed after a warm-up run that
-    captures the graphs, and the FP32 / mixed results' relative L2 distance
-    to the FP64 result."""
+    captures the graphs; every class's result against the C oracle (FP64 and
+    FP32 bit for bit, relative L2 distance to the FP64 oracle) and the mixed
+    class's distance at checkpoints through the run."""
     import nlsemagic_gb300 as ng
     from nlsemagic_gb300 import workloads as W
     w1 = W.grey_soliton_1d()
     w2 = W.dark_vortices_2d(n=args.grid2d, steps=args.config2_steps)
     out = {}
     for name, w, steps in (("config1", w1, w1.steps), ("config2", w2, args.config2_steps)):
-        res = {"workload": w.name, "rk4_steps": steps}
-        final = {}
+        marks = sorted({max(1, steps // 8), max(1, steps // 4), max(1, steps // 2), steps})
+        t0 = time.perf_counter()
+        ref = oracle_trajectory(w, marks, 2)
+        ref32 = oracle_trajectory(w, [steps], 1)[steps]
+        t_oracle = time.perf_counter() - t0
+        res = {"workload": w.name, "rk4_steps": steps,
+               "oracle": "C oracle (FP64 and FP32, bit-identical to the reference C "
+                         "integrators), %d host threads, %.1f s" % (os.cpu_count() or 1, t_oracle)}
+        mass0 = W.mass(w.U, w.h, w.ndim)
         for prec, label in ((ng.PREC_DOUBLE, "fp64"), (ng.PREC_MIXED, "mixed"),
                             (ng.PREC_SINGLE, "fp32")):
+            knobs = tune_for(args, w.U.shape, w.method, prec, w.BC)
             with ng.Solver(w.U.shape, method=w.method, precision=prec, BC=w.BC, s=w.s, a=w.a,
                            h2=w.h2, k=w.k) as sv:
                 sv.upload(w.U, w.V)
@@ -527,11 +682,25 @@ def run_configs(args):
                 sv.run(steps)
                 sv.sync()
                 t = time.perf_counter() - t0
-                final[label] = sv.download()
-                res[label] = {"value": w.U.size * steps / t / 1e9, "unit": UNIT,
-                              "launches_per_step": sv.launches_per_step}
-        for label in ("mixed", "fp32"):
-            res[label]["rel_l2_vs_fp64"] = W.rel_l2(final[label], final["fp64"])
+                final = sv.download()
+                r = {"value": w.U.size * steps / t / 1e9, "unit": UNIT,
+                     "launches_per_step": sv.launches_per_step, "launch_knobs": knobs,
+                     "rel_l2_vs_oracle_fp64": W.rel_l2(final, ref[steps]),
+                     "mass_rel_drift": abs(W.mass(final, w.h, w.ndim) - mass0) / mass0}
+                if label == "fp64":
+                    r["bit_identical_to_oracle"] = bool(np.array_equal(final, ref[steps]))
+                elif label == "fp32":
+                    r["bit_identical_to_fp32_oracle"] = bool(np.array_equal(final, ref32))
+                else:
+                    r["tolerance"] = 1e-6
+                    sv.upload(w.U, w.V)
+                    done, by_step = 0, {}
+                    for m in marks:
+                        sv.run(m - done)
+                        done = m
+                        by_step[str(m)] = W.rel_l2(sv.download(), ref[m])
+                    r["rel_l2_vs_oracle_fp64_by_step"] = by_step
+                res[label] = r
         out[name] = res
         log("%s: %s" % (name, json.dumps(res)))
     return out
@@ -548,49 +717,66 @@ def fifo_latencies(arrivals, service):
 
 
 def run_serving(args):
-    """Continuous-batching request loop on a seeded Poisson stream (dims
-    1D:2D:3D = 5:4:1, sizes and step counts log-uniform, FP64 or mixed per
-    request) against one solve at a time (each request through its own
-    Solver: create, upload, run, download, release), both saturated (every
-    request queued at t = 0) and at the offered arrival rate."""
+    """Continuous-batching request loop on a seeded Poisson stream with the
+    serving configuration's distributions (dims 1D:2D:3D = 5:4:1, sizes
+    log-uniform 1D 512-65536, 2D 64^2-1024^2, 3D 32^3-256^3, steps 100-5000,
+    FP64 or mixed 50/50), scaled down from 20,000 requests to
+    --serve-requests.  First every request is queued at t = 0 (saturated:
+    the loop's capacity); then the same stream arrives at several offered
+    rates (fractions of that capacity, or --serve-rates).  Against: one solve
+    at a time, first come first served (each request through its own Solver:
+    create, upload, run, download, release), whose latencies at each rate
+    follow from the measured service times of a back-to-back pass."""
     from nlsemagic_gb300 import workloads as W
     from nlsemagic_gb300.serve import Server, percentile, serve_sequential
-    reqs = W.serving_requests(count=args.serve_requests, rate=args.serve_rate,
+    full = 20000
+    reqs = W.serving_requests(count=args.serve_requests, rate=1.0,
                               n1=(512, 65536), n2=(64, 1024), n3=(32, args.serve_max3d),
                               steps=(100, args.serve_max_steps))
     pool = args.serve_pool_gb << 30
 
-    def server():
-        return Server(pool_bytes=pool, chunk_steps=args.serve_chunk, solo_bytes=pool)
+    def server(order="srpt"):
+        return Server(pool_bytes=pool, chunk_steps=args.serve_chunk, solo_bytes=pool, order=order)
 
+    seq, seq_done = serve_sequential(reqs, time_scale=0.0)
+    service = [c.done - c.admitted for c in seq_done]  # in arrival order
+    log("one at a time: %s" % json.dumps(seq))
     srv = server()
-    sat, _ = srv.serve(reqs, time_scale=0.0)  # saturated: all queued at t = 0
+    sat, _ = srv.serve(reqs, time_scale=0.0)
     srv.close()
     log("served (saturated): %s" % json.dumps(sat))
-    srv = server()
-    live, _ = srv.serve(reqs, time_scale=1.0)  # Poisson arrivals at the offered rate
-    srv.close()
-    log("served (rate %.1f/s): %s" % (args.serve_rate, json.dumps(live)))
-    seq, seq_done = serve_sequential(reqs, time_scale=0.0)
-    service = [c.done - c.admitted for c in seq_done]
-    arrivals = [r.arrival for r in sorted(reqs, key=lambda r: r.arrival)]
-    lat = fifo_latencies(arrivals, service)
-    seq_live = {"p50_latency_s": percentile(lat, 50), "p99_latency_s": percentile(lat, 99)}
-    log("sequential: %s" % json.dumps(seq))
-    return {"requests": len(reqs), "rate_per_s": args.serve_rate,
+    if args.serve_rates:
+        rates = [float(x) for x in args.serve_rates.split(",")]
+    else:
+        rates = [f * sat["requests_per_s"] for f in (0.3, 0.6, 0.9)]
+    arrivals1 = [r.arrival for r in sorted(reqs, key=lambda r: r.arrival)]
+    per_rate = []
+    for rate in rates:
+        srv = server()
+        live, _ = srv.serve(reqs, time_scale=1.0 / rate)
+        srv.close()
+        lat = fifo_latencies([a / rate for a in arrivals1], service)
+        fcfs = {"p50_latency_s": percentile(lat, 50), "p99_latency_s": percentile(lat, 99)}
+        row = {"rate_per_s": rate,
+               "server": {k: live[k] for k in ("p50_latency_s", "p99_latency_s", "p50_queue_s",
+                                               "p99_queue_s", "gpt_steps_per_s", "wall_s")},
+               "one_at_a_time_fcfs": fcfs,
+               "server_p99_le_fcfs_p99": live["p99_latency_s"] <= fcfs["p99_latency_s"]}
+        per_rate.append(row)
+        log("rate %.2f/s: %s" % (rate, json.dumps(row)))
+    return {"requests": len(reqs), "stream_size": full,
+            "scaled_down_by": full / float(len(reqs)),
             "dims_ratio": "5:4:1", "sizes": {"1d": [512, 65536], "2d": [64, 1024],
                                              "3d": [32, args.serve_max3d]},
             "steps": [100, args.serve_max_steps], "precision": "FP64 or mixed, 50/50",
             "chunk_steps": args.serve_chunk,
+            "policy": "batched launch for 1D/2D/small 3D plus one large 3D solve at a time, "
+                      "shortest remaining work first",
             "value": sat["gpt_steps_per_s"], "unit": UNIT,
             "requests_per_s": sat["requests_per_s"],
-            "at_rate": {"p50_latency_s": live["p50_latency_s"],
-                        "p99_latency_s": live["p99_latency_s"],
-                        "p99_queue_s": live["p99_queue_s"], "wall_s": live["wall_s"],
-                        "gpt_steps_per_s": live["gpt_steps_per_s"]},
+            "rates": per_rate,
             "one_at_a_time": {"value": seq["gpt_steps_per_s"], "unit": UNIT,
-                              "requests_per_s": seq["requests_per_s"],
-                              "at_rate": seq_live},
+                              "requests_per_s": seq["requests_per_s"]},
             "throughput_over_one_at_a_time": sat["gpt_steps_per_s"] / seq["gpt_steps_per_s"]
             if seq["gpt_steps_per_s"] else None,
             "requests_per_s_over_one_at_a_time": sat["requests_per_s"] / seq["requests_per_s"]
@@ -605,7 +791,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--grid", type=int, default=320)
     ap.add_argument("--rk4-steps", type=int, default=500)
-    ap.add_argument("--graph-steps", type=int, default=10)
+    ap.add_argument("--graph-steps", type=int, default=0,
+                    help="RK4 steps per captured graph (0: the autotuned or default knob)")
+    ap.add_argument("--tune", type=int, default=1, choices=[0, 1],
+                    help="1: tune the launch knobs of each problem class (cached) and apply them")
     ap.add_argument("--fp64-steps", type=int, default=-1,
                     help="RK4 steps of the FP64 comparison run (-1: the workload's own)")
     ap.add_argument("--cpu-sample-steps", type=int, default=1)
@@ -613,16 +802,19 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=1000)
     ap.add_argument("--batch-seq-sample", type=int, default=0,
                     help="time only the first N solves one at a time (0: all)")
-    ap.add_argument("--serve-requests", type=int, default=200)
-    ap.add_argument("--serve-rate", type=float, default=20.0)
+    ap.add_argument("--serve-requests", type=int, default=100,
+                    help="requests of the serving stream (the configuration names 20,000)")
+    ap.add_argument("--serve-rates", default="",
+                    help="offered rates, requests/s, comma-separated (default: 0.3, 0.6 and "
+                         "0.9 of the saturated rate)")
     ap.add_argument("--serve-chunk", type=int, default=100)
-    ap.add_argument("--serve-max3d", type=int, default=128)
-    ap.add_argument("--serve-max-steps", type=int, default=2000)
+    ap.add_argument("--serve-max3d", type=int, default=256)
+    ap.add_argument("--serve-max-steps", type=int, default=5000)
     ap.add_argument("--serve-pool-gb", type=int, default=64)
     ap.add_argument("--pdl", type=int, default=1, choices=[0, 1],
                     help="3D 2SHOC stage kernels: 1 overlap through programmatic dependent "
                          "launch, 0 plain stream order (same bits)")
-    ap.add_argument("--only", choices=["batched", "serving", "configs"], default=None,
+    ap.add_argument("--only", choices=["batched", "serving", "configs", "fp64"], default=None,
                     help="run one auxiliary section alone and print its JSON (for profiling)")
     ap.add_argument("--grid2d", type=int, default=512, help="side of configuration 2")
     ap.add_argument("--config2-steps", type=int, default=2000)
@@ -633,8 +825,8 @@ def main():
     if args.only:
         import nlsemagic_gb300 as ng
         ng.load()
-        out = {"batched": run_batched, "serving": run_serving,
-               "configs": run_configs}[args.only](args)
+        out = {"batched": run_batched, "serving": run_serving, "configs": run_configs,
+               "fp64": run_fp64}[args.only](args)
         print(json.dumps({"section": args.only, **out}), flush=True)
         return
     from nlsemagic_gb300 import workloads as W

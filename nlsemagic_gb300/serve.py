@@ -1,26 +1,37 @@
 """Continuous-batching request loop.
 
 Requests (solves with their own dimension, grid, step count and precision
-class) arrive over time.  The loop:
+class) arrive over time.  The loop keeps the device busy with two kinds of
+work in flight at once, each on its own stream, and polls them without
+blocking:
 
-1. admits arrived requests, first come first served, while device memory
-   allows.  Small solves (1D, 2D, and 3D below ``solo_points``) take a slot
-   in the batched persistent launch (:class:`~nlsemagic_gb300.api.Batch`,
-   admitted by its pool budget); large 3D solves get a resident
-   :class:`~nlsemagic_gb300.api.Solver` of their own, which uses the tiled 3D
-   stage kernels (admitted against ``solo_bytes``).  State and potential are
-   uploaded once and stay resident until the request completes;
-2. advances every admitted solve by up to ``chunk_steps`` RK4 steps per round:
-   one persistent launch per precision class for all batched solves, and one
-   graph-captured chunk per resident solver, each on its own stream, so
-   requests that arrived at different times share the device;
-3. retires finished requests: the final state is downloaded as the snapshot
-   returned to the caller and the memory is released.
+1. **The batch.**  Small solves (1D, 2D, and 3D below ``solo_points``) take
+   a slot in the batched persistent launch (:class:`~nlsemagic_gb300.api.Batch`,
+   admitted by its pool budget while no launch is in flight).  Each launch
+   advances every admitted solve by up to ``chunk_steps`` RK4 steps; a new
+   launch starts as soon as the previous one finishes, so requests that
+   arrive meanwhile join at the next launch.
+2. **One large solve.**  Large 3D solves get a resident
+   :class:`~nlsemagic_gb300.api.Solver` (the tiled 3D stage kernels),
+   admitted against ``solo_bytes``.  One of them runs at a time, a slice of
+   about ``slice_s`` seconds of estimated work; at every slice boundary the
+   admitted large solve with the least remaining work goes next (shortest
+   remaining processing time), so a short request is never stuck behind a
+   long one, and a long one runs alone at full speed rather than sharing
+   the GPU with the others.
+
+Work is estimated as points x steps, times ``fp64_cost`` for the FP64 class
+(about its speed ratio to the mixed class).  Waiting requests are admitted
+least work first (``order="srpt"``) or in arrival order
+(``order="fifo"``).  State and potential are uploaded once and stay resident
+until the request completes; the final state is downloaded as the snapshot
+returned to the caller.
 
 Latency of a request = completion time - arrival time.  The loop reports
 p50 / p99 latency, queueing delay, aggregate grid-point-steps/s and
 completed requests/s.  There is no reference counterpart (NLSEmagic
-integrates one solve per call).
+integrates one solve per call; its drivers loop over chunks of one solve,
+src/NLSEmagic3D/NLSEmagic3D.m:298-344).
 """
 from __future__ import annotations
 
@@ -31,7 +42,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from .api import Batch, Solver
-from ._lib import NLSE_ERR_CAPACITY, NLSEError
+from ._lib import NLSE_ERR_CAPACITY, PREC_DOUBLE, NLSEError
 
 
 @dataclass
@@ -74,21 +85,50 @@ def summarize(done, wall, busy=None, launches=None, rejected=0):
     return out
 
 
+class _Solo:
+    __slots__ = ("req", "admitted", "solver", "left", "bytes", "inflight")
+
+    def __init__(self, req, admitted, solver, left, nbytes):
+        self.req, self.admitted, self.solver = req, admitted, solver
+        self.left, self.bytes, self.inflight = left, nbytes, 0
+
+
 class Server:
     def __init__(self, pool_bytes, chunk_steps=64, max_solves=8192, keep_snapshots=False,
-                 solo_points=1 << 18, solo_bytes=None):
+                 solo_points=1 << 18, solo_bytes=None, order="srpt", slice_s=0.02,
+                 fp64_cost=12.0, mixed_rate=15e9):
+        if order not in ("srpt", "fifo"):
+            raise ValueError("order must be 'srpt' or 'fifo'")
         self.batch = Batch(pool_bytes, max_solves)
         self.pool_bytes = int(pool_bytes)
         self.chunk_steps = int(chunk_steps)
         self.keep_snapshots = keep_snapshots
         self.solo_points = int(solo_points)
         self.solo_bytes = int(solo_bytes if solo_bytes is not None else pool_bytes)
+        self.order = order
+        self.slice_s = float(slice_s)
+        self.fp64_cost = float(fp64_cost)
+        self.mixed_rate = float(mixed_rate)
 
     def close(self):
         self.batch.close()
 
     def is_solo(self, inst):
         return inst.U.ndim == 3 and inst.U.size >= self.solo_points
+
+    def work(self, inst, steps=None):
+        """Estimated work: point-steps, FP64 weighted by fp64_cost."""
+        w = float(inst.U.size) * (inst.steps if steps is None else steps)
+        return w * (self.fp64_cost if inst.precision == PREC_DOUBLE else 1.0)
+
+    def _slice_steps(self, solo):
+        # steps of about slice_s seconds at the estimated rate
+        per_step = self.work(solo.req.inst, 1) / self.mixed_rate
+        n = max(1, int(self.slice_s / per_step)) if per_step > 0 else solo.left
+        return min(solo.left, n)
+
+    def _key(self, r):
+        return self.work(r.inst) if self.order == "srpt" else r.arrival
 
     def serve(self, requests, time_scale=1.0, max_wall=None):
         """Serve `requests` (objects with .rid, .arrival seconds, .inst with
@@ -97,99 +137,118 @@ class Server:
         a summary dict and the list of Completed records."""
         b = self.batch
         pending = deque(sorted(requests, key=lambda r: r.arrival))
-        waiting = deque()
+        wait_small, wait_solo = [], []
         active = {}  # batch slot -> (request, admitted)
-        solos = []   # [request, admitted, Solver, steps_left, bytes]
+        solos = []   # admitted large solves
+        running = None  # the large solve with a slice in flight
+        batch_busy = False
         solo_used = 0
-        done = []
-        rejected = []
+        done, rejected = [], []
         t0 = time.perf_counter()
-        busy = 0.0
-        launches = 0
-        while pending or waiting or active or solos:
-            now = time.perf_counter() - t0
+        clock = lambda: time.perf_counter() - t0  # noqa: E731
+        busy, busy_since, launches = 0.0, None, 0
+
+        def finish(r, tadm, snap, solo):
+            done.append(Completed(r.rid, r.arrival * time_scale, tadm, clock(),
+                                  int(r.inst.U.size), int(r.inst.steps), int(r.inst.precision),
+                                  solo, snap if self.keep_snapshots else None))
+
+        while pending or wait_small or wait_solo or active or solos:
+            now = clock()
             if max_wall is not None and now > max_wall:
                 break
             while pending and pending[0].arrival * time_scale <= now:
-                waiting.append(pending.popleft())
-            # admission in arrival order, by the device-memory budgets
-            while waiting:
-                r = waiting[0]
-                i = r.inst
-                if self.is_solo(i):
+                r = pending.popleft()
+                (wait_solo if self.is_solo(r.inst) else wait_small).append(r)
+            progressed = False
+            # ---- admission (the batch only between its launches)
+            if wait_small and not batch_busy:
+                wait_small.sort(key=self._key)
+                keep = []
+                for r in wait_small:
+                    i = r.inst
+                    if Batch.bytes_for(i.U.shape, i.precision, i.method) > self.pool_bytes:
+                        rejected.append(r.rid)
+                        continue
+                    try:
+                        slot = b.add(i.U, i.V, i.s, i.a, i.h * i.h, i.BC, i.steps, i.k, i.method,
+                                     i.precision)
+                    except NLSEError as e:
+                        if e.code != NLSE_ERR_CAPACITY:
+                            raise
+                        keep.append(r)  # waits for pool memory
+                        continue
+                    active[slot] = (r, clock())
+                wait_small = keep
+            if wait_solo:
+                wait_solo.sort(key=self._key)
+                keep = []
+                for r in wait_solo:
+                    i = r.inst
                     need = Solver.bytes_for(i.U.shape, i.method, i.precision, i.BC)
                     if need > self.solo_bytes:
                         rejected.append(r.rid)
-                        waiting.popleft()
                         continue
                     if solo_used + need > self.solo_bytes:
-                        break  # wait for a resident solver to retire
+                        keep.append(r)  # waits for a large solve to retire
+                        continue
                     sv = Solver(i.U.shape, method=i.method, precision=i.precision, BC=i.BC, s=i.s,
                                 a=i.a, h2=i.h * i.h, k=i.k)
                     sv.upload(i.U, i.V)
-                    solos.append([r, time.perf_counter() - t0, sv, int(i.steps), need])
+                    solos.append(_Solo(r, clock(), sv, int(i.steps), need))
                     solo_used += need
-                    waiting.popleft()
-                    continue
-                need = Batch.bytes_for(i.U.shape, i.precision, i.method)
-                if need > self.pool_bytes:
-                    rejected.append(r.rid)
-                    waiting.popleft()
-                    continue
-                try:
-                    slot = b.add(i.U, i.V, i.s, i.a, i.h * i.h, i.BC, i.steps, i.k, i.method,
-                                 i.precision)
-                except NLSEError as e:
-                    if e.code == NLSE_ERR_CAPACITY:
-                        break  # wait for pool memory to free up
-                    raise
-                active[slot] = (r, time.perf_counter() - t0)
-                waiting.popleft()
-            if not active and not solos:
-                if pending:
-                    dt = pending[0].arrival * time_scale - (time.perf_counter() - t0)
-                    if dt > 0:
-                        time.sleep(dt)
-                continue
-            # one round: batched launch(es) plus a chunk of every resident solver
-            ts = time.perf_counter()
-            if active:
+                wait_solo = keep
+            # ---- launches
+            if not batch_busy and active:
                 b.run(self.chunk_steps)
-            for sl in solos:
-                n = min(self.chunk_steps, sl[3])
-                sl[2].run(n)
-                sl[3] -= n
-                launches += n * sl[2].launches_per_step
-            if active:
-                b.sync()
+                batch_busy = True
+                progressed = True
+            if running is None and solos:
+                running = min(solos, key=lambda x: (self.work(x.req.inst, x.left)
+                                                    if self.order == "srpt" else x.req.arrival))
+                n = self._slice_steps(running)
+                running.solver.run(n)
+                running.inflight = n
+                launches += n * running.solver.launches_per_step
+                progressed = True
+            if (batch_busy or running is not None) and busy_since is None:
+                busy_since = clock()
+            # ---- completions
+            if batch_busy and b.idle():
+                batch_busy = False
                 launches += b.last_launches
-            for sl in solos:
-                sl[2].sync()
-            busy += time.perf_counter() - ts
-            for slot in list(active):
-                if b.remaining(slot) == 0:
-                    r, tadm = active.pop(slot)
-                    snap = b.download(slot)
-                    done.append(Completed(r.rid, r.arrival * time_scale, tadm,
-                                          time.perf_counter() - t0, int(r.inst.U.size),
-                                          int(r.inst.steps), int(r.inst.precision), False,
-                                          snap if self.keep_snapshots else None))
-                    b.remove(slot)
-            keep = []
-            for sl in solos:
-                if sl[3] > 0:
-                    keep.append(sl)
-                    continue
-                r, tadm, sv, _, need = sl
-                snap = sv.download()
-                sv.close()
-                solo_used -= need
-                done.append(Completed(r.rid, r.arrival * time_scale, tadm,
-                                      time.perf_counter() - t0, int(r.inst.U.size),
-                                      int(r.inst.steps), int(r.inst.precision), True,
-                                      snap if self.keep_snapshots else None))
-            solos = keep
-        wall = time.perf_counter() - t0
+                for slot in list(active):
+                    if b.remaining(slot) == 0:
+                        r, tadm = active.pop(slot)
+                        snap = b.download(slot)
+                        b.remove(slot)
+                        finish(r, tadm, snap, False)
+                progressed = True
+            if running is not None and running.solver.idle():
+                running.left -= running.inflight
+                running.inflight = 0
+                if running.left <= 0:
+                    snap = running.solver.download()
+                    running.solver.close()
+                    solo_used -= running.bytes
+                    solos.remove(running)
+                    finish(running.req, running.admitted, snap, True)
+                running = None
+                progressed = True
+            if not batch_busy and running is None and busy_since is not None:
+                busy += clock() - busy_since
+                busy_since = None
+            if progressed:
+                continue
+            if batch_busy or running is not None:
+                time.sleep(0.0002)  # work in flight: poll again shortly
+            elif pending and not wait_small and not wait_solo:
+                dt = pending[0].arrival * time_scale - clock()
+                if dt > 0:
+                    time.sleep(dt)
+        if busy_since is not None:
+            busy += clock() - busy_since
+        wall = clock()
         return summarize(done, wall, busy, launches, len(rejected)), done
 
 

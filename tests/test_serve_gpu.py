@@ -88,3 +88,16 @@ def test_serving_solo_and_batched_results_equal_alone(gpu_lib):
         want = ng.take_steps(i.U, i.V, i.s, i.a, i.h * i.h, i.BC, i.steps, i.k, method=i.method,
                              precision=i.precision)
         assert bits_equal(c.snapshot, want)
+
+
+def test_serving_runs_least_remaining_work_first(gpu_lib):
+    # large 3D requests queued together run one at a time, the one with the
+    # least remaining work first, so they complete in order of their work
+    from nlsemagic_gb300.serve import Server
+    reqs = W.serving_requests(count=6, rate=1e3, ratio=(0, 0, 1), n3=(20, 28), steps=(20, 200))
+    srv = Server(pool_bytes=1 << 28, chunk_steps=16, solo_points=1000, slice_s=1e-4)
+    summary, done = srv.serve(reqs, time_scale=0.0)
+    srv.close()
+    assert summary["requests"] == len(reqs) and all(c.solo for c in done)
+    finished = [c.rid for c in sorted(done, key=lambda c: c.done)]
+    assert finished == [r.rid for r in sorted(reqs, key=lambda r: srv.work(r.inst))]
