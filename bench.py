@@ -308,6 +308,7 @@ def run_gpu(args, w):
     import torch
 
     import nlsemagic_gb300 as ng
+    from nlsemagic_gb300 import workloads as W
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
@@ -438,6 +439,11 @@ def run_gpu(args, w):
                 "mixed_rel_l2_tolerance": 1e-6,
                 "fp64_bit_identical_to_oracle": "by test (tests/test_config_parity_gpu.py, "
                                                 "this grid, all 500 steps)"}
+        vf, uf = fp64_solve(w, fp64_steps, fma=True)
+        fp64["contracted"] = {"value": vf, "unit": UNIT, "speedup": vf / fp64["value"],
+                              "rel_l2_vs_oracle_fp64": W.rel_l2(uf, u64),
+                              "what": "NLSE_FLAG_FMA: the FP64 kernels compiled with "
+                                      "multiply-add contraction (tolerance 1e-12)"}
         try:
             rates = fp64_rates()
             ops = FP64_OPS[(3, w.method)]
@@ -600,14 +606,16 @@ def fp64_rates():
             "how": "timed kernel, 8 independent chains per thread, 16 blocks of 256 per SM"}
 
 
-def fp64_solve(w, steps, graph_steps=10):
-    """Gpt-steps/s of the exact FP64 class on workload w (resident solver,
-    graphs, CUDA events on the solver stream) and its final state."""
+def fp64_solve(w, steps, graph_steps=10, fma=False):
+    """Gpt-steps/s of the FP64 class on workload w (resident solver, graphs,
+    CUDA events on the solver stream) and its final state; fma: the
+    contracted kernels (NLSE_FLAG_FMA)."""
     import torch
 
     import nlsemagic_gb300 as ng
+    flags = ng.FLAG_MSD_GUARD | (ng.FLAG_FMA if fma else 0)
     with ng.Solver(w.U.shape, method=w.method, precision=ng.PREC_DOUBLE, BC=w.BC, s=w.s, a=w.a,
-                   h2=w.h2, k=w.k) as sv:
+                   h2=w.h2, k=w.k, flags=flags) as sv:
         sv.set_graph_steps(graph_steps)
         sv.upload(w.U, w.V)
         sv.run(max(1, min(steps, graph_steps)))  # captures the graph
@@ -635,12 +643,15 @@ def run_fp64(args):
     steps3 = args.fp64_steps if args.fp64_steps > 0 else 20
     for name, w, steps in (("3d_2shoc", W.vortex_rings_3d(n=args.grid, method=2), steps3),
                            ("2d_2shoc", W.dark_vortices_2d(n=args.grid2d), 200)):
-        v, _ = fp64_solve(w, steps)
+        v, u = fp64_solve(w, steps)
+        vf, uf = fp64_solve(w, steps, fma=True)
         ops = FP64_OPS[(w.ndim, w.method)]
         out[name] = {"workload": w.name, "rk4_steps": steps, "value": v, "unit": UNIT,
                      "fp64_ops_per_point_step": ops,
                      "fp64_issue_frac_of_measured_add_rate": v * 1e9 * ops / rates["add_per_s"],
-                     "hbm_frac_of_measured": v * BYTES_FP64 / peaks()[0]}
+                     "hbm_frac_of_measured": v * BYTES_FP64 / peaks()[0],
+                     "contracted": {"value": vf, "unit": UNIT, "speedup": vf / v,
+                                    "rel_l2_vs_exact_fp64": W.rel_l2(uf, u)}}
         log("%s: %s" % (name, json.dumps(out[name])))
     return out
 
@@ -745,6 +756,10 @@ def run_serving(args):
     sat, _ = srv.serve(reqs, time_scale=0.0)
     srv.close()
     log("served (saturated): %s" % json.dumps(sat))
+    srv = Server(pool_bytes=pool, chunk_steps=args.serve_chunk, solo_bytes=pool, per_class=False)
+    sat1, _ = srv.serve(reqs, time_scale=0.0)
+    srv.close()
+    log("served (saturated, one large solve at a time): %s" % json.dumps(sat1))
     if args.serve_rates:
         rates = [float(x) for x in args.serve_rates.split(",")]
     else:
@@ -770,10 +785,14 @@ def run_serving(args):
                                              "3d": [32, args.serve_max3d]},
             "steps": [100, args.serve_max_steps], "precision": "FP64 or mixed, 50/50",
             "chunk_steps": args.serve_chunk,
-            "policy": "batched launch for 1D/2D/small 3D plus one large 3D solve at a time, "
-                      "shortest remaining work first",
+            "policy": "batched launch for 1D/2D/small 3D plus one large 3D solve of each "
+                      "precision class at a time, shortest remaining work first",
             "value": sat["gpt_steps_per_s"], "unit": UNIT,
             "requests_per_s": sat["requests_per_s"],
+            "saturated_one_large_solve_at_a_time": {
+                "value": sat1["gpt_steps_per_s"], "unit": UNIT,
+                "requests_per_s": sat1["requests_per_s"],
+                "p99_latency_s": sat1["p99_latency_s"]},
             "rates": per_rate,
             "one_at_a_time": {"value": seq["gpt_steps_per_s"], "unit": UNIT,
                               "requests_per_s": seq["requests_per_s"]},

@@ -7,7 +7,7 @@ The compute path is the CUDA library ``libnlse_gb300.so`` (C ABI in
 CPU fallback: without the built library every call raises
 :class:`NativeLibraryMissing`.
 """
-from ._lib import (FLAG_GATHER, FLAG_MSD_GUARD, PREC_DOUBLE, PREC_MIXED, PREC_SINGLE,  # noqa: F401
+from ._lib import (FLAG_FMA, FLAG_GATHER, FLAG_MSD_GUARD, PREC_DOUBLE, PREC_MIXED, PREC_SINGLE,  # noqa: F401
                    IC_GAUSS, IC_GREY, IC_RINGS, IC_SECH, IC_TANH, IC_VORTICES, NOISE_ADD,
                    NOISE_NONE, NOISE_PHASE, NativeLibraryMissing, NLSEError, load)
 from .api import *  # noqa: F401,F403

@@ -25,6 +25,7 @@ NLSE_ERR_STATE = 7
 PREC_SINGLE, PREC_DOUBLE, PREC_MIXED = 1, 2, 3
 FLAG_MSD_GUARD = 1
 FLAG_GATHER = 2
+FLAG_FMA = 4
 
 _ERRNAMES = {1: "NLSE_ERR_ARG", 2: "NLSE_ERR_CUDA", 3: "NLSE_ERR_NOMEM", 4: "NLSE_ERR_TIMEOUT",
              5: "NLSE_ERR_NONFINITE", 6: "NLSE_ERR_CAPACITY", 7: "NLSE_ERR_STATE"}

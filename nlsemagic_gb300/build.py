@@ -39,6 +39,7 @@ UNITS = {
     "kern_small_exact.cu": ["-fmad=false"],
     "kern_small_mixed.cu": [],
     "kern_probe.cu": [],
+    "kern_exact_fma.cu": [],  # contracted FP64 (NLSE_FLAG_FMA): -fmad left on
 }
 
 

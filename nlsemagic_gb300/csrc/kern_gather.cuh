@@ -153,7 +153,10 @@ __device__ C2<R> f_at_d(const Geom& g, const Consts<R>& c, const C2<R>* U, const
   return f_bnd<R, BC>(c, U[b], V[b], U[q], fq);
 }
 
-template <typename R, int DIM, int METHOD, int BC>
+// VAR tells apart the copies of the exact kernels that the FP64 class's
+// contracted form compiles in its own unit (kern_exact_fma.cu): 0 here, 1
+// there, same source, distinct symbols.
+template <typename R, int DIM, int METHOD, int BC, int VAR = 0>
 __global__ void __launch_bounds__(256) gather_stage(Geom g, Consts<R> c,
                                                     const C2<R>* __restrict__ Yin,
                                                     C2<R>* Psi, const R* __restrict__ V,
@@ -172,7 +175,7 @@ __global__ void __launch_bounds__(256) gather_stage(Geom g, Consts<R> c,
 
 // Two-phase 2SHOC stage: D at every point into scratch, then F from it.
 // Same results as gather_stage, without recomputing D at every neighbour.
-template <typename R, int DIM, int BC>
+template <typename R, int DIM, int BC, int VAR = 0>
 __global__ void __launch_bounds__(256) d_stage(Geom g, Consts<R> c, const C2<R>* __restrict__ Yin,
                                                const R* __restrict__ V, C2<R>* __restrict__ D) {
   pdl_trigger();  // the next kernel may launch; it waits for this one
@@ -185,7 +188,7 @@ __global__ void __launch_bounds__(256) d_stage(Geom g, Consts<R> c, const C2<R>*
   }
 }
 
-template <typename R, int DIM, int BC>
+template <typename R, int DIM, int BC, int VAR = 0>
 __global__ void __launch_bounds__(256) gather_stage_d(Geom g, Consts<R> c,
                                                       const C2<R>* __restrict__ Yin, C2<R>* Psi,
                                                       const R* __restrict__ V,

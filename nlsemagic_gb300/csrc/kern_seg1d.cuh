@@ -208,7 +208,7 @@ cudaError_t launch(const Geom& g, const MixedStageArgs& a, const Consts<float>& 
                   pdl, g, c, io, stage);
 }
 
-template <typename R, int METHOD, int BC>
+template <typename R, int METHOD, int BC, int VAR = 0>  // VAR: as exact::gather_stage
 __global__ void __launch_bounds__(NT)
     stage1d_exact(Geom g, Consts<R> c, const C2<R>* __restrict__ Yin, C2<R>* Psi,
                   const R* __restrict__ V, C2<R>* __restrict__ K, C2<R>* __restrict__ Yout,
@@ -219,10 +219,10 @@ __global__ void __launch_bounds__(NT)
   segment_exact<R, METHOD, BC, SOLO_SEG>(g, c, Yin, Psi, V, K, Yout, stage, blockIdx.x, sm);
 }
 
-template <typename R, int METHOD, int BC>
+template <typename R, int METHOD, int BC, int VAR = 0>
 cudaError_t launch_exact(const Geom& g, const Consts<R>& c, const ExactStageArgs<R>& a,
                          int stage, cudaStream_t st, bool pdl) {
-  return launch_k(stage1d_exact<R, METHOD, BC>, dim3((unsigned)segments<SOLO_SEG>(g.n)),
+  return launch_k(stage1d_exact<R, METHOD, BC, VAR>, dim3((unsigned)segments<SOLO_SEG>(g.n)),
                   dim3(NT), 0, st, pdl, g, c, a.Yin, a.Psi, a.V, a.K, a.Yout, stage);
 }
 

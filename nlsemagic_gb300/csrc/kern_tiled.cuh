@@ -26,6 +26,8 @@
 // (operands (hi, E) via nlse_mixed.cuh), through a policy type.
 #pragma once
 
+#include <type_traits>
+
 #include <cuda.h>
 
 #include "../../include/nlse_gb300.h"
@@ -625,12 +627,18 @@ cudaError_t launch3d(const Geom& g, const typename Pol::Args& A, const void* in0
 // --------------------------------------------------------------------------
 // entry point used by the launcher in kern_exact.cu
 // --------------------------------------------------------------------------
-template <typename R, int DIM, int METHOD, int BC>
+// The exact policy under another name: the kernels of the FP64 class's
+// contracted form (VAR 1, compiled in kern_exact_fma.cu) get their own symbols.
+template <typename R, int VAR>
+struct ExactPolVar : ExactPol<R> {};
+
+template <typename R, int DIM, int METHOD, int BC, int VAR = 0>
 cudaError_t launch_exact(const Geom& g, const Consts<R>& c, const ExactStageArgs<R>& a, int stage,
                          cudaStream_t st) {
   if (DIM != 3 || BC == 4) return cudaErrorNotSupported;
-  typename ExactPol<R>::Args A{a, c, stage, error_word()};
-  return launch3d<ExactPol<R>, METHOD, BC == 4 ? 1 : BC>(g, A, a.Yin, nullptr, st);
+  typedef typename std::conditional<VAR == 0, ExactPol<R>, ExactPolVar<R, VAR>>::type Pol;
+  typename Pol::Args A{a, c, stage, error_word()};
+  return launch3d<Pol, METHOD, BC == 4 ? 1 : BC>(g, A, a.Yin, nullptr, st);
 }
 
 }  // namespace tiled

@@ -231,6 +231,8 @@ static int validate(const nlse_problem* p) {
   if (!(p->h2 > 0.0) || !isfinite(p->h2)) return fail(NLSE_ERR_ARG, "h2 must be > 0");
   if (!(p->k > 0.0) || !isfinite(p->k)) return fail(NLSE_ERR_ARG, "k must be > 0");
   if (!isfinite(p->s)) return fail(NLSE_ERR_ARG, "s must be finite");
+  if ((p->flags & NLSE_FLAG_FMA) && p->precision != NLSE_PREC_DOUBLE)
+    return fail(NLSE_ERR_ARG, "NLSE_FLAG_FMA applies to the FP64 class only");
   return NLSE_OK;
 }
 
@@ -611,9 +613,12 @@ static int enqueue_step(nlse_solver* s) {
     ExactStageArgs<double> a1{psi, psi, V, K, ya, D}, a2{ya, psi, V, K, yb, D},
         a3{yb, psi, V, K, ya, D}, a4{ya, psi, V, K, nullptr, D};
     const ExactStageArgs<double>* as[4] = {&a1, &a2, &a3, &a4};
+    const bool fma = (p.flags & NLSE_FLAG_FMA) != 0;
     for (int st = 1; st <= 4 && e == cudaSuccess; ++st)
-      e = launch_exact_stage<double>(s->g, p.method, p.bc, s->cd, *as[st - 1], st, s->stream,
-                                     s->kernel_kind);
+      e = fma ? launch_exact_stage_fma(s->g, p.method, p.bc, s->cd, *as[st - 1], st, s->stream,
+                                       s->kernel_kind)
+              : launch_exact_stage<double>(s->g, p.method, p.bc, s->cd, *as[st - 1], st,
+                                           s->stream, s->kernel_kind);
   } else if (p.precision == NLSE_PREC_SINGLE) {
     typedef C2<float> T;
     T *psi = (T*)s->psi, *K = (T*)s->K, *ya = (T*)s->ya, *yb = (T*)s->yb;

@@ -589,6 +589,10 @@ extern "C" int nlse_batch_add(nlse_batch* b, const nlse_problem* p, const double
   if (nsteps < 0) return nlse::set_error(NLSE_ERR_ARG, "nsteps must be >= 0");
   if (p->precision != NLSE_PREC_DOUBLE && p->precision != NLSE_PREC_MIXED)
     return nlse::set_error(NLSE_ERR_ARG, "batched solves are FP64 or mixed precision");
+  if (p->flags & NLSE_FLAG_FMA)
+    return nlse::set_error(NLSE_ERR_ARG,
+                           "the batched launch computes FP64 without contraction "
+                           "(NLSE_FLAG_FMA is for single solves)");
   {
     int rc = nlse_validate_problem(p);  // same rules as single solves
     if (rc) return rc;

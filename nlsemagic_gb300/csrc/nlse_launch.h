@@ -42,6 +42,13 @@ cudaError_t launch_exact_stage(const Geom& g, int method, int BC, const Consts<R
                                const ExactStageArgs<R>& a, int stage, cudaStream_t st,
                                int kernel_kind);
 
+// The FP64 class's contracted form (NLSE_FLAG_FMA; kern_exact_fma.cu): the
+// same kernels and dispatch as launch_exact_stage<double>, compiled with
+// multiply-add contraction.
+cudaError_t launch_exact_stage_fma(const Geom& g, int method, int BC, const Consts<double>& c,
+                                   const ExactStageArgs<double>& a, int stage, cudaStream_t st,
+                                   int kernel_kind);
+
 cudaError_t launch_mixed_stage(const Geom& g, int method, int BC, const Consts<float>& c,
                                const MixedStageArgs& a, int stage, cudaStream_t st,
                                int kernel_kind);

@@ -136,6 +136,23 @@ def test_invalid_arguments_rejected_before_cuda(lib, kw, why):
     assert _lib.last_error()
 
 
+def test_contracted_flag_is_fp64_only(lib):
+    # NLSE_FLAG_FMA asks for the FP64 kernels compiled with contraction; other
+    # classes reject it before any CUDA call
+    re_, im_ = ng.api.planar(np.ones(16, complex))
+    V = np.zeros(16)
+    dp = ctypes.POINTER(ctypes.c_double)
+    out = [np.empty(16), np.empty(16)]
+    for prec in (1, 3):
+        p = ng.api.make_problem(1, (16, 1, 1), 1, prec, 1, -1.0, 1.0, 0.01, 1e-3,
+                                ng.FLAG_MSD_GUARD | ng.FLAG_FMA)
+        rc = lib.nlse_take_steps(ctypes.byref(p), re_.ctypes.data_as(dp), im_.ctypes.data_as(dp),
+                                 V.ctypes.data_as(dp), out[0].ctypes.data_as(dp),
+                                 out[1].ctypes.data_as(dp), 1)
+        assert rc == ng._lib.NLSE_ERR_ARG
+        assert b"FP64 class only" in lib.nlse_last_error_string()
+
+
 def test_stability_helper(lib):
     k = ng.linear_stability_k(3, 2, 0.3, 1.0)
     assert abs(k - 0.75 * 0.09 / (3 * 2 ** 0.5)) < 1e-15

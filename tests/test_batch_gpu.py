@@ -209,3 +209,17 @@ def test_mixed_batch_tile_edges(gpu_lib, method, BC):
         assert np.all(np.isfinite(got))
         assert bits_equal(got, one), c["U"].shape
     b.close()
+
+
+def test_batch_rejects_contracted_fp64(gpu_lib):
+    # the batched launch computes FP64 without contraction only
+    import nlsemagic_gb300 as ng
+    U = np.ones(64, complex)
+    b = ng.Batch(1 << 24)
+    try:
+        with pytest.raises(ng.NLSEError) as e:
+            b.add(U, np.zeros(64), -1.0, 1.0, 0.01, 1, 4, 1e-3, 1, ng.PREC_DOUBLE,
+                  flags=ng.FLAG_MSD_GUARD | ng.FLAG_FMA)
+        assert e.value.code == ng._lib.NLSE_ERR_ARG
+    finally:
+        b.close()

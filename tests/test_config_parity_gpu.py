@@ -8,7 +8,8 @@ whole runs of the configurations are compared end to end:
   FP32 oracle, mixed within 1e-6 relative L2 of the FP64 oracle; the mass
   sum |U|^2 h^2 of the FP64 result equal to the oracle's;
 * configuration 3 -- 3D, 320^3 vortex rings in a harmonic trap, MSD: 2SHOC
-  for all 500 RK4 steps, CD for 100; FP64 bit-identical, mixed within 1e-6.
+  for all 500 RK4 steps, CD for 100; FP64 bit-identical, mixed within 1e-6;
+* on both, the FP64 class's contracted form (NLSE_FLAG_FMA) within 1e-12.
 
 The oracle (test infrastructure, oracle/) runs each solve over all host cores
 (oracle.set_threads, same bits as serial).  Its runs are queued on a
@@ -85,10 +86,12 @@ def work(gpu_lib):
     q.t.join()
 
 
-def gpu_run(w, steps, precision):
+def gpu_run(w, steps, precision, flags=None):
     import nlsemagic_gb300 as ng
+    if flags is None:
+        flags = ng.FLAG_MSD_GUARD
     with ng.Solver(w.U.shape, method=w.method, precision=precision, BC=w.BC, s=w.s, a=w.a,
-                   h2=w.h2, k=w.k) as sv:
+                   h2=w.h2, k=w.k, flags=flags) as sv:
         sv.upload(w.U, w.V)
         sv.run(steps)
         sv.sync()
@@ -147,3 +150,13 @@ def test_config3_2shoc_320_full_run(work):
     m0 = mass(w.U, w.h, 3)
     assert mass(got, w.h, 3) == mass(ref, w.h, 3)
     assert abs(mass(mixed, w.h, 3) - mass(ref, w.h, 3)) <= 1e-6 * m0
+
+
+def test_fp64_contracted_full_runs_within_1e12(work):
+    import nlsemagic_gb300 as ng
+    flags = ng.FLAG_MSD_GUARD | ng.FLAG_FMA
+    for w, name in ((work["w2"], "c2_fp64"), (work["w3"], "c3_fp64")):
+        got = gpu_run(w, w.steps, ng.PREC_DOUBLE, flags)
+        ref = work["oracle"].get(name)
+        err = W.rel_l2(got, ref)
+        assert err <= 1e-12, (w.name, err)

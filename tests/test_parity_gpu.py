@@ -85,6 +85,28 @@ def test_exact_random_grids(gpu_lib, ndim, method, prec, BC, gather):
         assert bits_equal(got, want), "shape %s" % (shape,)
 
 
+def test_fp64_contracted_within_1e12(gpu_lib):
+    # NLSE_FLAG_FMA: the FP64 kernels compiled with multiply-add contraction.
+    # Not the oracle's bits, but within 1e-12 relative L2 of them, on every
+    # dimension, method and boundary code, through the tiled and gather paths.
+    import nlsemagic_gb300 as ng
+    differ = 0
+    for ndim, method, BC in [c for c in itertools.product([1, 2, 3], [1, 2], [1, 2, 3, 4])
+                             if not (c[2] == 4 and c[0] != 1)]:
+        rng = np.random.default_rng(500 + 100 * ndim + 10 * method + BC)
+        shape = {1: (301,), 2: (45, 38), 3: (34, 21, 19)}[ndim]
+        U = (1 + 0.2 * rng.standard_normal(shape)) + 0.2j * rng.standard_normal(shape)
+        V = 0.1 * rng.random(shape)
+        args = (U, V, -1.0, 1.1, 0.11, BC, 20, 0.002)
+        want = oracle.take_steps(*args, method=method, precision=2, flags=oracle.MSD_GUARD)
+        for gather in (False, True):
+            flags = ng.FLAG_MSD_GUARD | ng.FLAG_FMA | (ng.FLAG_GATHER if gather else 0)
+            got = ng.take_steps(*args, method=method, precision=ng.PREC_DOUBLE, flags=flags)
+            assert W.rel_l2(got, want) <= 1e-12, (ndim, method, BC, gather)
+            differ += not bits_equal(got, want)
+    assert differ > 0  # the contracted kernels ran
+
+
 @pytest.mark.parametrize("shape", [(33, 5, 5), (65, 66, 4), (129, 3, 7), (31, 33, 34), (64, 64, 9),
                                    (130, 17, 3), (4, 4, 130), (3, 200, 3)])
 @pytest.mark.parametrize("method", [1, 2])
