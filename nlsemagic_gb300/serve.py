@@ -11,14 +11,21 @@ blocking:
    advances every admitted solve by up to ``chunk_steps`` RK4 steps; a new
    launch starts as soon as the previous one finishes, so requests that
    arrive meanwhile join at the next launch.
-2. **One large solve.**  Large 3D solves get a resident
+2. **One large solve per precision class.**  Large 3D solves get a resident
    :class:`~nlsemagic_gb300.api.Solver` (the tiled 3D stage kernels),
-   admitted against ``solo_bytes``.  One of them runs at a time, a slice of
-   about ``slice_s`` seconds of estimated work; at every slice boundary the
-   admitted large solve with the least remaining work goes next (shortest
-   remaining processing time), so a short request is never stuck behind a
-   long one, and a long one runs alone at full speed rather than sharing
-   the GPU with the others.
+   admitted against ``solo_bytes``.  One of each class runs at a time, a
+   slice of about ``slice_s`` seconds of estimated work; at every slice
+   boundary the admitted large solve of that class with the least remaining
+   work goes next (shortest remaining processing time), so a short request
+   is never stuck behind a long one, and a long one does not share the GPU
+   with others of its kind.  The two classes run side by side because they
+   load different units: an FP64 solve is bound by FP64 issue with DRAM
+   nearly idle, a mixed solve by HBM bandwidth (``per_class=False``: one
+   large solve at a time).
+
+With ``fp64_fma`` (default) the large FP64 solves run the contracted FP64
+kernels (NLSE_FLAG_FMA); the batched launch computes FP64 without
+contraction.
 
 Work is estimated as points x steps, times ``fp64_cost`` for the FP64 class
 (about its speed ratio to the mixed class).  Waiting requests are admitted
@@ -42,7 +49,8 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from .api import Batch, Solver
-from ._lib import NLSE_ERR_CAPACITY, PREC_DOUBLE, NLSEError
+from ._lib import (FLAG_FMA, FLAG_MSD_GUARD, NLSE_ERR_CAPACITY, PREC_DOUBLE,
+                   NLSEError)
 
 
 @dataclass
@@ -85,6 +93,15 @@ def summarize(done, wall, busy=None, launches=None, rejected=0):
     return out
 
 
+def solve_flags(inst, fp64_fma):
+    """Problem flags of a request run on its own Solver: the MSD guard, and
+    for FP64 requests with fp64_fma the contracted FP64 kernels
+    (NLSE_FLAG_FMA: within 1e-12 of the reference's bits, fewer FP64
+    instructions)."""
+    fma = fp64_fma and inst.precision == PREC_DOUBLE
+    return FLAG_MSD_GUARD | (FLAG_FMA if fma else 0)
+
+
 class _Solo:
     __slots__ = ("req", "admitted", "solver", "left", "bytes", "inflight")
 
@@ -96,7 +113,7 @@ class _Solo:
 class Server:
     def __init__(self, pool_bytes, chunk_steps=64, max_solves=8192, keep_snapshots=False,
                  solo_points=1 << 18, solo_bytes=None, order="srpt", slice_s=0.02,
-                 fp64_cost=12.0, mixed_rate=15e9):
+                 fp64_cost=12.0, mixed_rate=15e9, per_class=True, fp64_fma=True):
         if order not in ("srpt", "fifo"):
             raise ValueError("order must be 'srpt' or 'fifo'")
         self.batch = Batch(pool_bytes, max_solves)
@@ -109,6 +126,8 @@ class Server:
         self.slice_s = float(slice_s)
         self.fp64_cost = float(fp64_cost)
         self.mixed_rate = float(mixed_rate)
+        self.per_class = bool(per_class)
+        self.fp64_fma = bool(fp64_fma)
 
     def close(self):
         self.batch.close()
@@ -127,6 +146,13 @@ class Server:
         n = max(1, int(self.slice_s / per_step)) if per_step > 0 else solo.left
         return min(solo.left, n)
 
+    def _classes(self, solos):
+        """Running slots for large solves: one per precision class present
+        (per_class), or a single shared one."""
+        if not self.per_class:
+            return [0] if solos else []
+        return sorted({x.req.inst.precision for x in solos})
+
     def _key(self, r):
         return self.work(r.inst) if self.order == "srpt" else r.arrival
 
@@ -140,7 +166,7 @@ class Server:
         wait_small, wait_solo = [], []
         active = {}  # batch slot -> (request, admitted)
         solos = []   # admitted large solves
-        running = None  # the large solve with a slice in flight
+        running = {}  # precision class -> the large solve of it with a slice in flight
         batch_busy = False
         solo_used = 0
         done, rejected = [], []
@@ -193,7 +219,7 @@ class Server:
                         keep.append(r)  # waits for a large solve to retire
                         continue
                     sv = Solver(i.U.shape, method=i.method, precision=i.precision, BC=i.BC, s=i.s,
-                                a=i.a, h2=i.h * i.h, k=i.k)
+                                a=i.a, h2=i.h * i.h, k=i.k, flags=solve_flags(i, self.fp64_fma))
                     sv.upload(i.U, i.V)
                     solos.append(_Solo(r, clock(), sv, int(i.steps), need))
                     solo_used += need
@@ -203,15 +229,21 @@ class Server:
                 b.run(self.chunk_steps)
                 batch_busy = True
                 progressed = True
-            if running is None and solos:
-                running = min(solos, key=lambda x: (self.work(x.req.inst, x.left)
-                                                    if self.order == "srpt" else x.req.arrival))
-                n = self._slice_steps(running)
-                running.solver.run(n)
-                running.inflight = n
-                launches += n * running.solver.launches_per_step
+            for cls in self._classes(solos):
+                if cls in running:
+                    continue
+                mine = [x for x in solos if x.req.inst.precision == cls or not self.per_class]
+                if not mine:
+                    continue
+                x = min(mine, key=lambda x: (self.work(x.req.inst, x.left)
+                                             if self.order == "srpt" else x.req.arrival))
+                n = self._slice_steps(x)
+                x.solver.run(n)
+                x.inflight = n
+                running[cls] = x
+                launches += n * x.solver.launches_per_step
                 progressed = True
-            if (batch_busy or running is not None) and busy_since is None:
+            if (batch_busy or running) and busy_since is None:
                 busy_since = clock()
             # ---- completions
             if batch_busy and b.idle():
@@ -224,23 +256,25 @@ class Server:
                         b.remove(slot)
                         finish(r, tadm, snap, False)
                 progressed = True
-            if running is not None and running.solver.idle():
-                running.left -= running.inflight
-                running.inflight = 0
-                if running.left <= 0:
-                    snap = running.solver.download()
-                    running.solver.close()
-                    solo_used -= running.bytes
-                    solos.remove(running)
-                    finish(running.req, running.admitted, snap, True)
-                running = None
+            for cls, x in list(running.items()):
+                if not x.solver.idle():
+                    continue
+                x.left -= x.inflight
+                x.inflight = 0
+                if x.left <= 0:
+                    snap = x.solver.download()
+                    x.solver.close()
+                    solo_used -= x.bytes
+                    solos.remove(x)
+                    finish(x.req, x.admitted, snap, True)
+                del running[cls]
                 progressed = True
-            if not batch_busy and running is None and busy_since is not None:
+            if not batch_busy and not running and busy_since is not None:
                 busy += clock() - busy_since
                 busy_since = None
             if progressed:
                 continue
-            if batch_busy or running is not None:
+            if batch_busy or running:
                 time.sleep(0.0002)  # work in flight: poll again shortly
             elif pending and not wait_small and not wait_solo:
                 dt = pending[0].arrival * time_scale - clock()
@@ -252,13 +286,14 @@ class Server:
         return summarize(done, wall, busy, launches, len(rejected)), done
 
 
-def serve_sequential(requests, time_scale=1.0, keep_snapshots=False):
+def serve_sequential(requests, time_scale=1.0, keep_snapshots=False, fp64_fma=True):
     """Baseline: one solve at a time, first come first served, each through
     its own Solver (tiled 3D kernels, graph-captured chunks): create, upload,
     run all steps, download, release -- the reference's one-call-per-solve
     model without its per-call device reset.  The requests are run back to
     back; each one's latency is that of a single FIFO server fed by the same
-    arrival times (start = max(previous finish, arrival))."""
+    arrival times (start = max(previous finish, arrival)).  FP64 requests take
+    the same arithmetic as the server's large solves (solve_flags)."""
     t0 = time.perf_counter()
     done = []
     clock = 0.0
@@ -268,7 +303,7 @@ def serve_sequential(requests, time_scale=1.0, keep_snapshots=False):
         start = max(clock, arr)
         ts = time.perf_counter()
         s = Solver(i.U.shape, method=i.method, precision=i.precision, BC=i.BC, s=i.s, a=i.a,
-                   h2=i.h * i.h, k=i.k)
+                   h2=i.h * i.h, k=i.k, flags=solve_flags(i, fp64_fma))
         s.upload(i.U, i.V)
         s.run(i.steps)
         snap = s.download()

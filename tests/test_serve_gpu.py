@@ -60,7 +60,7 @@ def test_serving_solo_and_batched_results_equal_alone(gpu_lib):
     # kernels), the rest in the batched launch; each result equals the same
     # solve run alone on the same path, bit for bit
     import nlsemagic_gb300 as ng
-    from nlsemagic_gb300.serve import Server, serve_sequential
+    from nlsemagic_gb300.serve import Server, serve_sequential, solve_flags
     reqs = W.serving_requests(count=24, rate=500.0, n1=(256, 1024), n2=(32, 64), n3=(18, 30),
                               steps=(20, 60))
     srv = Server(pool_bytes=1 << 28, chunk_steps=16, keep_snapshots=True, solo_points=8000)
@@ -71,9 +71,10 @@ def test_serving_solo_and_batched_results_equal_alone(gpu_lib):
     by_id = {r.rid: r for r in reqs}
     for c in done:
         i = by_id[c.rid].inst
-        if c.solo:
+        if c.solo:  # FP64 large solves take the contracted kernels
             want = ng.take_steps(i.U, i.V, i.s, i.a, i.h * i.h, i.BC, i.steps, i.k,
-                                 method=i.method, precision=i.precision)
+                                 method=i.method, precision=i.precision,
+                                 flags=solve_flags(i, srv.fp64_fma))
         else:
             b = ng.Batch(1 << 26)
             sl = b.add(i.U, i.V, i.s, i.a, i.h * i.h, i.BC, i.steps, i.k, i.method, i.precision)
@@ -86,18 +87,25 @@ def test_serving_solo_and_batched_results_equal_alone(gpu_lib):
     for c in seq_done:
         i = by_id[c.rid].inst
         want = ng.take_steps(i.U, i.V, i.s, i.a, i.h * i.h, i.BC, i.steps, i.k, method=i.method,
-                             precision=i.precision)
+                             precision=i.precision, flags=solve_flags(i, True))
         assert bits_equal(c.snapshot, want)
 
 
 def test_serving_runs_least_remaining_work_first(gpu_lib):
-    # large 3D requests queued together run one at a time, the one with the
-    # least remaining work first, so they complete in order of their work
+    # large 3D requests queued together run one at a time (one per precision
+    # class with per_class), the one with the least remaining work first, so
+    # they complete in order of their work (within each class)
     from nlsemagic_gb300.serve import Server
-    reqs = W.serving_requests(count=6, rate=1e3, ratio=(0, 0, 1), n3=(20, 28), steps=(20, 200))
-    srv = Server(pool_bytes=1 << 28, chunk_steps=16, solo_points=1000, slice_s=1e-4)
-    summary, done = srv.serve(reqs, time_scale=0.0)
-    srv.close()
-    assert summary["requests"] == len(reqs) and all(c.solo for c in done)
-    finished = [c.rid for c in sorted(done, key=lambda c: c.done)]
-    assert finished == [r.rid for r in sorted(reqs, key=lambda r: srv.work(r.inst))]
+    reqs = W.serving_requests(count=8, rate=1e3, ratio=(0, 0, 1), n3=(20, 28), steps=(20, 200))
+    for per_class in (False, True):
+        srv = Server(pool_bytes=1 << 28, chunk_steps=16, solo_points=1000, slice_s=1e-4,
+                     per_class=per_class)
+        summary, done = srv.serve(reqs, time_scale=0.0)
+        srv.close()
+        assert summary["requests"] == len(reqs) and all(c.solo for c in done)
+        classes = (None,) if not per_class else sorted({r.inst.precision for r in reqs})
+        for cls in classes:
+            mine = [r for r in reqs if cls is None or r.inst.precision == cls]
+            ids = {r.rid for r in mine}
+            finished = [c.rid for c in sorted(done, key=lambda c: c.done) if c.rid in ids]
+            assert finished == [r.rid for r in sorted(mine, key=lambda r: srv.work(r.inst))]
