@@ -797,18 +797,30 @@ __device__ __forceinline__ void shell_coord(const ShellMap<W>& s, long long t, i
 }
 
 // ---- CD: face points in gather form ----------------------------------------
+// The point's own update operands are loaded before F (as in face2shoc).
 template <int METHOD, int BC>
 __global__ void __launch_bounds__(256) shell3d(Geom g, Args A, const ShellMap<1> sm) {
-  const float2* Ein = A.stage == 1 ? A.a.lo_in : A.a.e_in;
+  const int stage = A.stage;
+  const float2* Ein = stage == 1 ? A.a.lo_in : A.a.e_in;
   mixed::YIn Y{A.a.hi_in, Ein};
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < sm.total;
        t += (long long)gridDim.x * blockDim.x) {
     int x, y, z;
     shell_coord(sm, t, x, y, z);
-    long long p = lin(g, z, y, x);
-    float2 T = mixed::f_at<3, METHOD, BC>(g, A.c, Y, A.a.V, z, y, x);
-    mixed::update(A.c, A.stage, p, T, A.a.hi_in, A.a.lo_in, A.a.e_in, A.a.K, A.a.e_out,
-                  A.a.hi_out, A.a.lo_out);
+    const long long p = lin(g, z, y, x);
+    const mixed::HE u = Y.at(p);
+    const float2 lo = stage == 1 ? u.e : A.a.lo_in[p];
+    const float2 kv = stage == 4 ? A.a.K[p] : lo;
+    const float2 T = mixed::f_at<3, METHOD, BC>(g, A.c, Y, A.a.V, z, y, x);
+    float2 eo, ko, ho, lo2;
+    mixed::stage_update(A.c, stage, T, u.h, lo, u.e, kv, eo, ko, ho, lo2);
+    if (stage == 2) A.a.K[p] = ko;
+    if (stage < 4) {
+      A.a.e_out[p] = eo;
+    } else {
+      A.a.hi_out[p] = ho;
+      A.a.lo_out[p] = lo2;
+    }
   }
 }
 
@@ -955,11 +967,17 @@ __global__ void __launch_bounds__(256) ghost3d(Geom g, Args A, const ShellMap<1>
 }
 
 // ---- 2SHOC: face points ------------------------------------------------------
+// Every input of a face point -- its stencil operands and its own lo, K and
+// V -- is loaded before any arithmetic, so the point costs one memory round
+// trip rather than two (the update's operands do not depend on F).  Same
+// arithmetic as mixed::update, so the same bits.  32 registers: the 8 blocks
+// per SM of the launch (face.blocks_per_sm) stay resident.
 template <int BC>
-__global__ void __launch_bounds__(256) face2shoc(Geom g, Args A, const ShellMap<1> sm) {
+__global__ void __launch_bounds__(256, 8) face2shoc(Geom g, Args A, const ShellMap<1> sm) {
   pdl_wait();  // F next to the faces and the interior points of this stage
   pdl_trigger();
-  const float2* Ein = A.stage == 1 ? A.a.lo_in : A.a.e_in;
+  const int stage = A.stage;
+  const float2* Ein = stage == 1 ? A.a.lo_in : A.a.e_in;
   mixed::YIn Y{A.a.hi_in, Ein};
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < sm.total;
        t += (long long)gridDim.x * blockDim.x) {
@@ -971,9 +989,20 @@ __global__ void __launch_bounds__(256) face2shoc(Geom g, Args A, const ShellMap<
     const long long q = lin(g, qi, qj, qk);
     const mixed::HE ub = Y.at(p), uq = Y.at(q);
     const float2 fq = BC == 2 ? A.a.fq[q] : make_float2(0.f, 0.f);
-    const float2 T = mixed::f_boundary<2, BC>(A.c, ub, A.a.V[p], uq, fq, nullptr);
-    mixed::update(A.c, A.stage, p, T, A.a.hi_in, A.a.lo_in, A.a.e_in, A.a.K, A.a.e_out,
-                  A.a.hi_out, A.a.lo_out);
+    const float v = A.a.V[p];
+    // stage 1: E = lo; stages 2-4 read lo itself (hi and E are ub's)
+    const float2 lo = stage == 1 ? ub.e : A.a.lo_in[p];
+    const float2 kv = stage == 4 ? A.a.K[p] : lo;
+    const float2 T = mixed::f_boundary<2, BC>(A.c, ub, v, uq, fq, nullptr);
+    float2 eo, ko, ho, lo2;
+    mixed::stage_update(A.c, stage, T, ub.h, lo, ub.e, kv, eo, ko, ho, lo2);
+    if (stage == 2) A.a.K[p] = ko;
+    if (stage < 4) {
+      A.a.e_out[p] = eo;
+    } else {
+      A.a.hi_out[p] = ho;
+      A.a.lo_out[p] = lo2;
+    }
   }
 }
 

@@ -200,8 +200,8 @@ __device__ __noinline__ void seg_mixed(const BSolve& s, int stage, int par, long
                                    *reinterpret_cast<seg1d::Smem<SEG1>*>(smem));
 }
 
-// mixed 2D rectangle t (single pass)
-template <int METHOD, int BC, int STAGE>
+// mixed 2D rectangle t (single pass); PREF as wide2d::tile
+template <int METHOD, int BC, int STAGE, bool PREF>
 __device__ __noinline__ void rect_mixed(const BSolve& s, int par, long long t, void* smem) {
   const MixedIO io = mixed_io(s, STAGE, par);
   const MixedStageArgs a{io.hi_in, io.lo_in, io.d_in, io.V,    io.K,   io.d_out,
@@ -209,37 +209,38 @@ __device__ __noinline__ void rect_mixed(const BSolve& s, int par, long long t, v
   const int sx = wide2d::shift(s.g.M, wide2d::TX), sy = wide2d::shift(s.g.N, W2_TY);
   const int nbx = (s.g.M + sx + wide2d::TX - 1) / wide2d::TX;
   // constants read from the descriptor in shared memory
-  wide2d::tile<METHOD, BC, STAGE, W2_TY, true>(s.g, a, s.cf, (int)(t % nbx), (int)(t / nbx), sx,
-                                               sy, *reinterpret_cast<wide2d::Smem<W2_TY>*>(smem));
+  wide2d::tile<METHOD, BC, STAGE, W2_TY, true, PREF>(
+      s.g, a, s.cf, (int)(t % nbx), (int)(t / nbx), sx, sy,
+      *reinterpret_cast<wide2d::Smem<W2_TY>*>(smem));
 }
 
-template <int METHOD, int BC>
+template <int METHOD, int BC, bool PREF>
 __device__ __forceinline__ void rect_by_stage(const BSolve& s, int stage, int par, long long t,
                                               void* smem) {
   switch (stage) {
-    case 1: rect_mixed<METHOD, BC, 1>(s, par, t, smem); break;
-    case 2: rect_mixed<METHOD, BC, 2>(s, par, t, smem); break;
-    case 3: rect_mixed<METHOD, BC, 3>(s, par, t, smem); break;
-    default: rect_mixed<METHOD, BC, 4>(s, par, t, smem); break;
+    case 1: rect_mixed<METHOD, BC, 1, PREF>(s, par, t, smem); break;
+    case 2: rect_mixed<METHOD, BC, 2, PREF>(s, par, t, smem); break;
+    case 3: rect_mixed<METHOD, BC, 3, PREF>(s, par, t, smem); break;
+    default: rect_mixed<METHOD, BC, 4, PREF>(s, par, t, smem); break;
   }
 }
 
 // segment / rectangle tiles of the mixed class (BC 1-3)
-template <int METHOD>
+template <int METHOD, bool PREF>
 __device__ void staged_tile(const BSolve& s, int kind, int stage, int par, long long t,
                             void* smem) {
   switch (s.bc) {
     case 1:
       if (kind == K_SEG1D) seg_mixed<METHOD, 1>(s, stage, par, t, smem);
-      else rect_by_stage<METHOD, 1>(s, stage, par, t, smem);
+      else rect_by_stage<METHOD, 1, PREF>(s, stage, par, t, smem);
       break;
     case 2:
       if (kind == K_SEG1D) seg_mixed<METHOD, 2>(s, stage, par, t, smem);
-      else rect_by_stage<METHOD, 2>(s, stage, par, t, smem);
+      else rect_by_stage<METHOD, 2, PREF>(s, stage, par, t, smem);
       break;
     default:
       if (kind == K_SEG1D) seg_mixed<METHOD, 3>(s, stage, par, t, smem);
-      else rect_by_stage<METHOD, 3>(s, stage, par, t, smem);
+      else rect_by_stage<METHOD, 3, PREF>(s, stage, par, t, smem);
       break;
   }
 }
@@ -378,8 +379,8 @@ __global__ void __launch_bounds__(BT, batch_min_blocks<CLS, STAGED>()) batch_ker
             bool done = false;
             if constexpr (CLS == NLSE_PREC_MIXED) {
               if (tl.kind != K_LINEAR) {  // single pass: phase 1 only
-                if (s.method == 1) staged_tile<1>(s, tl.kind, stage, par, tl.start, smem);
-                else staged_tile<2>(s, tl.kind, stage, par, tl.start, smem);
+                if (s.method == 1) staged_tile<1, STAGED>(s, tl.kind, stage, par, tl.start, smem);
+                else staged_tile<2, STAGED>(s, tl.kind, stage, par, tl.start, smem);
                 done = true;
               }
             }

@@ -17,6 +17,11 @@ __device__ __forceinline__ void cp_async(void* sdst, const void* gsrc, bool vali
                : "memory");
 }
 
+// Hint: fetch the line holding p into L2 (no register receives it).
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];\n" ::"l"(p));
+}
+
 // Wait for all of this thread's copies; a block barrier after it makes every
 // thread's copies visible to the block.
 __device__ __forceinline__ void cp_async_wait_all() {
