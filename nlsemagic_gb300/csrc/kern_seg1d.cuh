@@ -65,6 +65,16 @@ __device__ __forceinline__ void segment(const Geom& g, const Consts<float>& c, c
     cp_async<8>(&sh[i], io.hi_in + (in ? x : 0), in);
     cp_async<8>(&se[i], E + (in ? x : 0), in);
   }
+  // the points' own inputs, loaded at their update: towards L2 now, so that
+  // their DRAM latency overlaps the staging (the uneven batch: 25.2 against
+  // 24.8 Gpt-steps/s)
+  for (int r = 0; r < SEG / NT; ++r) {
+    const int x = x0 + tid + NT * r;
+    if (x < 0 || x >= n) continue;
+    prefetch_l2(io.V + x);
+    prefetch_l2(io.lo_in + x);
+    if (stage == 4) prefetch_l2(io.K + x);
+  }
   cp_async_wait_all();
   __syncthreads();
   auto Y = [&](int x) -> HE {
