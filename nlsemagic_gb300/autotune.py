@@ -114,17 +114,30 @@ def candidates(shape, precision):
     return cands
 
 
-def time_config(shape, method, precision, BC, cfg, steps, h=0.3, reps=2):
-    for k, v in cfg.items():
-        set_knob(k, v)
+def _solver_for(shape, method, precision, BC, h=0.3):
     U, V = _smooth_state(shape, h)
     ndim, _ = grid_dims(shape)
     from .workloads import linear_stability_k
     k = 0.5 * linear_stability_k(ndim, method, h, 1.0)
-    with Solver(shape, method=method, precision=precision, BC=BC, s=-1.0, a=1.0, h2=h * h,
-                k=k) as s:
-        s.upload(U, V)
-        s.run(max(1, cfg.get("graph.steps", 8)))  # capture outside the timing
+    sv = Solver(shape, method=method, precision=precision, BC=BC, s=-1.0, a=1.0, h2=h * h, k=k)
+    sv.upload(U, V)
+    return sv
+
+
+def time_config(shape, method, precision, BC, cfg, steps, reps=2, solver=None):
+    """Best of reps timings of `steps` RK4 steps with the knobs of cfg.  A
+    given solver is reused: its graphs are captured again under cfg (the
+    knobs are read at capture; none of them changes what the solver
+    allocates)."""
+    for k, v in cfg.items():
+        set_knob(k, v)
+    own = solver is None
+    s = _solver_for(shape, method, precision, BC) if own else solver
+    try:
+        gs = max(1, cfg.get("graph.steps", 8))
+        s.set_graph_steps(0)   # drop the graphs captured under other knobs
+        s.set_graph_steps(gs)
+        s.run(gs)  # capture outside the timing
         s.sync()
         best = float("inf")
         for _ in range(reps):
@@ -132,24 +145,30 @@ def time_config(shape, method, precision, BC, cfg, steps, h=0.3, reps=2):
             s.run(steps)
             s.sync()
             best = min(best, time.perf_counter() - t0)
+    finally:
+        if own:
+            s.close()
     return best
 
 
 def tune(shape, method=2, precision=3, BC=2, steps=20, force=False, verbose=False):
-    """Time every candidate, cache and return the best configuration."""
+    """Time every candidate (one solver, its graphs captured again for each),
+    cache and return the best configuration."""
     key = problem_key(shape, method, precision, BC)
     cache = _load_cache()
     if key in cache and not force:
         return cache[key]
     saved = {k: get_knob(k) for k in KNOBS}
     results = []
+    sv = _solver_for(shape, method, precision, BC)
     try:
         for cfg in candidates(shape, precision):
-            t = time_config(shape, method, precision, BC, cfg, steps)
+            t = time_config(shape, method, precision, BC, cfg, steps, solver=sv)
             results.append((t, cfg))
             if verbose:
                 print("%-40s %.4f s" % (cfg, t))
     finally:
+        sv.close()
         for k, v in saved.items():
             set_knob(k, v)
     t, best = min(results, key=lambda r: r[0])
