@@ -86,10 +86,10 @@ typedef struct nlse_problem {
  * where the compiler forms them.  No reference counterpart.  The results are
  * no longer the reference's bits but stay within 1e-12 relative L2 of them
  * over the benchmark runs; the FP64 class is bound by FP64 issue, and
- * contraction removes instructions.  Honoured by the one-shot calls and
- * the resident solver; nlse_batch_add rejects it (the batched launch
- * computes FP64 without contraction), and nlse_take_steps_noalloc computes
- * without contraction. */
+ * contraction removes instructions.  Honoured by the one-shot calls, the
+ * resident solver and nlse_batch_add (such FP64 solves run in a launch of
+ * their own on a contracted copy of the batch kernel);
+ * nlse_take_steps_noalloc computes without contraction. */
 #define NLSE_FLAG_FMA 4
 
 const char *nlse_last_error_string(void);

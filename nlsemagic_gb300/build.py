@@ -40,6 +40,7 @@ UNITS = {
     "kern_small_mixed.cu": [],
     "kern_probe.cu": [],
     "kern_exact_fma.cu": [],  # contracted FP64 (NLSE_FLAG_FMA): -fmad left on
+    "nlse_batch_fma.cu": [],  # the batched launch's contracted FP64 kernel
 }
 
 

@@ -1,7 +1,7 @@
 // Batched solves in one persistent launch (C ABI: nlse_batch_* in
 // include/nlse_gb300.h).
 //
-// Device side: a cooperative persistent kernel.  All active solves are cut
+// Device side (batch_kern.cuh): a cooperative persistent kernel.  All active solves are cut
 // into tiles; per RK4 stage every CTA pulls tiles from an atomic work-queue
 // counter of that stage until the queue is empty, evaluates the stage on the
 // tile, and then waits at a grid barrier.  Tiles by solve:
@@ -22,6 +22,8 @@
 //
 // This unit is compiled with -fmad=false so that the FP64 solves are
 // bit-identical to the single-solve path and to the reference integrators.
+// FP64 solves added with NLSE_FLAG_FMA form a third class, launched on the
+// contracted copy of the kernel (nlse_batch_fma.cu).
 #include <stdio.h>
 #include <string.h>
 
@@ -29,383 +31,14 @@
 #include <mutex>
 #include <vector>
 
-#include "../../include/nlse_gb300.h"
-#include "kern_gather.cuh"
-#include "kern_seg1d.cuh"
-#include "kern_wide2d.cuh"
-#include "nlse_launch.h"
+#include "batch_kern.cuh"
 
-using namespace nlse;
-
-namespace {
-
-constexpr int TILE = 1024;
-constexpr int BT = 256;  // threads per CTA
-// Tile sizes: 32 x 32 rectangles and 1024-point segments (on the uneven
-// 512-solve batch 23.6 Gpt-steps/s, against 19.4 with 32 x 16 rectangles
-// and 19.5 with those and 512-point segments).
-constexpr int W2_TY = 32;  // height of the 2D rectangles
-static_assert(BT == wide2d::NT && BT == seg1d::NT, "tile functions take 256 threads");
-
-// tile kinds
-enum { K_LINEAR = 0, K_SEG1D = 1, K_RECT2D = 2 };
-
-// shared memory of the mixed class's segment and rectangle tiles
-constexpr int SEG1 = 1024;  // points of a 1D segment
-constexpr size_t SMEM_TILE = sizeof(seg1d::Smem<SEG1>) > sizeof(wide2d::Smem<W2_TY>)
-                                 ? sizeof(seg1d::Smem<SEG1>)
-                                 : sizeof(wide2d::Smem<W2_TY>);
-
-struct BSolve {
-  Geom g;
-  int method, bc, prec, cur;
-  long long steps_left;  // steps this solve still runs when the launch starts
-  Consts<double> cd;
-  Consts<float> cf;
-  void* buf[8];
-  // exact: psi, K, ya, yb, V ; mixed: hi0, hi1, lo0, lo1, K, da, db, V
-  void* dsc;  // 2SHOC: the stage's D at every point (C2<double> / float2), else null
-};
-
-struct BTile {
-  int solve;
-  int kind;         // K_LINEAR: start = first point; K_SEG1D / K_RECT2D: start = tile index
-  long long start;
-};
-
-// the kind of tile a solve is cut into
-static int tile_kind(const BSolve& d) {
-  if (d.prec != NLSE_PREC_MIXED || d.bc == 4) return K_LINEAR;
-  if (d.g.ndim == 1) return K_SEG1D;
-  if (d.g.ndim == 2) return K_RECT2D;
-  return K_LINEAR;
-}
-
-static long long tile_count(const BSolve& d) {
-  switch (tile_kind(d)) {
-    case K_SEG1D: return seg1d::segments<SEG1>(d.g.n);
-    case K_RECT2D: return wide2d::tiles(d.g, W2_TY);
-    default: return (d.g.n + TILE - 1) / TILE;
-  }
-}
-
-// ---------------------------------------------------------------- device --
-// Per RK4 stage a 2SHOC solve runs two phases: D at every point into dsc
-// (d_at, boundary-condition D on the faces), then -- after a grid barrier --
-// F from those D values and the stage update (f_at_d).  CD solves only run
-// the second phase.  Both phases evaluate the gather-form expressions, so
-// the results equal the single-solve kernels' bit for bit.
-
-// exact (FP64) stage input / output buffers of a stage
-struct ExactIO {
-  C2<double> *psi, *K, *Yout;
-  const C2<double>* Yin;
-  const double* V;
-};
-__device__ __forceinline__ ExactIO exact_io(const BSolve& s, int stage) {
-  typedef C2<double> T2;
-  ExactIO io;
-  io.psi = (T2*)s.buf[0];
-  io.K = (T2*)s.buf[1];
-  T2* ya = (T2*)s.buf[2];
-  T2* yb = (T2*)s.buf[3];
-  io.V = (const double*)s.buf[4];
-  io.Yin = stage == 1 ? io.psi : (stage == 3 ? yb : ya);
-  io.Yout = stage == 2 ? yb : ya;
-  return io;
-}
-
-struct MixedIO {
-  const float2 *hi_in, *lo_in, *d_in;
-  float2 *hi_out, *lo_out, *K, *d_out;
-  const float* V;
-};
-__device__ __forceinline__ MixedIO mixed_io(const BSolve& s, int stage, int par) {
-  MixedIO io;
-  io.hi_in = (const float2*)s.buf[par];
-  io.lo_in = (const float2*)s.buf[2 + par];
-  io.hi_out = (float2*)s.buf[1 - par];
-  io.lo_out = (float2*)s.buf[3 - par];
-  io.K = (float2*)s.buf[4];
-  float2* da = (float2*)s.buf[5];
-  float2* db = (float2*)s.buf[6];
-  io.V = (const float*)s.buf[7];
-  io.d_in = stage == 3 ? db : da;
-  io.d_out = stage == 2 ? db : da;
-  return io;
-}
-
-template <int DIM, int BC>
-__device__ __noinline__ void dtile_exact(const BSolve& s, int stage, long long p0, long long p1) {
-  const ExactIO io = exact_io(s, stage);
-  const Consts<double>& c = s.cd;
-  C2<double>* D = (C2<double>*)s.dsc;
-  for (long long p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
-    int i, j, k;
-    decompose(s.g, p, i, j, k);
-    D[p] = exact::d_at<double, DIM, BC>(s.g, c, io.Yin, io.V, i, j, k);
-  }
-}
-
-template <int DIM, int METHOD, int BC>
-__device__ __noinline__ void ftile_exact(const BSolve& s, int stage, long long p0, long long p1) {
-  const ExactIO io = exact_io(s, stage);
-  const Consts<double>& c = s.cd;
-  const C2<double>* D = (const C2<double>*)s.dsc;
-  for (long long p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
-    int i, j, k;
-    decompose(s.g, p, i, j, k);
-    C2<double> T = METHOD == 2 ? exact::f_at_d<double, DIM, BC>(s.g, c, io.Yin, io.V, D, i, j, k)
-                               : exact::f_at<double, DIM, 1, BC>(s.g, c, io.Yin, io.V, i, j, k);
-    exact::update<double>(c, stage, p, T, io.psi, io.K, io.Yout);
-  }
-}
-
-template <int DIM, int BC>
-__device__ __noinline__ void dtile_mixed(const BSolve& s, int stage, int par, long long p0,
-                                         long long p1) {
-  const MixedIO io = mixed_io(s, stage, par);
-  mixed::YIn Y{io.hi_in, stage == 1 ? io.lo_in : io.d_in};
-  float2* D = (float2*)s.dsc;
-  for (long long p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
-    int i, j, k;
-    decompose(s.g, p, i, j, k);
-    D[p] = mixed::d_at<DIM, BC>(s.g, s.cf, Y, io.V, i, j, k);
-  }
-}
-
-template <int DIM, int METHOD, int BC>
-__device__ __noinline__ void ftile_mixed(const BSolve& s, int stage, int par, long long p0,
-                                         long long p1) {
-  const MixedIO io = mixed_io(s, stage, par);
-  mixed::YIn Y{io.hi_in, stage == 1 ? io.lo_in : io.d_in};
-  const float2* D = (const float2*)s.dsc;
-  for (long long p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
-    int i, j, k;
-    decompose(s.g, p, i, j, k);
-    float2 T = METHOD == 2 ? mixed::f_at_d<DIM, BC>(s.g, s.cf, Y, io.V, D, i, j, k)
-                           : mixed::f_at<DIM, 1, BC>(s.g, s.cf, Y, io.V, i, j, k);
-    mixed::update(s.cf, stage, p, T, io.hi_in, io.lo_in, io.d_in, io.K, io.d_out, io.hi_out,
-                  io.lo_out);
-  }
-}
-
-// mixed 1D segment t (single pass)
-template <int METHOD, int BC>
-__device__ __noinline__ void seg_mixed(const BSolve& s, int stage, int par, long long t,
-                                       void* smem) {
-  const MixedIO io = mixed_io(s, stage, par);
-  const seg1d::IO sio{io.hi_in, io.lo_in, io.d_in, io.V, io.K, io.d_out, io.hi_out, io.lo_out};
-  seg1d::segment<METHOD, BC, SEG1>(s.g, s.cf, sio, stage, t,
-                                   *reinterpret_cast<seg1d::Smem<SEG1>*>(smem));
-}
-
-// mixed 2D rectangle t (single pass); PREF as wide2d::tile
-template <int METHOD, int BC, int STAGE, bool PREF>
-__device__ __noinline__ void rect_mixed(const BSolve& s, int par, long long t, void* smem) {
-  const MixedIO io = mixed_io(s, STAGE, par);
-  const MixedStageArgs a{io.hi_in, io.lo_in, io.d_in, io.V,    io.K,   io.d_out,
-                         io.hi_out, io.lo_out, nullptr, nullptr, nullptr};
-  const int sx = wide2d::shift(s.g.M, wide2d::TX), sy = wide2d::shift(s.g.N, W2_TY);
-  const int nbx = (s.g.M + sx + wide2d::TX - 1) / wide2d::TX;
-  // constants read from the descriptor in shared memory
-  wide2d::tile<METHOD, BC, STAGE, W2_TY, true, PREF>(
-      s.g, a, s.cf, (int)(t % nbx), (int)(t / nbx), sx, sy,
-      *reinterpret_cast<wide2d::Smem<W2_TY>*>(smem));
-}
-
-template <int METHOD, int BC, bool PREF>
-__device__ __forceinline__ void rect_by_stage(const BSolve& s, int stage, int par, long long t,
-                                              void* smem) {
-  switch (stage) {
-    case 1: rect_mixed<METHOD, BC, 1, PREF>(s, par, t, smem); break;
-    case 2: rect_mixed<METHOD, BC, 2, PREF>(s, par, t, smem); break;
-    case 3: rect_mixed<METHOD, BC, 3, PREF>(s, par, t, smem); break;
-    default: rect_mixed<METHOD, BC, 4, PREF>(s, par, t, smem); break;
-  }
-}
-
-// segment / rectangle tiles of the mixed class (BC 1-3)
-template <int METHOD, bool PREF>
-__device__ void staged_tile(const BSolve& s, int kind, int stage, int par, long long t,
-                            void* smem) {
-  switch (s.bc) {
-    case 1:
-      if (kind == K_SEG1D) seg_mixed<METHOD, 1>(s, stage, par, t, smem);
-      else rect_by_stage<METHOD, 1, PREF>(s, stage, par, t, smem);
-      break;
-    case 2:
-      if (kind == K_SEG1D) seg_mixed<METHOD, 2>(s, stage, par, t, smem);
-      else rect_by_stage<METHOD, 2, PREF>(s, stage, par, t, smem);
-      break;
-    default:
-      if (kind == K_SEG1D) seg_mixed<METHOD, 3>(s, stage, par, t, smem);
-      else rect_by_stage<METHOD, 3, PREF>(s, stage, par, t, smem);
-      break;
-  }
-}
-
-// phase 0: D (2SHOC solves), phase 1: F + update
-template <int CLS, int DIM, int METHOD, int BC>
-__device__ __forceinline__ void tile_one(const BSolve& s, int ph, int stage, int par, long long p0,
-                                         long long p1) {
-  if (CLS == NLSE_PREC_DOUBLE) {
-    if (ph == 0) dtile_exact<DIM, BC>(s, stage, p0, p1);
-    else ftile_exact<DIM, METHOD, BC>(s, stage, p0, p1);
-  } else {
-    if (ph == 0) dtile_mixed<DIM, BC>(s, stage, par, p0, p1);
-    else ftile_mixed<DIM, METHOD, BC>(s, stage, par, p0, p1);
-  }
-}
-
-template <int CLS, int DIM, int METHOD>
-__device__ void by_bc(const BSolve& s, int ph, int stage, int par, long long p0, long long p1) {
-  switch (s.bc) {
-    case 1: tile_one<CLS, DIM, METHOD, 1>(s, ph, stage, par, p0, p1); break;
-    case 2: tile_one<CLS, DIM, METHOD, 2>(s, ph, stage, par, p0, p1); break;
-    case 3: tile_one<CLS, DIM, METHOD, 3>(s, ph, stage, par, p0, p1); break;
-    default:
-      if (DIM == 1) tile_one<CLS, 1, METHOD, 4>(s, ph, stage, par, p0, p1);
-      break;
-  }
-}
-
-template <int CLS>
-__device__ void process_tile(const BSolve& s, int ph, int stage, int par, long long p0,
-                             long long p1) {
-  if (s.method == 1) {
-    if (s.g.ndim == 1) by_bc<CLS, 1, 1>(s, ph, stage, par, p0, p1);
-    else if (s.g.ndim == 2) by_bc<CLS, 2, 1>(s, ph, stage, par, p0, p1);
-    else by_bc<CLS, 3, 1>(s, ph, stage, par, p0, p1);
-  } else {
-    if (s.g.ndim == 1) by_bc<CLS, 1, 2>(s, ph, stage, par, p0, p1);
-    else if (s.g.ndim == 2) by_bc<CLS, 2, 2>(s, ph, stage, par, p0, p1);
-    else by_bc<CLS, 3, 2>(s, ph, stage, par, p0, p1);
-  }
-}
-
-struct BarrierState {
-  unsigned count;
-  unsigned gen;
-};
-
-// Grid barrier with a bounded wait.  All CTAs are co-resident (cooperative
-// launch).  Returns false if the wait budget ran out (error word set).
-__device__ bool grid_barrier(BarrierState* bar, int* err, long long budget) {
-  __shared__ int s_ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    s_ok = 1;
-    volatile unsigned* vgen = &bar->gen;
-    unsigned g = *vgen;
-    __threadfence();
-    unsigned arrived = atomicAdd(&bar->count, 1u);
-    if (arrived == gridDim.x - 1) {
-      bar->count = 0;
-      __threadfence();
-      atomicAdd(&bar->gen, 1u);
-    } else {
-      long long t0 = clock64();
-      while (*vgen == g) {
-        if (*(volatile int*)err) {
-          s_ok = 0;
-          break;
-        }
-        if (clock64() - t0 > budget) {
-          atomicExch(err, NLSE_ERR_TIMEOUT);
-          s_ok = 0;
-          break;
-        }
-        __nanosleep(64);
-      }
-    }
-    __threadfence();
-  }
-  __syncthreads();
-  return s_ok != 0;
-}
-
-// One launch per precision class.  tiles[0, ntiles_d) are the tiles of the
-// 2SHOC solves in gather form (phase 0 runs over them), tiles[0, ntiles) all
-// tiles.  STAGED: every tile is a segment or a rectangle (mixed class).
-// Resident CTAs per SM the kernels are compiled for: the general kernels
-// at 3 (FP64) and 4 (mixed: the gather paths fit 64 registers), and the
-// mixed kernel for runs whose solves all take segment or rectangle tiles at
-// 6 (40 registers; latency of the per-tile barriers hidden by more CTAs:
-// 20.5 against 15.7 Gpt-steps/s on the uneven 512-solve batch).
-template <int CLS, bool STAGED>
-constexpr int batch_min_blocks() {
-  return CLS == NLSE_PREC_MIXED ? (STAGED ? 6 : 4) : 3;
-}
-
-template <int CLS, bool STAGED>
-__global__ void __launch_bounds__(BT, batch_min_blocks<CLS, STAGED>()) batch_kernel(const BSolve* __restrict__ solves,
-                                                      const BTile* __restrict__ tiles, int ntiles,
-                                                      int ntiles_d, int steps, unsigned* qctr,
-                                                      BarrierState* bar, int* err,
-                                                      long long budget) {
-  __shared__ BSolve s;
-  __shared__ int s_solve;      // the solve whose descriptor s holds (-1: none)
-  __shared__ BTile s_tile[2];  // this tile and the next one claimed (solve -1: queue empty)
-  __shared__ __align__(16) unsigned char smem[CLS == NLSE_PREC_MIXED ? SMEM_TILE : 16];
-  if (threadIdx.x == 0) s_solve = -1;
-  for (int step = 0; step < steps; ++step) {
-    for (int stage = 1; stage <= 4; ++stage) {
-      for (int ph = ntiles_d > 0 ? 0 : 1; ph < 2; ++ph) {
-        const int pass = (step * 4 + stage - 1) * 2 + ph;
-        const int nt = ph == 0 ? ntiles_d : ntiles;
-        if (threadIdx.x == 0) {
-          const int t = (int)atomicAdd(&qctr[pass], 1u);
-          s_tile[0] = t < nt ? tiles[t] : BTile{-1, 0, 0};
-        }
-        __syncthreads();
-        for (int it = 0;; ++it) {
-          const BTile tl = s_tile[it & 1];
-          if (tl.solve < 0) break;
-          // claim the next tile now; its record is stored when this one is done
-          unsigned nx = 0;
-          if (threadIdx.x == 0) nx = atomicAdd(&qctr[pass], 1u);
-          if (tl.solve != s_solve) {
-            __syncthreads();  // every thread has compared s_solve
-            const int* src = reinterpret_cast<const int*>(&solves[tl.solve]);
-            int* dst = reinterpret_cast<int*>(&s);
-            for (int w = threadIdx.x; w < (int)(sizeof(BSolve) / sizeof(int)); w += blockDim.x)
-              dst[w] = src[w];
-            if (threadIdx.x == 0) s_solve = tl.solve;
-            __syncthreads();
-          }
-          if (step < s.steps_left) {
-            const int par = s.cur ^ (step & 1);
-            bool done = false;
-            if constexpr (CLS == NLSE_PREC_MIXED) {
-              if (tl.kind != K_LINEAR) {  // single pass: phase 1 only
-                if (s.method == 1) staged_tile<1, STAGED>(s, tl.kind, stage, par, tl.start, smem);
-                else staged_tile<2, STAGED>(s, tl.kind, stage, par, tl.start, smem);
-                done = true;
-              }
-            }
-            if constexpr (!STAGED) {
-              if (!done) {
-                long long p1 = tl.start + TILE;
-                if (p1 > s.g.n) p1 = s.g.n;
-                process_tile<CLS>(s, ph, stage, par, tl.start, p1);
-              }
-            }
-          }
-          if (threadIdx.x == 0) s_tile[(it + 1) & 1] = (int)nx < nt ? tiles[nx] : BTile{-1, 0, 0};
-          __syncthreads();
-        }
-        if (!grid_barrier(bar, err, budget)) return;
-      }
-    }
-  }
-}
-
-}  // namespace
-
-// Shared with nlse_abi.cu: error reporting, validation, scalar constants.
+// Shared with nlse_abi.cu: error reporting, validation, scalar constants;
+// from nlse_batch_fma.cu: the contracted FP64 kernel.
 namespace nlse {
 int set_error(int code, const char* fmt, ...);
+int batch_fma_blocks_per_sm();
+cudaError_t batch_fma_launch(unsigned blocks, void** args, cudaStream_t st);
 }
 int nlse_validate_problem(const nlse_problem* p);
 void nlse_fill_consts(const nlse_problem* p, void* cd, void* cf);
@@ -451,7 +84,8 @@ struct nlse_batch {
   // staging for transfers (planar doubles)
   double* stage = nullptr;
   size_t stage_cap = 0;
-  int max_blocks[3] = {0, 0, 0};  // FP64, mixed, mixed with staged tiles only
+  // resident CTAs: FP64, mixed, mixed with staged tiles only, contracted FP64
+  int max_blocks[4] = {0, 0, 0, 0};
   int last_launches = 0;
 };
 
@@ -565,11 +199,13 @@ extern "C" int nlse_batch_create(long long pool_bytes, int max_solves, nlse_batc
                                                 BT, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perst, batch_kernel<NLSE_PREC_MIXED, true>,
                                                 BT, 0);
-  if (per64 < 1 || permx < 1 || perst < 1)
+  const int perfma = nlse::batch_fma_blocks_per_sm();
+  if (per64 < 1 || permx < 1 || perst < 1 || perfma < 1)
     return cleanup(nlse::set_error(NLSE_ERR_CUDA, "batch kernel cannot be resident"));
   b->max_blocks[0] = sms * per64;
   b->max_blocks[1] = sms * permx;
   b->max_blocks[2] = sms * perst;
+  b->max_blocks[3] = sms * perfma;
   *out = b;
   return NLSE_OK;
 }
@@ -590,10 +226,6 @@ extern "C" int nlse_batch_add(nlse_batch* b, const nlse_problem* p, const double
   if (nsteps < 0) return nlse::set_error(NLSE_ERR_ARG, "nsteps must be >= 0");
   if (p->precision != NLSE_PREC_DOUBLE && p->precision != NLSE_PREC_MIXED)
     return nlse::set_error(NLSE_ERR_ARG, "batched solves are FP64 or mixed precision");
-  if (p->flags & NLSE_FLAG_FMA)
-    return nlse::set_error(NLSE_ERR_ARG,
-                           "the batched launch computes FP64 without contraction "
-                           "(NLSE_FLAG_FMA is for single solves)");
   {
     int rc = nlse_validate_problem(p);  // same rules as single solves
     if (rc) return rc;
@@ -674,17 +306,18 @@ extern "C" int nlse_batch_run(nlse_batch* b, int max_steps) {
   int err = 0;
   BTRY(cudaMemcpy(&err, b->d_err, sizeof(int), cudaMemcpyDeviceToHost));
   if (err) return nlse::set_error(err, "a previous batch launch gave up waiting at a grid barrier");
-  // per class: the solves that still run, those with a D phase (2SHOC in
-  // gather form) first; steps = longest advance
-  std::vector<int> which[2];
-  long long ntiles[2] = {0, 0}, ntiles_d[2] = {0, 0};
-  int steps[2] = {0, 0};
+  // per class (FP64, mixed, contracted FP64): the solves that still run,
+  // those with a D phase (2SHOC in gather form) first; steps = longest advance
+  constexpr int NC = 3;
+  std::vector<int> which[NC];
+  long long ntiles[NC] = {0, 0, 0}, ntiles_d[NC] = {0, 0, 0};
+  int steps[NC] = {0, 0, 0};
   for (int pass = 0; pass < 2; ++pass)  // D-phase solves, then the others
     for (size_t t = 0; t < b->slots.size(); ++t) {
       Slot& S = b->slots[t];
       const bool dphase = S.d.method == 2 && tile_kind(S.d) == K_LINEAR;
       if (!S.used || S.d.steps_left <= 0 || dphase != (pass == 0)) continue;
-      const int c = S.d.prec == NLSE_PREC_DOUBLE ? 0 : 1;
+      const int c = S.d.prec != NLSE_PREC_DOUBLE ? 1 : (S.prob.flags & NLSE_FLAG_FMA) ? 2 : 0;
       which[c].push_back((int)t);
       const long long nt = tile_count(S.d);
       ntiles[c] += nt;
@@ -692,8 +325,10 @@ extern "C" int nlse_batch_run(nlse_batch* b, int max_steps) {
       long long adv = S.d.steps_left < max_steps ? S.d.steps_left : max_steps;
       if (adv > steps[c]) steps[c] = (int)adv;
     }
-  const long long total_tiles = ntiles[0] + ntiles[1];
-  if (total_tiles == 0 || (steps[0] == 0 && steps[1] == 0)) return NLSE_OK;
+  const long long total_tiles = ntiles[0] + ntiles[1] + ntiles[2];
+  int max_adv = 0;
+  for (int c = 0; c < NC; ++c) max_adv = steps[c] > max_adv ? steps[c] : max_adv;
+  if (total_tiles == 0 || max_adv == 0) return NLSE_OK;
   if (total_tiles > (1LL << 31) - 1) return nlse::set_error(NLSE_ERR_CAPACITY, "too many tiles");
   if ((size_t)total_tiles > b->tiles_cap) {
     if (b->d_tiles) cudaFree(b->d_tiles);
@@ -705,17 +340,17 @@ extern "C" int nlse_batch_run(nlse_batch* b, int max_steps) {
     BTRY(cudaMallocHost(&b->h_tiles, sizeof(BTile) * cap));
     b->tiles_cap = cap;
   }
-  const size_t passes = (size_t)(steps[0] > steps[1] ? steps[0] : steps[1]) * 8;
+  const size_t passes = (size_t)max_adv * 8;
   if (passes > b->qctr_cap) {
     if (b->d_qctr) cudaFree(b->d_qctr);
     b->d_qctr = nullptr;
     BTRY(cudaMalloc(&b->d_qctr, sizeof(unsigned) * passes));
     b->qctr_cap = passes;
   }
-  // solve table and tile lists (class 0 tiles, then class 1 tiles)
+  // solve table and tile lists (class 0 tiles, then class 1, then class 2)
   int nsolves = 0;
   long long tt = 0;
-  for (int c = 0; c < 2; ++c)
+  for (int c = 0; c < NC; ++c)
     for (int id : which[c]) {
       Slot& S = b->slots[id];
       b->h_solves[nsolves] = S.d;
@@ -735,7 +370,7 @@ extern "C" int nlse_batch_run(nlse_batch* b, int max_steps) {
                        b->stream));
   long long budget = 100000000000LL;  // clock cycles a CTA may wait at one barrier
   long long first = 0;
-  for (int c = 0; c < 2; ++c) {
+  for (int c = 0; c < NC; ++c) {
     if (which[c].empty() || steps[c] == 0) {
       first += ntiles[c];
       continue;
@@ -745,21 +380,25 @@ extern "C" int nlse_batch_run(nlse_batch* b, int max_steps) {
     BTRY(cudaMemsetAsync(b->d_bar, 0, sizeof(BarrierState), b->stream));
     bool staged = c == 1;  // every solve of the class in segment / rectangle tiles
     for (int id : which[c]) staged = staged && tile_kind(b->slots[id].d) != K_LINEAR;
-    int blocks = b->max_blocks[staged ? 2 : c];
+    int blocks = b->max_blocks[c == 2 ? 3 : staged ? 2 : c];
     if ((long long)blocks > ntiles[c]) blocks = (int)ntiles[c];
     const BTile* tiles = b->d_tiles + first;
     int nt_i = (int)ntiles[c], ntd_i = (int)ntiles_d[c], st_i = steps[c];
     void* args[] = {(void*)&b->d_solves, (void*)&tiles, &nt_i, &ntd_i, &st_i,
                     (void*)&b->d_qctr, (void*)&b->d_bar, (void*)&b->d_err, &budget};
-    const void* kern = c == 0   ? (const void*)batch_kernel<NLSE_PREC_DOUBLE, false>
-                       : staged ? (const void*)batch_kernel<NLSE_PREC_MIXED, true>
-                                : (const void*)batch_kernel<NLSE_PREC_MIXED, false>;
-    BTRY(cudaLaunchCooperativeKernel(kern, dim3(blocks), dim3(BT), args, 0, b->stream));
+    if (c == 2) {
+      BTRY(nlse::batch_fma_launch((unsigned)blocks, args, b->stream));
+    } else {
+      const void* kern = c == 0   ? (const void*)batch_kernel<NLSE_PREC_DOUBLE, false>
+                         : staged ? (const void*)batch_kernel<NLSE_PREC_MIXED, true>
+                                  : (const void*)batch_kernel<NLSE_PREC_MIXED, false>;
+      BTRY(cudaLaunchCooperativeKernel(kern, dim3(blocks), dim3(BT), args, 0, b->stream));
+    }
     ++b->last_launches;
     first += ntiles[c];
   }
   // host bookkeeping of the steps each solve advanced in these launches
-  for (int c = 0; c < 2; ++c)
+  for (int c = 0; c < NC; ++c)
     for (int id : which[c]) {
       Slot& S = b->slots[id];
       long long adv = S.d.steps_left < steps[c] ? S.d.steps_left : steps[c];

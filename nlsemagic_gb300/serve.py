@@ -23,9 +23,9 @@ blocking:
    nearly idle, a mixed solve by HBM bandwidth (``per_class=False``: one
    large solve at a time).
 
-With ``fp64_fma`` (default) the large FP64 solves run the contracted FP64
-kernels (NLSE_FLAG_FMA); the batched launch computes FP64 without
-contraction.
+With ``fp64_fma`` (default) the FP64 solves run the contracted FP64
+kernels (NLSE_FLAG_FMA): the large ones on their solver, the small ones in
+the batched launch's contracted FP64 class.
 
 Work is estimated as points x steps, times ``fp64_cost`` for the FP64 class
 (about its speed ratio to the mixed class).  Waiting requests are admitted
@@ -94,8 +94,8 @@ def summarize(done, wall, busy=None, launches=None, rejected=0):
 
 
 def solve_flags(inst, fp64_fma):
-    """Problem flags of a request run on its own Solver: the MSD guard, and
-    for FP64 requests with fp64_fma the contracted FP64 kernels
+    """Problem flags of a request, on its own Solver or in the batch: the MSD
+    guard, and for FP64 requests with fp64_fma the contracted FP64 kernels
     (NLSE_FLAG_FMA: within 1e-12 of the reference's bits, fewer FP64
     instructions)."""
     fma = fp64_fma and inst.precision == PREC_DOUBLE
@@ -198,7 +198,7 @@ class Server:
                         continue
                     try:
                         slot = b.add(i.U, i.V, i.s, i.a, i.h * i.h, i.BC, i.steps, i.k, i.method,
-                                     i.precision)
+                                     i.precision, flags=solve_flags(i, self.fp64_fma))
                     except NLSEError as e:
                         if e.code != NLSE_ERR_CAPACITY:
                             raise

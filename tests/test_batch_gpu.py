@@ -1,6 +1,7 @@
 """Batched persistent launch: many uneven solves in one launch.
 
-* FP64 solves in a batch are bit-identical to the C oracle.
+* FP64 solves in a batch are bit-identical to the C oracle; those added with
+  NLSE_FLAG_FMA (contracted kernel copy) are within 1e-12 of it.
 * A solve's result is identical alone and in a mixed batch (bitwise: solves
   never interact), and mixed-precision results are within the mixed
   tolerance of the FP64 oracle.
@@ -211,14 +212,54 @@ def test_mixed_batch_tile_edges(gpu_lib, method, BC):
     b.close()
 
 
-def test_batch_rejects_contracted_fp64(gpu_lib):
-    # the batched launch computes FP64 without contraction only
+def test_batch_contracted_fp64_class(gpu_lib, cases):
+    # FP64 solves added with NLSE_FLAG_FMA run on the contracted copy of the
+    # batch kernel, a third launch beside the exact FP64 and mixed ones:
+    # within 1e-12 of the oracle, each the same alone and in the mix, and the
+    # exact FP64 solves of the same batch still bit-identical
+    import nlsemagic_gb300 as ng
+    fma = ng.FLAG_MSD_GUARD | ng.FLAG_FMA
+    steps = 30
+    alone = []
+    for c in cases:
+        b = ng.Batch(1 << 26)
+        sl = b.add(c["U"], c["V"], c["s"], c["a"], c["h2"], c["BC"], steps, c["k"], c["method"],
+                   ng.PREC_DOUBLE, flags=fma)
+        b.run(steps)
+        alone.append(b.download(sl))
+        b.close()
+    b = ng.Batch(1 << 28)
+    slots = []
+    for c in cases:
+        slots.append(("fma", b.add(c["U"], c["V"], c["s"], c["a"], c["h2"], c["BC"], steps,
+                                   c["k"], c["method"], ng.PREC_DOUBLE, flags=fma)))
+        slots.append(("exact", b.add(c["U"], c["V"], c["s"], c["a"], c["h2"], c["BC"], steps,
+                                     c["k"], c["method"], ng.PREC_DOUBLE)))
+        slots.append(("mixed", b.add(c["U"], c["V"], c["s"], c["a"], c["h2"], c["BC"], steps,
+                                     c["k"], c["method"], ng.PREC_MIXED)))
+    b.run(steps)
+    b.sync()
+    assert b.last_launches == 3
+    for t, c in enumerate(cases):
+        ref = oracle_run(c, steps)
+        got = {kind: b.download(sl) for kind, sl in slots[3 * t:3 * t + 3]}
+        assert bits_equal(got["exact"], ref)
+        assert bits_equal(got["fma"], alone[t])
+        err = np.linalg.norm((got["fma"] - ref).ravel()) / np.linalg.norm(ref.ravel())
+        assert err <= 1e-12, err
+        err = np.linalg.norm((got["mixed"] - ref).ravel()) / np.linalg.norm(ref.ravel())
+        assert err <= MIXED_TOL, err
+    b.close()
+
+
+def test_batch_rejects_contracted_mixed(gpu_lib):
+    # NLSE_FLAG_FMA selects a form of the FP64 class only
     import nlsemagic_gb300 as ng
     U = np.ones(64, complex)
     b = ng.Batch(1 << 24)
     try:
         with pytest.raises(ng.NLSEError) as e:
-            b.add(U, np.zeros(64), -1.0, 1.0, 0.01, 1, 4, 1e-3, 1, ng.PREC_DOUBLE,
+            b.add(U, np.zeros(64), -1.0, 1.0, 0.01, 1, 4, 1e-3, 1, ng.PREC_MIXED,
                   flags=ng.FLAG_MSD_GUARD | ng.FLAG_FMA)
         assert e.value.code == ng._lib.NLSE_ERR_ARG
     finally:

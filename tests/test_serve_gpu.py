@@ -25,7 +25,7 @@ def small_stream(count=30, rate=400.0):
 
 def test_serving_results_equal_alone(gpu_lib):
     import nlsemagic_gb300 as ng
-    from nlsemagic_gb300.serve import Server
+    from nlsemagic_gb300.serve import Server, solve_flags
     reqs = small_stream()
     srv = Server(pool_bytes=1 << 28, chunk_steps=16, keep_snapshots=True)
     summary, done = srv.serve(reqs)
@@ -36,7 +36,8 @@ def test_serving_results_equal_alone(gpu_lib):
     for r in reqs[:12]:
         i = r.inst
         b = ng.Batch(1 << 26)
-        sl = b.add(i.U, i.V, i.s, i.a, i.h * i.h, i.BC, i.steps, i.k, i.method, i.precision)
+        sl = b.add(i.U, i.V, i.s, i.a, i.h * i.h, i.BC, i.steps, i.k, i.method, i.precision,
+                   flags=solve_flags(i, srv.fp64_fma))
         b.run(i.steps)
         assert bits_equal(by_id[r.rid].snapshot, b.download(sl))
         b.close()
@@ -75,9 +76,10 @@ def test_serving_solo_and_batched_results_equal_alone(gpu_lib):
             want = ng.take_steps(i.U, i.V, i.s, i.a, i.h * i.h, i.BC, i.steps, i.k,
                                  method=i.method, precision=i.precision,
                                  flags=solve_flags(i, srv.fp64_fma))
-        else:
+        else:  # small FP64 solves take the batch kernel's contracted copy
             b = ng.Batch(1 << 26)
-            sl = b.add(i.U, i.V, i.s, i.a, i.h * i.h, i.BC, i.steps, i.k, i.method, i.precision)
+            sl = b.add(i.U, i.V, i.s, i.a, i.h * i.h, i.BC, i.steps, i.k, i.method, i.precision,
+                       flags=solve_flags(i, srv.fp64_fma))
             b.run(i.steps)
             want = b.download(sl)
             b.close()
