@@ -281,6 +281,10 @@ int nlse_take_steps_noalloc(const nlse_problem *p, const double *dUr, const doub
  *                  finish; 0: plain stream order.  Same bits either way.
  *   "face.blocks_per_sm"  blocks of 256 threads per SM of the 3D face
  *                  kernels (1-64, default 8; grid-stride beyond).
+ *   "wide.strips"  1 (default): mixed-precision 3D 2SHOC solvers keep the x
+ *                  faces' own lo, K and V in face-indexed arrays that the
+ *                  face kernel reads instead of the strided x faces; 0: the
+ *                  full arrays.  Same bits.
  *   "small1d.max_points"  FP32 and mixed 1D solves of at most this many
  *                  points (default 2048, 0 = never, at most 65536) run each
  *                  chunk in single-block launches instead of a launch per

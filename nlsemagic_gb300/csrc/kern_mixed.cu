@@ -14,6 +14,9 @@ int g_pdl = 1;  // 3D 2SHOC stage kernels launched with PDL
 // room for the next interior kernel's tiles under PDL: 22.1 Gpt-steps/s at
 // 320^3 against 21.7 with 16 (and 20.3 with 1, 22.0 with 4).
 int g_face_bps = 8;
+// 3D 2SHOC: x-face strips (the x faces' own lo, K, V, face-indexed) for the
+// face kernel
+int g_strips = 1;
 int g_tile_order = 1;
 // 3D 2SHOC interior kernel (TMA staging): two planes per iteration.  Same
 // bits as one plane; 23.6 Gpt-steps/s at 320^3 against 21.9.
@@ -78,6 +81,34 @@ static cudaError_t by_bc(const Geom& g, int BC, const Consts<float>& c, const Mi
 
 static bool wide_path(const Geom& g, int BC, int kernel_kind) {
   return kernel_kind == KERNEL_TILED && g.ndim == 3 && tiled_supported(g, 3) && BC != 4;
+}
+
+bool mixed_strip_path(const Geom& g, int method, int BC, int kernel_kind) {
+  return wide::g_strips && method == 2 && wide_path(g, BC, kernel_kind);
+}
+
+// x-face strips of lo and V, from the full arrays
+__global__ void strip_fill_k(Geom g, const float2* __restrict__ lo, const float* __restrict__ V,
+                             float2* slo, float* sV) {
+  const long long per = (long long)g.N * g.L, n = 2 * per;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int side = (int)(i / per);
+    const long long yz = i - side * per;
+    const int z = (int)(yz / g.N), y = (int)(yz - (long long)z * g.N);
+    const long long p = ((long long)z * g.N + y) * g.M + (side ? g.M - 1 : 0);
+    slo[i] = lo[p];
+    sV[i] = V[p];
+  }
+}
+
+cudaError_t mixed_strip_fill(const Geom& g, const float2* lo, const float* V, float2* slo,
+                             float* sV, cudaStream_t st) {
+  const long long n = xstrip_entries(g);
+  long long b = (n + 255) / 256;
+  if (b > 4096) b = 4096;
+  strip_fill_k<<<(unsigned)(b < 1 ? 1 : b), 256, 0, st>>>(g, lo, V, slo, sV);
+  return cudaGetLastError();
 }
 
 int mixed_stage_launches(const Geom& g, int method, int BC, int kernel_kind, bool has_dsc) {

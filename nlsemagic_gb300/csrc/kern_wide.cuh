@@ -1006,6 +1006,62 @@ __global__ void __launch_bounds__(256, 8) face2shoc(Geom g, Args A, const ShellM
   }
 }
 
+// x-face strips (MixedStageArgs::s_*): the entry of (y, z) on side 0
+// (x = 0) or 1 (x = M-1)
+__host__ __device__ __forceinline__ long long xsi(const Geom& g, int side, int y, int z) {
+  return ((long long)side * g.L + z) * g.N + y;
+}
+
+// face2shoc with x-face strips.  An x face is strided in memory: each of a
+// point's loads there is a 32-byte sector of its own.  The point's own lo,
+// K and V -- which only the face kernels and the state's ingest write --
+// live in the strips (contiguous), so of face2shoc's six sectors per x-face
+// point three remain (hi and E at the point and its neighbour, one sector
+// each, and F there); K at the x faces is kept in the strip only.  The
+// other face points as face2shoc.  40 registers (6 CTAs per SM): at 32 it
+// spills.
+template <int BC>
+__global__ void __launch_bounds__(256, 6) face2shoc_x(Geom g, Args A, const ShellMap<1> sm) {
+  pdl_wait();
+  pdl_trigger();
+  const int stage = A.stage;
+  const float2* Ein = stage == 1 ? A.a.lo_in : A.a.e_in;
+  mixed::YIn Y{A.a.hi_in, Ein};
+  const long long xpart = sm.nz + sm.ny;  // the x faces' points: [xpart, total)
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < sm.total;
+       t += (long long)gridDim.x * blockDim.x) {
+    int x, y, z;
+    shell_coord(sm, t, x, y, z);
+    const bool xf = t >= xpart;
+    const long long p = lin(g, z, y, x);
+    const long long si = xf ? xsi(g, x == 0 ? 0 : 1, y, z) : 0;
+    int qi, qj, qk;
+    msd_coords(g, z, y, x, qi, qj, qk);
+    const long long q = lin(g, qi, qj, qk);
+    const mixed::HE ub = Y.at(p), uq = Y.at(q);
+    const float2 fq = BC == 2 ? A.a.fq[q] : make_float2(0.f, 0.f);
+    const float v = xf ? A.a.s_V[si] : A.a.V[p];
+    const float2 lo = stage == 1 ? ub.e : (xf ? A.a.s_lo_in[si] : A.a.lo_in[p]);
+    const float2 kv = stage == 4 ? (xf ? A.a.s_K[si] : A.a.K[p]) : lo;
+    const float2 T = mixed::f_boundary<2, BC>(A.c, ub, v, uq, fq, nullptr);
+    float2 eo, ko, ho, lo2;
+    mixed::stage_update(A.c, stage, T, ub.h, lo, ub.e, kv, eo, ko, ho, lo2);
+    if (stage == 2) {
+      if (xf)
+        A.a.s_K[si] = ko;
+      else
+        A.a.K[p] = ko;
+    }
+    if (stage < 4) {
+      A.a.e_out[p] = eo;
+    } else {
+      A.a.hi_out[p] = ho;
+      A.a.lo_out[p] = lo2;
+      if (xf) A.a.s_lo_out[si] = lo2;
+    }
+  }
+}
+
 // ---- launch --------------------------------------------------------------------
 extern int g_zc_override;  // autotuner hook (0: chosen by default_zc)
 
@@ -1187,6 +1243,8 @@ cudaError_t launch(const Geom& g, const Args& A, cudaStream_t st) {
                         : launch_inner_stage<METHOD, false>(g, A, st, m0, m1);
     if (e != cudaSuccess) return e;
   }
+  if (METHOD == 2 && A.a.s_V)
+    return launch_k(face2shoc_x<BC>, dim3(nb), dim3(256), 0, st, g_pdl != 0, g, A, faces);
   if (METHOD == 2) return launch_k(face2shoc<BC>, dim3(nb), dim3(256), 0, st, g_pdl != 0, g, A, faces);
   shell3d<METHOD, BC><<<nb, 256, 0, st>>>(g, A, faces);
   return cudaGetLastError();

@@ -62,6 +62,7 @@ extern int g_z2;
 extern int g_wide_ty;
 extern int g_wide2d;
 extern int g_seg1d;
+extern int g_strips;
 }
 namespace wide2d {
 extern int g_ty;
@@ -132,6 +133,11 @@ extern "C" int nlse_tune_set(const char* key, long long value) {
     nlse::wide::g_pdl = (int)value;
     return NLSE_OK;
   }
+  if (!strcmp(key, "wide.strips")) {
+    if (value != 0 && value != 1) return fail(NLSE_ERR_ARG, "wide.strips must be 0 or 1");
+    nlse::wide::g_strips = (int)value;
+    return NLSE_OK;
+  }
   if (!strcmp(key, "small1d.max_points")) {
     if (value < 0 || value > 65536) return fail(NLSE_ERR_ARG, "small1d.max_points out of range");
     g_small1d_max = value;
@@ -185,6 +191,10 @@ extern "C" int nlse_tune_get(const char* key, long long* value) {
   }
   if (!strcmp(key, "wide.pdl")) {
     *value = nlse::wide::g_pdl;
+    return NLSE_OK;
+  }
+  if (!strcmp(key, "wide.strips")) {
+    *value = nlse::wide::g_strips;
     return NLSE_OK;
   }
   if (!strcmp(key, "small1d.max_points")) {
@@ -356,6 +366,11 @@ struct nlse_solver {
   float4* gh;
   float* Vf;
   int cur;
+  // x-face strips of lo (by parity), K and V (3D 2SHOC,
+  // mixed_strip_path); fresh: lo and V there match the full arrays
+  float2 *s_lo[2], *s_K;
+  float* s_V;
+  bool strips_fresh;
   // device staging for planar transfers: re, im, V (n doubles each)
   double* stage;
   double* vort;  // vorticity scratch (3 n doubles), allocated on first use
@@ -402,7 +417,7 @@ extern "C" int nlse_solver_destroy(nlse_solver* s) {
   free_graphs(s);
   void* ptrs[] = {s->psi, s->K, s->ya, s->yb, s->V, s->hi[0], s->hi[1], s->lo[0], s->lo[1],
                   s->mK, s->da, s->db, s->dc, s->fq, s->gh, s->Vf, s->stage, s->d_mass, s->d_bad,
-                  s->dsc, s->vort, s->d_diag};
+                  s->dsc, s->vort, s->d_diag, s->s_lo[0], s->s_lo[1], s->s_K, s->s_V};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -463,6 +478,13 @@ extern "C" int nlse_solver_create(const nlse_problem* p, nlse_solver** out) {
     const long long ng = mixed_ghost_entries(s->g, p->method, p->bc, s->kernel_kind);
     const long long nf = mixed_fq_entries(s->g, p->method, p->bc, s->kernel_kind);
     if (!r && ng) r = dalloc(s, (void**)&s->gh, sizeof(float4) * ng);
+    if (!r && ng && p->method == 2 && s->g.ndim == 3) {  // x-face strips
+      const size_t sb = sizeof(float2) * (size_t)xstrip_entries(s->g);
+      float2** sp[] = {&s->s_lo[0], &s->s_lo[1], &s->s_K};
+      for (float2** q : sp)
+        if (!r) r = dalloc(s, (void**)q, sb);
+      if (!r) r = dalloc(s, (void**)&s->s_V, sizeof(float) * (size_t)xstrip_entries(s->g));
+    }
     if (!r && nf) r = dalloc(s, (void**)&s->fq, sizeof(float2) * nf);
     const long long nd = mixed_dsc_entries(s->g, p->method, p->bc, s->kernel_kind);
     if (!r && nd) r = dalloc(s, &s->dsc, sizeof(float2) * nd);
@@ -501,9 +523,30 @@ static int ingest(nlse_solver* s, const double* re, const double* im, const doub
     default:
       CUDA_TRY(planar_to_hilo(re, im, s->hi[s->cur], s->lo[s->cur], n, s->stream));
       if (V) CUDA_TRY(real_to_float(V, s->Vf, n, s->stream));
+      s->strips_fresh = false;  // refilled before the next stage launch
       break;
   }
   return NLSE_OK;
+}
+
+// Whether the stage launches keep x-face strips now; refills them from the
+// state first where they may be stale (a new state, or steps run without
+// them).
+static int strips_ready(nlse_solver* s) {
+  const nlse_problem& p = s->prob;
+  const bool on =
+      s->s_V && p.precision == NLSE_PREC_MIXED && mixed_strip_path(s->g, p.method, p.bc, s->kernel_kind);
+  if (!on) {
+    s->strips_fresh = false;
+    return 0;
+  }
+  if (!s->strips_fresh) {
+    cudaError_t e =
+        mixed_strip_fill(s->g, s->lo[s->cur], s->Vf, s->s_lo[s->cur], s->s_V, s->stream);
+    if (e != cudaSuccess) return -1;
+    s->strips_fresh = true;
+  }
+  return 1;
 }
 
 extern "C" int nlse_solver_upload_device(nlse_solver* s, const double* dUr, const double* dUi,
@@ -642,6 +685,17 @@ static int enqueue_step(nlse_solver* s) {
     MixedStageArgs a3{s->hi[c], s->lo[c], s->db, s->Vf, s->mK, s->dc, nullptr, nullptr, G, F, D};
     MixedStageArgs a4{s->hi[c], s->lo[c], s->dc, s->Vf, s->mK, nullptr, s->hi[1 - c], s->lo[1 - c],
                       G, F, D};
+    const int sr = strips_ready(s);
+    if (sr < 0) return fail(NLSE_ERR_CUDA, "x-face strip refill failed");
+    if (sr) {  // the strips of each stage's arrays
+      MixedStageArgs* am[4] = {&a1, &a2, &a3, &a4};
+      for (int t = 0; t < 4; ++t) {
+        am[t]->s_lo_in = s->s_lo[c];
+        am[t]->s_K = s->s_K;
+        am[t]->s_V = s->s_V;
+      }
+      a4.s_lo_out = s->s_lo[1 - c];
+    }
     const MixedStageArgs* as[4] = {&a1, &a2, &a3, &a4};
     for (int st = 1; st <= 4 && e == cudaSuccess; ++st)
       e = launch_mixed_stage(s->g, p.method, p.bc, s->cf, *as[st - 1], st, s->stream,
@@ -712,6 +766,13 @@ extern "C" int nlse_solver_run(nlse_solver* s, long long nsteps) {
   if (s->g.ndim == 1 && s->g.n <= g_small1d_max && s->prob.precision != NLSE_PREC_DOUBLE &&
       (s->prob.method == 1 || s->dsc) && nsteps > 0)
     return run_small1d(s, nsteps);
+  // 3D 2SHOC mixed with x-face strips: filled (where stale) before the
+  // steps, outside any graph
+  int sr = 0;
+  if (s->prob.precision == NLSE_PREC_MIXED) {
+    sr = strips_ready(s);
+    if (sr < 0) return fail(NLSE_ERR_CUDA, "x-face strip refill failed");
+  }
   const int G = s->graph_steps;
   if (G > 0 && nsteps >= G) {
     long long reps = nsteps / G;

@@ -35,7 +35,23 @@ struct MixedStageArgs {
   float4* gh;          // ghost values (hi, E) one cell outside each face, mixed_ghost_entries()
   float2* fq;          // F at the points next to a face (n entries, MSD only)
   float2* dsc;         // 2SHOC on the gather path: D scratch (n points), or null
+  // 3D 2SHOC on the tiled path: x-face strips (null: not kept).  The x
+  // faces' own lo, K and V in face-indexed order, [side][z][y], which the
+  // face kernel reads and writes there instead of the full arrays' strided
+  // x faces (K at the x faces is kept in the strip only).
+  const float2* s_lo_in;
+  float2 *s_lo_out, *s_K;
+  const float* s_V;
 };
+
+// Entries of one x-face strip array: 2 sides x N x L.
+inline long long xstrip_entries(const Geom& g) { return 2LL * g.N * g.L; }
+// Whether a grid keeps x-face strips (the knob wide.strips), and their
+// refill from the state's lo and V.
+bool mixed_strip_path(const Geom& g, int method, int BC, int kernel_kind);
+cudaError_t mixed_strip_fill(const Geom& g, const float2* lo, const float* V, float2* slo,
+                             float* sV, cudaStream_t st);
+
 
 template <typename R>
 cudaError_t launch_exact_stage(const Geom& g, int method, int BC, const Consts<R>& c,
