@@ -87,9 +87,9 @@ bool mixed_strip_path(const Geom& g, int method, int BC, int kernel_kind) {
   return wide::g_strips && method == 2 && wide_path(g, BC, kernel_kind);
 }
 
-// x-face strips of lo and V, from the full arrays
+// x-face strips of lo and V, and V next to the faces, from the full arrays
 __global__ void strip_fill_k(Geom g, const float2* __restrict__ lo, const float* __restrict__ V,
-                             float2* slo, float* sV) {
+                             float2* slo, float* sV, float* sVq) {
   const long long per = (long long)g.N * g.L, n = 2 * per;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
@@ -99,15 +99,16 @@ __global__ void strip_fill_k(Geom g, const float2* __restrict__ lo, const float*
     const long long p = ((long long)z * g.N + y) * g.M + (side ? g.M - 1 : 0);
     slo[i] = lo[p];
     sV[i] = V[p];
+    sVq[i] = V[side ? p - 1 : p + 1];
   }
 }
 
 cudaError_t mixed_strip_fill(const Geom& g, const float2* lo, const float* V, float2* slo,
-                             float* sV, cudaStream_t st) {
+                             float* sV, float* sVq, cudaStream_t st) {
   const long long n = xstrip_entries(g);
   long long b = (n + 255) / 256;
   if (b > 4096) b = 4096;
-  strip_fill_k<<<(unsigned)(b < 1 ? 1 : b), 256, 0, st>>>(g, lo, V, slo, sV);
+  strip_fill_k<<<(unsigned)(b < 1 ? 1 : b), 256, 0, st>>>(g, lo, V, slo, sV, sVq);
   return cudaGetLastError();
 }
 

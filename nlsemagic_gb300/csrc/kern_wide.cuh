@@ -924,8 +924,17 @@ __global__ void __launch_bounds__(256) ghost3d(Geom g, Args A, const ShellMap<1>
                         at(zz - 1, rr, cb)};
       const int y = ya + ly, z = za + lz;
       const long long pb = ((long long)z * N + y) * M + (side ? M - 1 : 0);
+      float vb, vq;  // V at the face point and its neighbour: strips, if kept
+      if (A.a.s_V) {
+        const long long si = ((long long)side * L + z) * N + y;
+        vb = A.a.s_V[si];
+        vq = A.a.s_Vq[si];
+      } else {
+        vb = A.a.V[pb];
+        vq = A.a.V[pb + dn];
+      }
       A.a.gh[(side ? gl.xhi : gl.xlo) + y + (long long)N * z] =
-          ghost_value<BC>(A.c, ub, A.a.V[pb], uq, A.a.V[pb + dn], nq, tn);
+          ghost_value<BC>(A.c, ub, vb, uq, vq, nq, tn);
     }
     return;
   }

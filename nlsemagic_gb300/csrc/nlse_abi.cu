@@ -369,7 +369,7 @@ struct nlse_solver {
   // x-face strips of lo (by parity), K and V (3D 2SHOC,
   // mixed_strip_path); fresh: lo and V there match the full arrays
   float2 *s_lo[2], *s_K;
-  float* s_V;
+  float *s_V, *s_Vq;
   bool strips_fresh;
   // device staging for planar transfers: re, im, V (n doubles each)
   double* stage;
@@ -417,7 +417,7 @@ extern "C" int nlse_solver_destroy(nlse_solver* s) {
   free_graphs(s);
   void* ptrs[] = {s->psi, s->K, s->ya, s->yb, s->V, s->hi[0], s->hi[1], s->lo[0], s->lo[1],
                   s->mK, s->da, s->db, s->dc, s->fq, s->gh, s->Vf, s->stage, s->d_mass, s->d_bad,
-                  s->dsc, s->vort, s->d_diag, s->s_lo[0], s->s_lo[1], s->s_K, s->s_V};
+                  s->dsc, s->vort, s->d_diag, s->s_lo[0], s->s_lo[1], s->s_K, s->s_V, s->s_Vq};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -484,6 +484,7 @@ extern "C" int nlse_solver_create(const nlse_problem* p, nlse_solver** out) {
       for (float2** q : sp)
         if (!r) r = dalloc(s, (void**)q, sb);
       if (!r) r = dalloc(s, (void**)&s->s_V, sizeof(float) * (size_t)xstrip_entries(s->g));
+      if (!r) r = dalloc(s, (void**)&s->s_Vq, sizeof(float) * (size_t)xstrip_entries(s->g));
     }
     if (!r && nf) r = dalloc(s, (void**)&s->fq, sizeof(float2) * nf);
     const long long nd = mixed_dsc_entries(s->g, p->method, p->bc, s->kernel_kind);
@@ -542,7 +543,7 @@ static int strips_ready(nlse_solver* s) {
   }
   if (!s->strips_fresh) {
     cudaError_t e =
-        mixed_strip_fill(s->g, s->lo[s->cur], s->Vf, s->s_lo[s->cur], s->s_V, s->stream);
+        mixed_strip_fill(s->g, s->lo[s->cur], s->Vf, s->s_lo[s->cur], s->s_V, s->s_Vq, s->stream);
     if (e != cudaSuccess) return -1;
     s->strips_fresh = true;
   }
@@ -693,6 +694,7 @@ static int enqueue_step(nlse_solver* s) {
         am[t]->s_lo_in = s->s_lo[c];
         am[t]->s_K = s->s_K;
         am[t]->s_V = s->s_V;
+        am[t]->s_Vq = s->s_Vq;
       }
       a4.s_lo_out = s->s_lo[1 - c];
     }

@@ -38,10 +38,11 @@ struct MixedStageArgs {
   // 3D 2SHOC on the tiled path: x-face strips (null: not kept).  The x
   // faces' own lo, K and V in face-indexed order, [side][z][y], which the
   // face kernel reads and writes there instead of the full arrays' strided
-  // x faces (K at the x faces is kept in the strip only).
+  // x faces (K at the x faces is kept in the strip only), and V at the
+  // points next to them (s_Vq, for the ghost kernel).
   const float2* s_lo_in;
   float2 *s_lo_out, *s_K;
-  const float* s_V;
+  const float *s_V, *s_Vq;
 };
 
 // Entries of one x-face strip array: 2 sides x N x L.
@@ -50,7 +51,7 @@ inline long long xstrip_entries(const Geom& g) { return 2LL * g.N * g.L; }
 // refill from the state's lo and V.
 bool mixed_strip_path(const Geom& g, int method, int BC, int kernel_kind);
 cudaError_t mixed_strip_fill(const Geom& g, const float2* lo, const float* V, float2* slo,
-                             float* sV, cudaStream_t st);
+                             float* sV, float* sVq, cudaStream_t st);
 
 
 template <typename R>
