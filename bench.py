@@ -459,7 +459,11 @@ def run_gpu(args, w):
     peak, peak_kind = peaks()
     achieved = value * BYTES_MODEL_MIXED / world  # GB/s per GPU (Gpt/s * B)
     traffic_ppt = read_traffic()
-    launches_per_job = steps * solver.launches_per_step + 2  # + 2 ingest conversions
+    # + 2 ingest conversions, + 1 refill of the x-face strips (3D 2SHOC) after
+    # each upload
+    from nlsemagic_gb300 import autotune as _at
+    strips = w.U.ndim == 3 and w.method == 2 and _at.get_knob("wide.strips") == 1
+    launches_per_job = steps * solver.launches_per_step + 2 + (1 if strips else 0)
     roof = {
         "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
         "frac": achieved / peak,
