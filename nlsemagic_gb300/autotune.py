@@ -15,9 +15,11 @@ knobs and keeps the fastest:
 * ``wide2d.ty``    tile height of the mixed-precision 2D stage kernel (8, 16
                    or 32 rows: CTAs in flight against halo re-reads).
 
-The library has one more knob, ``wide.pdl`` (1 by default: the 3D 2SHOC
-stage kernels overlap through programmatic dependent launch; 0: plain stream
-order).  Both give the same bits; it is not tuned here.
+The library has more knobs that give the same bits either way and are not
+tuned here, among them ``wide.pdl`` (1 by default: the 3D 2SHOC stage
+kernels are launched with programmatic dependent launch; 0: plain stream
+order) and ``wide.strips`` (1 by default: the 3D 2SHOC face kernels take the
+x faces' own lo, K and V from face-indexed arrays).
 
 Results are cached in a JSON file (``$NLSE_TUNE_CACHE`` or
 ``~/.cache/nlse_gb300/tune.json``) keyed by device name and problem class;
