@@ -849,9 +849,11 @@ extern "C" long long nlse_solver_bytes_for(const nlse_problem* p) {
     b = 4 * 2 * es * n + es * n +
         2 * es * exact_dsc_entries(g, p->method, p->bc, kind, p->precision == NLSE_PREC_SINGLE);
   } else {
-    b = 8 * 8 * n + 4 * n + 16 * mixed_ghost_entries(g, p->method, p->bc, kind) +
-        8 * mixed_fq_entries(g, p->method, p->bc, kind) +
+    const long long ng = mixed_ghost_entries(g, p->method, p->bc, kind);
+    b = 8 * 8 * n + 4 * n + 16 * ng + 8 * mixed_fq_entries(g, p->method, p->bc, kind) +
         8 * mixed_dsc_entries(g, p->method, p->bc, kind);
+    // x-face strips: lo (2 parities) and K (float2), V and V next to the face
+    if (ng && p->method == 2 && g.ndim == 3) b += (3 * 8 + 2 * 4) * xstrip_entries(g);
   }
   return b + (long long)sizeof(double) + (long long)sizeof(int) + 3 * 8 * n;
 }

@@ -95,6 +95,19 @@ def test_single_pass_2d_needs_no_d_scratch(lib):
         autotune.set_knob("wide2d", old)
 
 
+def test_bytes_for_counts_the_x_face_strips(lib):
+    # a 3D 2SHOC mixed solver keeps five face-indexed strip arrays of 2 N L
+    # entries (lo twice and K as float2, V twice as float); the estimate the
+    # serving loop admits by includes them
+    shape = (40, 30, 20)
+    M, N, L = shape
+    mixed = ng.Solver.bytes_for(shape, method=2, precision=ng.PREC_MIXED, BC=2)
+    cd = ng.Solver.bytes_for(shape, method=1, precision=ng.PREC_MIXED, BC=2)
+    n = M * N * L
+    ghosts = mixed - cd - 8 * n - (3 * 8 + 2 * 4) * 2 * N * L  # ghost and F scratch remain
+    assert ghosts > 0 and ghosts % 16 == 0, (mixed, cd)
+
+
 def test_autotune_candidates_per_class():
     from nlsemagic_gb300 import autotune
     two = autotune.candidates((256, 256), 3)
